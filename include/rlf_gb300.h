@@ -1,0 +1,83 @@
+/*
+ * Batched and device-resident API of the GB300 shape-measurement library (librlf_gb300.so).
+ * These entry points have no counterpart in the reference: they replace the per-galaxy loop of
+ * data_processing.c:61-138 by a pipeline that keeps the observation in GPU memory and fits many
+ * galaxies concurrently.  Plain C types only.
+ */
+#ifndef RLF_GB300_H
+#define RLF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { RLF_F64 = 0, RLF_MIXED = 1 };
+
+/* per-galaxy result: the outputs of source_fitting (galaxy_fitting.c:41-117) plus counters */
+typedef struct {
+  double e1, e2, var_e1, var_e2, oneDimvar, maxL;
+  int error;         /* 1 = bad measurement (the reference's bad list) */
+  int iters;         /* simplex iterations */
+  int nevals;        /* likelihood evaluations */
+  int newton_iters;  /* Newton iterations over all nodes and evaluations */
+  int status;        /* 0, or device-side limits reached (2: QAG intervals, 4: bad simplex start) */
+  int ncoords;       /* facet cells */
+} rlf_fit_result;
+
+typedef struct {
+  int precision;     /* RLF_F64 (reference arithmetic) or RLF_MIXED */
+  int batch;         /* galaxies extracted/fitted/removed together; 1 = the reference's order */
+  int gaussian;      /* 0 exponential profile (default), 1 Gaussian (the -DGAUSSIAN build) */
+  int refit;         /* rlf_obs_process: 1 = run the re-fit pass over bad galaxies */
+  int verbose;
+  const double *start;  /* optional [n_gal*3] simplex start (e1, e2, step); NULL = (0, 0, 0.1) */
+} rlf_options;
+
+/* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
+ * Defaults: RLF_F64, batch 1, exponential profile. Returns 0. */
+int rlf_configure(const rlf_options *opt);
+const char *rlf_version(void);
+int rlf_device_count(void);
+
+/* -------- device-resident observation -------- */
+typedef struct rlf_observation rlf_observation;
+
+/* Upload an observation.  uu/vv/ww: [n_rows] metres; wavenumbers/spec: [n_ch];
+ * sigma2/flag: [n_ch * n_rows] channel-major (the reference's layout), flag may be NULL.
+ * len: facet half-extent in wavelengths (RadioLensfit2.cpp:406).  Returns NULL on error. */
+rlf_observation *rlf_obs_create(int n_rows, int n_ch, const double *uu, const double *vv,
+                                const double *ww, const double *wavenumbers, const double *spec,
+                                double len, const float *sigma2, const uint8_t *flag,
+                                int precision);
+void rlf_obs_destroy(rlf_observation *obs);
+/* data / sky model from host complex128 [n_ch*n_rows] (NULL = zero) */
+int rlf_obs_set_vis(rlf_observation *obs, const double *data_c128, const double *sky_c128);
+/* data from host complex64 [n_ch*n_rows] */
+int rlf_obs_set_data_c64(rlf_observation *obs, const float *data_c64);
+int rlf_obs_get_vis(rlf_observation *obs, double *data_c128, double *sky_c128);
+/* data = sum of sheared galaxy models + complex Gaussian noise (sigma per component), on the GPU */
+int rlf_obs_simulate(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                     const double *e1, const double *e2, const double *l, const double *m,
+                     double noise_sigma, uint64_t seed, int gaussian);
+/* sky model = sum of round models (data_simulation.c:131-165) */
+int rlf_obs_sky_model(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                      const double *l, const double *m, int gaussian);
+/* keep / restore copies of data and sky model on the device */
+int rlf_obs_snapshot(rlf_observation *obs);
+int rlf_obs_restore(rlf_observation *obs);
+/* extraction -> fit -> removal for galaxies in catalogue order, then (opt->refit) the re-fit
+ * pass over bad galaxies (RadioLensfit2.cpp:597-606).  out: [n_gal]; n_bad: galaxies still bad. */
+int rlf_obs_process(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                    const double *l, const double *m, int numr, const double *ro,
+                    const rlf_options *opt, rlf_fit_result *out, int *n_bad);
+/* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
+ * [total, extract, fit, remove] */
+int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RLF_GB300_H */

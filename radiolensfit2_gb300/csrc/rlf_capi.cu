@@ -1,0 +1,1196 @@
+// Host runtime of the GB300 shape-measurement library: the reference-named C entry points
+// (host buffers in, host buffers out), the device-resident observation, and the per-galaxy
+// pipeline that replaces the loop of data_processing.c:61-138.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <map>
+#include <vector>
+
+#include "rlf_device.cuh"
+#include "rlf_fit.cuh"
+#include "rlf_vis.cuh"
+#include "../../include/rlf_gb300.h"
+
+typedef struct {
+  double real;
+  double imag;
+} complexd;
+
+// datatype.h:49-74, FACET branch
+typedef struct {
+  int numr;
+  double* ro;
+  double* rprior;
+  unsigned int nchannels;
+  double band_factor;
+  double acc_time;
+  double* spec;
+  double* wavenumbers;
+  double* uu;
+  double* vv;
+  double l0;
+  double m0;
+  complexd* data;
+  double* sigma2;
+  double* mod;
+  unsigned int facet;
+  unsigned int ncoords;
+} likelihood_params;
+
+struct rlf_gsl_vector_layout {
+  size_t size;
+  size_t stride;
+  double* data;
+  void* block;
+  int owner;
+};
+
+namespace rlf {
+
+#define RLF_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      fprintf(stderr, "rlf: %s failed: %s (%s:%d)\n", #call, cudaGetErrorString(e_),      \
+              __FILE__, __LINE__);                                                       \
+      return (int)e_;                                                                    \
+    }                                                                                    \
+  } while (0)
+#define RLF_OK(call)              \
+  do {                            \
+    int r_ = (call);              \
+    if (r_) return r_;            \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { if (p) cudaFree(p); }
+  int ensure(size_t count) {
+    if (count <= n && p) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      fprintf(stderr, "rlf: cudaMalloc(%zu bytes): %s\n", count * sizeof(T), cudaGetErrorString(e));
+      p = nullptr;
+      return (int)e;
+    }
+    n = count;
+    return 0;
+  }
+  int upload(const T* h, size_t count, cudaStream_t st) {
+    RLF_OK(ensure(count));
+    if (count) RLF_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    return 0;
+  }
+  int download(T* h, size_t count, cudaStream_t st) const {
+    if (count) RLF_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+    return 0;
+  }
+};
+
+struct Lib {
+  cudaStream_t st = nullptr;
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr};
+  // scratch for the per-function entry points
+  DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
+  DevBuf<double2> c0, c1;
+  DevBuf<float> f0;
+  DevBuf<uint8_t> b0;
+  DevBuf<uint16_t> u16;
+  DevBuf<unsigned> ucount;
+  DevBuf<int> i0;
+  DevBuf<FitOut> fo;
+  int init() {
+    if (st) return 0;
+    RLF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    return 0;
+  }
+};
+static Lib g_lib;
+
+static int lib_stream(cudaStream_t* st) {
+  RLF_OK(g_lib.init());
+  *st = g_lib.st;
+  return 0;
+}
+
+// ---------------------------------------------------------------- observation
+struct FacetCache {
+  DevBuf<uint16_t> cell;
+  DevBuf<double> ss, sw;
+};
+
+struct Timing {
+  cudaEvent_t ev[8];
+  bool made = false;
+  double ms[4] = {0, 0, 0, 0};
+};
+
+}  // namespace rlf
+
+struct rlf_observation {
+  int n_rows = 0, n_ch = 0;
+  long long n_vis = 0;
+  int precision = RLF_F64;
+  double len = 0;
+  std::vector<double> wavenumbers, spec;
+  rlf::DevBuf<double> uu, vv, ww;
+  rlf::DevBuf<float> sigma2;
+  rlf::DevBuf<uint8_t> flag;
+  rlf::DevBuf<double2> data64, sky64, data64_0, sky64_0;
+  rlf::DevBuf<float2> data32, sky32, data32_0, sky32_0;
+  std::map<unsigned, rlf::FacetCache*> facets;
+  rlf::DevBuf<double> partial;
+  int n_part = 0;
+  double ms[4] = {0, 0, 0, 0};
+  ~rlf_observation() {
+    for (auto& kv : facets) delete kv.second;
+  }
+  rlf::Observation view() const {
+    rlf::Observation o;
+    o.n_rows = n_rows;
+    o.n_ch = n_ch;
+    o.lay.s_row = 1;
+    o.lay.s_ch = n_rows;
+    o.uu = uu.p;
+    o.vv = vv.p;
+    o.ww = ww.p;
+    o.len = len;
+    return o;
+  }
+};
+
+namespace rlf {
+
+static int obs_facet(rlf_observation* ob, unsigned F, FacetCache** out, cudaStream_t st) {
+  auto it = ob->facets.find(F);
+  if (it != ob->facets.end()) { *out = it->second; return 0; }
+  if (F == 0 || F > kMaxExtractFacet) {
+    fprintf(stderr, "rlf: facet size %u outside 1..%u\n", F, kMaxExtractFacet);
+    return 1;
+  }
+  FacetCache* fc = new FacetCache();
+  const Observation o = ob->view();
+  int r = fc->cell.ensure((size_t)ob->n_vis);
+  if (!r) r = launch_cell_index(o, ob->flag.p, F, fc->cell.p, st);
+  if (!r) r = fc->ss.ensure((size_t)F * F);
+  if (!r) r = fc->sw.ensure((size_t)F * F);
+  if (!r) r = ob->partial.ensure((size_t)ob->n_part * 4 * F * F + 4 * F * F);
+  if (!r) r = launch_grid_weights(o, fc->cell.p, ob->sigma2.p, F, ob->partial.p, ob->n_part, fc->ss.p, fc->sw.p, st);
+  if (r) { delete fc; return r; }
+  ob->facets[F] = fc;
+  *out = fc;
+  return 0;
+}
+
+// Philox4x32-10 counter-based generator (Salmon et al., SC'11) for the simulator's noise.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += W0;
+    k.y += W1;
+  }
+  return c;
+}
+
+template <class C>
+__global__ void k_add_noise(long long n, C* vis, double sigma, uint64_t seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const uint4 r = philox(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 0u, 0u),
+                           make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    const double u1 = ((double)r.x + 1.0) * (1.0 / 4294967296.0);
+    const double u2 = (double)r.y * (1.0 / 4294967296.0);
+    const float rad = sqrtf(-2.f * logf((float)u1));
+    float s, c;
+    sincospif(2.f * (float)u2, &s, &c);
+    C v = vis[i];
+    v.x += (decltype(v.x))(sigma * (double)(rad * c));
+    v.y += (decltype(v.y))(sigma * (double)(rad * s));
+    vis[i] = v;
+  }
+}
+
+static std::vector<GalaxyParams> make_gals(int n, const double* flux, const double* scale, const double* e1,
+                                           const double* e2, const double* l, const double* m, double len,
+                                           unsigned fmax) {
+  std::vector<GalaxyParams> g(n);
+  for (int i = 0; i < n; ++i) {
+    g[i].l = l[i];
+    g[i].m = m[i];
+    g[i].flux = flux[i];
+    g[i].scale = scale[i];
+    g[i].e1 = e1 ? e1[i] : 0.0;
+    g[i].e2 = e2 ? e2[i] : 0.0;
+    unsigned F = facet_size(scale[i], len);
+    if (fmax && F > fmax) F = fmax;  // the reference's facet buffers hold facet_size(RMAX) cells
+    if (F < 2) F = 2;
+    g[i].facet = (int)F;
+    g[i].pad = 0;
+  }
+  return g;
+}
+
+// ------------------------------------------------------------------ pipeline
+// One pass of data_processing.c:61-138 over `order` (catalogue indices), `batch` galaxies at a
+// time: extraction + facet finalisation per galaxy, one persistent fit launch per batch, removal
+// per galaxy (skipped on the device for bad fits).  Everything is queued on one stream; the host
+// waits once at the end.  With batch = 1 the order of operations is the reference's.
+static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, const std::vector<int>& order,
+                    int numr, const double* ro, const rlf_options& opt, std::vector<FitOut>& out,
+                    cudaStream_t st, double* ms3) {
+  const int n = (int)order.size();
+  out.assign(n, FitOut{});
+  if (n == 0) return 0;
+  if (numr < 2 || numr > kMaxNodes) { fprintf(stderr, "rlf: %d scalelength nodes unsupported\n", numr); return 1; }
+  const Precision prec = (ob->precision == RLF_F64) ? kF64 : kMixed;
+  const int B = opt.batch > 0 ? opt.batch : 1;
+  const Observation o = ob->view();
+  unsigned fmax = 0;
+  for (int i = 0; i < n; ++i) fmax = std::max<unsigned>(fmax, (unsigned)gals[order[i]].facet);
+  const int max_cells = (int)(fmax * fmax);
+  std::vector<FacetCache*> cache(n);
+  for (int i = 0; i < n; ++i) RLF_OK(obs_facet(ob, (unsigned)gals[order[i]].facet, &cache[i], st));
+  FitConfigHost fc;
+  memset(&fc, 0, sizeof(fc));
+  fc.numr = numr;
+  fc.gaussian = opt.gaussian;
+  fc.np_max = kNpMax;
+  for (int i = 0; i < numr; ++i) fc.ro[i] = ro[i];
+  RLF_OK(fit_set_config(fc, st));
+  std::vector<GalaxyParams> hg(n);
+  std::vector<double> rprior((size_t)n * kMaxNodes, 0.0);
+  std::vector<int> facets(n);
+  std::vector<const double*> ssp(n), swp(n);
+  for (int i = 0; i < n; ++i) {
+    hg[i] = gals[order[i]];
+    // data_processing.c:68-76: ln prior of the scalelength at each node
+    const double mu = scale_mean(hg[i].flux);
+    for (int r = 1; r < numr; ++r) rprior[(size_t)i * kMaxNodes + r] = rfunc(mu, kRStd, ro[r]);
+    facets[i] = hg[i].facet;
+    ssp[i] = cache[i]->ss.p;
+    swp[i] = cache[i]->sw.p;
+  }
+  const int nb = std::min(B, n);
+  std::vector<int> slot_off(nb);
+  for (int k = 0; k < nb; ++k) slot_off[k] = k * max_cells;
+  DevBuf<GalaxyParams> dg;
+  DevBuf<double> dprior, dstart;
+  DevBuf<int> dfac, doff, dnc, dqueue;
+  DevBuf<const double*> dss, dsw;
+  DevBuf<FitOut> dout;
+  RLF_OK(dg.upload(hg.data(), n, st));
+  RLF_OK(dprior.upload(rprior.data(), rprior.size(), st));
+  RLF_OK(dfac.upload(facets.data(), n, st));
+  RLF_OK(dss.upload(ssp.data(), n, st));
+  RLF_OK(dsw.upload(swp.data(), n, st));
+  RLF_OK(doff.upload(slot_off.data(), nb, st));
+  if (opt.start) {
+    std::vector<double> sv((size_t)3 * n);
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) sv[3 * i + k] = opt.start[3 * order[i] + k];
+    RLF_OK(dstart.upload(sv.data(), sv.size(), st));
+  }
+  const int nbatches = (n + B - 1) / B;
+  RLF_OK(dout.ensure(n));
+  RLF_CUDA(cudaMemsetAsync(dout.p, 0, n * sizeof(FitOut), st));
+  RLF_OK(dnc.ensure(n));
+  RLF_OK(dqueue.ensure(nbatches));
+  RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, nbatches * sizeof(int), st));
+  const size_t esz = prec == kF64 ? sizeof(double) : sizeof(float);
+  DevBuf<unsigned char> cells;
+  const size_t plane = (size_t)nb * max_cells * esz;
+  RLF_OK(cells.ensure(5 * plane));
+  void* gu = cells.p;
+  void* gv = cells.p + plane;
+  void* dre = cells.p + 2 * plane;
+  void* dim = cells.p + 3 * plane;
+  void* sg = cells.p + 4 * plane;
+  RLF_OK(ob->partial.ensure((size_t)ob->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
+  std::vector<cudaEvent_t> ev((size_t)nbatches * 3 + 1);
+  for (auto& e : ev) RLF_CUDA(cudaEventCreate(&e));
+  const int grid_fit = fit_max_grid(prec);
+  RLF_CUDA(cudaEventRecord(ev[0], st));
+  for (int bi = 0; bi < nbatches; ++bi) {
+    const int b0 = bi * B;
+    const int bn = std::min(B, n - b0);
+    for (int k = 0; k < bn; ++k) {
+      const int i = b0 + k;
+      const unsigned F = (unsigned)facets[i];
+      if (prec == kF64)
+        RLF_OK(launch_extract_f64(o, ob->data64.p, ob->sky64.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
+                                  ob->partial.p, ob->n_part, st));
+      else
+        RLF_OK(launch_extract_mixed(o, ob->data32.p, ob->sky32.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
+                                    ob->partial.p, ob->n_part, st));
+      FacetOut fo;
+      fo.offset = doff.p + k;
+      fo.ncoords = dnc.p + i;
+      fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
+      fo.as_float = prec == kMixed;
+      RLF_OK(launch_facet_finalize(1, dfac.p + i, ob->partial.p, ob->n_part, 0, dss.p + i, dsw.p + i, ob->len,
+                                   fo, st));
+    }
+    RLF_CUDA(cudaEventRecord(ev[3 * bi + 1], st));
+    FacetBatch fb;
+    fb.n_gal = bn;
+    fb.max_cells = max_cells;
+    fb.offset = doff.p;
+    fb.count = dnc.p + b0;
+    fb.gu = gu; fb.gv = gv; fb.dre = dre; fb.dim = dim; fb.sig2 = sg;
+    fb.rprior = dprior.p + (size_t)b0 * kMaxNodes;
+    fb.start = opt.start ? dstart.p + (size_t)3 * b0 : nullptr;
+    fb.active = nullptr;
+    fb.out = dout.p + b0;
+    fb.queue = dqueue.p + bi;
+    RLF_OK(fit_launch(fb, prec, std::min(grid_fit, bn), st));
+    RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
+    for (int k = 0; k < bn; ++k) {
+      const int i = b0 + k;
+      const double* e12 = &dout.p[i].e1;
+      const int* err = &dout.p[i].error;
+      if (prec == kF64)
+        RLF_OK(launch_remove_f64(o, ob->data64.p, ob->sky64.p, dg.p + i, e12, err, opt.gaussian, st));
+      else
+        RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
+    }
+    RLF_CUDA(cudaEventRecord(ev[3 * bi + 3], st));
+  }
+  RLF_OK(dout.download(out.data(), n, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  double t[3] = {0, 0, 0};
+  for (int bi = 0; bi < nbatches; ++bi) {
+    for (int k = 0; k < 3; ++k) {
+      float x = 0;
+      cudaEventElapsedTime(&x, ev[3 * bi + k], ev[3 * bi + k + 1]);
+      t[k] += x;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (ms3) for (int k = 0; k < 3; ++k) ms3[k] += t[k];
+  return 0;
+}
+
+// the two passes of RadioLensfit2.cpp:597-606 over a device-resident observation
+static int process(rlf_observation* ob, int n_gal, const double* flux, const double* scale, const double* l,
+                   const double* m, int numr, const double* ro, const rlf_options& opt, rlf_fit_result* res,
+                   int* n_bad, cudaStream_t st) {
+  const unsigned fmax = facet_size(kRMax, ob->len);
+  std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, ob->len, fmax);
+  std::vector<int> order(n_gal);
+  for (int i = 0; i < n_gal; ++i) order[i] = i;
+  double ms3[3] = {0, 0, 0};
+  cudaEvent_t e0, e1;
+  RLF_CUDA(cudaEventCreate(&e0));
+  RLF_CUDA(cudaEventCreate(&e1));
+  RLF_CUDA(cudaEventRecord(e0, st));
+  std::vector<FitOut> out;
+  RLF_OK(run_pass(ob, gals, order, numr, ro, opt, out, st, ms3));
+  std::vector<int> bad;
+  for (int i = 0; i < n_gal; ++i) {
+    memcpy(&res[i], &out[i], sizeof(rlf_fit_result));
+    if (out[i].error) bad.push_back(i);
+  }
+  int nb = (int)bad.size();
+  if (opt.refit && nb > 0) {
+    std::vector<FitOut> out2;
+    RLF_OK(run_pass(ob, gals, bad, numr, ro, opt, out2, st, ms3));
+    nb = 0;
+    for (size_t k = 0; k < bad.size(); ++k) {
+      memcpy(&res[bad[k]], &out2[k], sizeof(rlf_fit_result));
+      if (out2[k].error) {  // data_processing.c:97-103: written with e = 0
+        res[bad[k]].e1 = 0.;
+        res[bad[k]].e2 = 0.;
+        nb++;
+      }
+    }
+  }
+  RLF_CUDA(cudaEventRecord(e1, st));
+  RLF_CUDA(cudaEventSynchronize(e1));
+  float tot = 0;
+  cudaEventElapsedTime(&tot, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ob->ms[0] = tot; ob->ms[1] = ms3[0]; ob->ms[2] = ms3[1]; ob->ms[3] = ms3[2];
+  if (n_bad) *n_bad = nb;
+  return 0;
+}
+
+static rlf_observation* obs_create(int n_rows, int n_ch, const double* uu, const double* vv, const double* ww,
+                                   const double* wavenumbers, const double* spec, double len, const float* sigma2,
+                                   const uint8_t* flag, int precision, cudaStream_t st) {
+  if (n_rows <= 0 || n_ch <= 0 || n_ch > kMaxCh) { fprintf(stderr, "rlf: bad observation shape\n"); return nullptr; }
+  rlf_observation* ob = new rlf_observation();
+  ob->n_rows = n_rows;
+  ob->n_ch = n_ch;
+  ob->n_vis = (long long)n_rows * n_ch;
+  ob->precision = precision;
+  ob->len = len;
+  ob->wavenumbers.assign(wavenumbers, wavenumbers + n_ch);
+  ob->spec.assign(spec, spec + n_ch);
+  ob->n_part = grid_partial_blocks();
+  int r = ob->uu.upload(uu, n_rows, st);
+  if (!r) r = ob->vv.upload(vv, n_rows, st);
+  if (!r) r = ob->ww.upload(ww, n_rows, st);
+  if (!r) r = ob->sigma2.upload(sigma2, (size_t)ob->n_vis, st);
+  if (!r && flag) r = ob->flag.upload(flag, (size_t)ob->n_vis, st);
+  if (!r && precision == RLF_F64) {
+    r = ob->data64.ensure(ob->n_vis);
+    if (!r) r = ob->sky64.ensure(ob->n_vis);
+    if (!r) r = (int)cudaMemsetAsync(ob->data64.p, 0, ob->n_vis * sizeof(double2), st);
+    if (!r) r = (int)cudaMemsetAsync(ob->sky64.p, 0, ob->n_vis * sizeof(double2), st);
+  } else if (!r) {
+    r = ob->data32.ensure(ob->n_vis);
+    if (!r) r = ob->sky32.ensure(ob->n_vis);
+    if (!r) r = (int)cudaMemsetAsync(ob->data32.p, 0, ob->n_vis * sizeof(float2), st);
+    if (!r) r = (int)cudaMemsetAsync(ob->sky32.p, 0, ob->n_vis * sizeof(float2), st);
+  }
+  if (!r) r = set_channels(n_ch, wavenumbers, spec, st);
+  if (!r) r = (int)cudaStreamSynchronize(st);
+  if (r) { delete ob; return nullptr; }
+  return ob;
+}
+
+// upload host complex128 [n] into the observation's data or sky array
+static int obs_put_c128(rlf_observation* ob, const double* h, bool sky, cudaStream_t st) {
+  const long long n = ob->n_vis;
+  if (ob->precision == RLF_F64) {
+    double2* d = sky ? ob->sky64.p : ob->data64.p;
+    if (h) RLF_CUDA(cudaMemcpyAsync(d, h, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    else RLF_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double2), st));
+    return 0;
+  }
+  float2* d = sky ? ob->sky32.p : ob->data32.p;
+  if (!h) { RLF_CUDA(cudaMemsetAsync(d, 0, n * sizeof(float2), st)); return 0; }
+  // stage in chunks through a device FP64 buffer
+  const long long chunk = 1LL << 24;
+  DevBuf<double2> tmp;
+  RLF_OK(tmp.ensure((size_t)std::min(chunk, n)));
+  for (long long i = 0; i < n; i += chunk) {
+    const long long c = std::min(chunk, n - i);
+    RLF_CUDA(cudaMemcpyAsync(tmp.p, h + 2 * i, c * sizeof(double2), cudaMemcpyHostToDevice, st));
+    RLF_OK(launch_convert_c64_to_f32(c, tmp.p, d + i, st));
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+static int obs_get_c128(rlf_observation* ob, double* h, bool sky, cudaStream_t st) {
+  const long long n = ob->n_vis;
+  if (!h) return 0;
+  if (ob->precision == RLF_F64) {
+    RLF_CUDA(cudaMemcpyAsync(h, sky ? ob->sky64.p : ob->data64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(cudaStreamSynchronize(st));
+    return 0;
+  }
+  const float2* d = sky ? ob->sky32.p : ob->data32.p;
+  const long long chunk = 1LL << 24;
+  DevBuf<double2> tmp;
+  RLF_OK(tmp.ensure((size_t)std::min(chunk, n)));
+  for (long long i = 0; i < n; i += chunk) {
+    const long long c = std::min(chunk, n - i);
+    RLF_OK(launch_convert_f32_to_c64(c, d + i, tmp.p, st));
+    RLF_CUDA(cudaMemcpyAsync(h + 2 * i, tmp.p, c * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(cudaStreamSynchronize(st));
+  }
+  return 0;
+}
+
+// facet arrays of a likelihood_params (FACET) uploaded as a one-galaxy FacetBatch (F64)
+struct OneFacet {
+  DevBuf<double> gu, gv, dre, dim, sig2, rprior;
+  DevBuf<int> off, cnt;
+  FacetBatch fb;
+  int load(const likelihood_params* par, cudaStream_t st) {
+    const int n = (int)par->ncoords;
+    std::vector<double> re(n > 0 ? n : 1), im(n > 0 ? n : 1), pr(kMaxNodes, 0.0);
+    for (int i = 0; i < n; ++i) { re[i] = par->data[i].real; im[i] = par->data[i].imag; }
+    for (int i = 0; i < par->numr && i < kMaxNodes; ++i) pr[i] = par->rprior[i];
+    RLF_OK(gu.upload(par->uu, n, st));
+    RLF_OK(gv.upload(par->vv, n, st));
+    RLF_OK(dre.upload(re.data(), n, st));
+    RLF_OK(dim.upload(im.data(), n, st));
+    RLF_OK(sig2.upload(par->sigma2, n, st));
+    RLF_OK(rprior.upload(pr.data(), kMaxNodes, st));
+    int z = 0;
+    RLF_OK(off.upload(&z, 1, st));
+    RLF_OK(cnt.upload(&n, 1, st));
+    FitConfigHost fc;
+    memset(&fc, 0, sizeof(fc));
+    if (par->numr < 2 || par->numr > kMaxNodes) { fprintf(stderr, "rlf: numr %d unsupported\n", par->numr); return 1; }
+    fc.numr = par->numr;
+    fc.gaussian = g_lib.opt.gaussian;
+    fc.np_max = kNpMax;
+    for (int i = 0; i < par->numr; ++i) fc.ro[i] = par->ro[i];
+    RLF_OK(fit_set_config(fc, st));
+    fb.n_gal = 1;
+    fb.max_cells = n;
+    fb.offset = off.p;
+    fb.count = cnt.p;
+    fb.gu = gu.p; fb.gv = gv.p; fb.dre = dre.p; fb.dim = dim.p; fb.sig2 = sig2.p;
+    fb.rprior = rprior.p;
+    fb.start = nullptr;
+    fb.active = nullptr;
+    fb.out = nullptr;
+    fb.queue = nullptr;
+    return 0;
+  }
+};
+
+// last spline built by marginalise_posterior_r, for marf (marginalise_r.c:231-238)
+static std::vector<double> g_marf_x, g_marf_y;
+
+}  // namespace rlf
+
+using namespace rlf;
+
+// =========================================================== batched / device API
+extern "C" {
+
+const char* rlf_version(void) { return "rlf-gb300 0.1 (sm_103a)"; }
+
+int rlf_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+int rlf_configure(const rlf_options* opt) {
+  if (opt) g_lib.opt = *opt;
+  if (g_lib.opt.batch < 1) g_lib.opt.batch = 1;
+  return 0;
+}
+
+rlf_observation* rlf_obs_create(int n_rows, int n_ch, const double* uu, const double* vv, const double* ww,
+                                const double* wavenumbers, const double* spec, double len, const float* sigma2,
+                                const uint8_t* flag, int precision) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return nullptr;
+  return obs_create(n_rows, n_ch, uu, vv, ww, wavenumbers, spec, len, sigma2, flag, precision, st);
+}
+
+void rlf_obs_destroy(rlf_observation* obs) { delete obs; }
+
+int rlf_obs_set_vis(rlf_observation* obs, const double* data_c128, const double* sky_c128) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  RLF_OK(obs_put_c128(obs, data_c128, false, st));
+  RLF_OK(obs_put_c128(obs, sky_c128, true, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_obs_set_data_c64(rlf_observation* obs, const float* data_c64) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const long long n = obs->n_vis;
+  if (obs->precision == RLF_F64) {
+    DevBuf<float2> tmp;
+    RLF_OK(tmp.upload(reinterpret_cast<const float2*>(data_c64), (size_t)n, st));
+    RLF_OK(launch_convert_f32_to_c64(n, tmp.p, obs->data64.p, st));
+    RLF_CUDA(cudaStreamSynchronize(st));
+  } else {
+    RLF_CUDA(cudaMemcpyAsync(obs->data32.p, data_c64, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    RLF_CUDA(cudaStreamSynchronize(st));
+  }
+  return 0;
+}
+
+int rlf_obs_get_vis(rlf_observation* obs, double* data_c128, double* sky_c128) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(obs_get_c128(obs, data_c128, false, st));
+  RLF_OK(obs_get_c128(obs, sky_c128, true, st));
+  return 0;
+}
+
+int rlf_obs_simulate(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* e1,
+                     const double* e2, const double* l, const double* m, double noise_sigma, uint64_t seed,
+                     int gaussian) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  std::vector<GalaxyParams> g = make_gals(n_gal, flux, scale, e1, e2, l, m, obs->len, 0);
+  DevBuf<GalaxyParams> dg;
+  RLF_OK(dg.upload(g.data(), g.size(), st));
+  const Observation o = obs->view();
+  const int chunk = 256;  // galaxies per launch keeps each launch short
+  for (int g0 = 0; g0 < n_gal; g0 += chunk) {
+    const int gn = std::min(chunk, n_gal - g0);
+    if (obs->precision == RLF_F64) RLF_OK(launch_sky_model_f64(o, obs->data64.p, dg.p + g0, gn, 1, gaussian, st));
+    else RLF_OK(launch_sky_model_mixed(o, obs->data32.p, dg.p + g0, gn, 1, gaussian, st));
+  }
+  if (noise_sigma > 0) {
+    if (obs->precision == RLF_F64) k_add_noise<double2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data64.p, noise_sigma, seed);
+    else k_add_noise<float2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data32.p, noise_sigma, seed);
+    RLF_CUDA(cudaGetLastError());
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_obs_sky_model(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* l,
+                      const double* m, int gaussian) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  std::vector<GalaxyParams> g = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, 0);
+  DevBuf<GalaxyParams> dg;
+  RLF_OK(dg.upload(g.data(), g.size(), st));
+  const Observation o = obs->view();
+  const int chunk = 256;
+  for (int g0 = 0; g0 < n_gal; g0 += chunk) {
+    const int gn = std::min(chunk, n_gal - g0);
+    if (obs->precision == RLF_F64) RLF_OK(launch_sky_model_f64(o, obs->sky64.p, dg.p + g0, gn, 0, gaussian, st));
+    else RLF_OK(launch_sky_model_mixed(o, obs->sky32.p, dg.p + g0, gn, 0, gaussian, st));
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_obs_snapshot(rlf_observation* obs) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const size_t n = (size_t)obs->n_vis;
+  if (obs->precision == RLF_F64) {
+    RLF_OK(obs->data64_0.ensure(n));
+    RLF_OK(obs->sky64_0.ensure(n));
+    RLF_CUDA(cudaMemcpyAsync(obs->data64_0.p, obs->data64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(cudaMemcpyAsync(obs->sky64_0.p, obs->sky64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  } else {
+    RLF_OK(obs->data32_0.ensure(n));
+    RLF_OK(obs->sky32_0.ensure(n));
+    RLF_CUDA(cudaMemcpyAsync(obs->data32_0.p, obs->data32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(cudaMemcpyAsync(obs->sky32_0.p, obs->sky32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_obs_restore(rlf_observation* obs) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const size_t n = (size_t)obs->n_vis;
+  if (obs->precision == RLF_F64) {
+    if (!obs->data64_0.p) return 1;
+    RLF_CUDA(cudaMemcpyAsync(obs->data64.p, obs->data64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(cudaMemcpyAsync(obs->sky64.p, obs->sky64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  } else {
+    if (!obs->data32_0.p) return 1;
+    RLF_CUDA(cudaMemcpyAsync(obs->data32.p, obs->data32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(cudaMemcpyAsync(obs->sky32.p, obs->sky32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+  }
+  return 0;
+}
+
+int rlf_obs_process(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* l,
+                    const double* m, int numr, const double* ro, const rlf_options* opt, rlf_fit_result* out,
+                    int* n_bad) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  rlf_options o = opt ? *opt : g_lib.opt;
+  return process(obs, n_gal, flux, scale, l, m, numr, ro, o, out, n_bad, st);
+}
+
+int rlf_obs_last_timing(rlf_observation* obs, double* ms4) {
+  for (int k = 0; k < 4; ++k) ms4[k] = obs->ms[k];
+  return 0;
+}
+
+// =========================================================== reference-named ABI
+// evaluate_uv_grid.c:50-55
+unsigned int facet_size(double theta_med, double len) { return rlf::facet_size(theta_med, len); }
+
+// galaxy_visibilities.c:40-53
+double gaussian_shape(double k1, double k2, double scale_factor, double wave_factor) {
+  return rlf::gaussian_shape(k1, k2, scale_factor, wave_factor);
+}
+double sersic_shape(double k1, double k2, double scale_factor, double wave_factor) {
+  return rlf::sersic_shape(k1, k2, scale_factor, wave_factor);
+}
+
+// likelihood.c:376-421
+double marginalise_over_position_shift(double x) { return rlf::position_marginal(x); }
+
+// distributions.c:59-87
+double rfunc(const double mu, const double sigma, double r) { return rlf::rfunc(mu, sigma, r); }
+double scale_mean(double flux) { return rlf::scale_mean(flux); }
+
+// evaluate_uv_grid.c:58-109 (single process)
+unsigned int evaluate_uv_grid_size(int rank, int nprocs, double len, double* wavenumbers, unsigned int num_channels,
+                                   unsigned int ncoords, double* u, double* v, unsigned int sizeg, bool* flag) {
+  (void)rank;
+  (void)nprocs;
+  cudaStream_t st;
+  if (lib_stream(&st)) return 0;
+  if (set_channels((int)num_channels, wavenumbers, nullptr, st)) return 0;
+  const size_t nv = (size_t)num_channels * ncoords;
+  Observation o;
+  o.n_rows = (int)ncoords; o.n_ch = (int)num_channels; o.lay.s_row = 1; o.lay.s_ch = ncoords;
+  if (g_lib.d0.upload(u, ncoords, st) || g_lib.d1.upload(v, ncoords, st)) return 0;
+  if (g_lib.b0.upload(reinterpret_cast<const uint8_t*>(flag), nv, st)) return 0;
+  if (g_lib.u16.ensure(nv) || g_lib.ucount.ensure((size_t)sizeg * sizeg + 1)) return 0;
+  o.uu = g_lib.d0.p; o.vv = g_lib.d1.p; o.ww = g_lib.d1.p; o.len = len;
+  if (launch_cell_index(o, g_lib.b0.p, sizeg, g_lib.u16.p, st)) return 0;
+  if (launch_count_cells(o, g_lib.u16.p, sizeg, g_lib.ucount.p, st)) return 0;
+  unsigned n = 0;
+  cudaMemcpyAsync(&n, g_lib.ucount.p + (size_t)sizeg * sizeg, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return n;
+}
+
+// evaluate_uv_grid.c:113-133
+unsigned int evaluate_facet_coords(double* grid_u, double* grid_v, double len, unsigned int sizeg, double* count_w) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return 0;
+  const size_t nc = (size_t)sizeg * sizeg;
+  if (g_lib.d0.upload(count_w, nc, st) || g_lib.d1.ensure(nc) || g_lib.d2.ensure(nc) || g_lib.ucount.ensure(1)) return 0;
+  if (launch_facet_coords(g_lib.d1.p, g_lib.d2.p, len, sizeg, g_lib.d0.p, g_lib.ucount.p, st)) return 0;
+  unsigned n = 0;
+  cudaMemcpyAsync(&n, g_lib.ucount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  cudaMemcpyAsync(grid_u, g_lib.d1.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(grid_v, g_lib.d2.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return n;
+}
+
+// evaluate_uv_grid.c:143-211 (non-MPI branch)
+void gridding_visibilities(double* wavenumbers, unsigned int num_channels, unsigned int ncoords, double* u, double* v,
+                           complexd* vis, float* sigma2, double len, unsigned int sizeg, complexd* new_vis,
+                           double* new_sigma2, bool* flag, double* sum_w) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  if (set_channels((int)num_channels, wavenumbers, nullptr, st)) return;
+  const size_t nv = (size_t)num_channels * ncoords, nc = (size_t)sizeg * sizeg;
+  const int n_part = grid_partial_blocks();
+  Observation o;
+  o.n_rows = (int)ncoords; o.n_ch = (int)num_channels; o.lay.s_row = 1; o.lay.s_ch = ncoords; o.len = len;
+  if (g_lib.d0.upload(u, ncoords, st) || g_lib.d1.upload(v, ncoords, st)) return;
+  if (g_lib.c0.upload(reinterpret_cast<const double2*>(vis), nv, st)) return;
+  if (g_lib.f0.upload(sigma2, nv, st)) return;
+  if (g_lib.b0.upload(reinterpret_cast<const uint8_t*>(flag), nv, st)) return;
+  if (g_lib.d2.ensure((size_t)n_part * 4 * nc + 4 * nc) || g_lib.c1.ensure(nc) || g_lib.d3.ensure(nc) ||
+      g_lib.d4.ensure(nc))
+    return;
+  o.uu = g_lib.d0.p; o.vv = g_lib.d1.p; o.ww = g_lib.d1.p;
+  if (launch_grid_vis_f64(o, g_lib.c0.p, g_lib.f0.p, g_lib.b0.p, sizeg, g_lib.d2.p, n_part, st)) return;
+  if (launch_grid_vis_finalize(g_lib.d2.p, n_part, sizeg, g_lib.c1.p, g_lib.d3.p, g_lib.d4.p, st)) return;
+  std::vector<double> sw(nc);
+  cudaMemcpyAsync(sw.data(), g_lib.d4.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  size_t n = 0;
+  for (size_t p = 0; p < nc; ++p) n += sw[p] != 0.0;
+  memcpy(sum_w, sw.data(), nc * sizeof(double));
+  cudaMemcpyAsync(new_vis, g_lib.c1.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(new_sigma2, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+}
+
+// evaluate_uv_grid.c:216-230
+void average_facets(unsigned long int size, complexd* grid_vis, double* grid_sigma2, double* sum_w) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  if (g_lib.c0.upload(reinterpret_cast<const double2*>(grid_vis), size, st) ||
+      g_lib.d0.upload(grid_sigma2, size, st) || g_lib.d1.upload(sum_w, size, st))
+    return;
+  if (launch_average_facets((long long)size, g_lib.c0.p, g_lib.d0.p, g_lib.d1.p, st)) return;
+  cudaMemcpyAsync(grid_vis, g_lib.c0.p, size * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(grid_sigma2, g_lib.d0.p, size * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+}
+
+// galaxy_visibilities.c:59-91
+void model_galaxy_visibilities_at_zero(double e1, double e2, double scale, unsigned int num_coords, double* grid_u,
+                                       double* grid_v, const double* sigma2, double* Modvis) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  if (g_lib.d0.upload(grid_u, num_coords, st) || g_lib.d1.upload(grid_v, num_coords, st) ||
+      g_lib.d2.upload(sigma2, num_coords, st) || g_lib.d3.ensure(num_coords))
+    return;
+  if (launch_model_at_zero(e1, e2, scale, (int)num_coords, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p,
+                           g_lib.opt.gaussian, st))
+    return;
+  cudaMemcpyAsync(Modvis, g_lib.d3.p, num_coords * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+}
+
+// galaxy_visibilities.c:154-190
+void data_galaxy_visibilities(double spectra, double wavenumber, double band_factor, double acc_time, double e1,
+                              double e2, double scale, double flux, double l, double m, unsigned int num_coords,
+                              double* uu_metres, double* vv_metres, double* ww_metres, complexd* vis) {
+  (void)band_factor;
+  (void)acc_time;  // smearing terms are commented out in the reference (galaxy_visibilities.c:179)
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  if (g_lib.d0.upload(uu_metres, num_coords, st) || g_lib.d1.upload(vv_metres, num_coords, st) ||
+      g_lib.d2.upload(ww_metres, num_coords, st) || g_lib.c0.ensure(num_coords))
+    return;
+  if (launch_galaxy_vis_channel((int)num_coords, spectra, wavenumber, e1, e2, scale, flux, l, m, g_lib.d0.p,
+                                g_lib.d1.p, g_lib.d2.p, g_lib.c0.p, g_lib.opt.gaussian, st))
+    return;
+  cudaMemcpyAsync(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+}
+
+// galaxy_visibilities.c:244-270
+void data_visibilities_phase_shift(double wavenumber, double l, double m, unsigned int num_coords, double* uu_metres,
+                                   double* vv_metres, double* ww_metres, complexd* vis) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  if (g_lib.d0.upload(uu_metres, num_coords, st) || g_lib.d1.upload(vv_metres, num_coords, st) ||
+      g_lib.d2.upload(ww_metres, num_coords, st) ||
+      g_lib.c0.upload(reinterpret_cast<const double2*>(vis), num_coords, st))
+    return;
+  if (launch_phase_shift_channel((int)num_coords, wavenumber, l, m, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.c0.p,
+                                 st))
+    return;
+  cudaMemcpyAsync(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+}
+
+// likelihood.c:156-187
+double loglikelihood_r(double ee1, double ee2, double scale, unsigned long int n_uv_coords, const double* variance,
+                       double* grid_u, double* grid_v, complexd* visData, double* visM) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return kBad;
+  const size_t n = n_uv_coords;
+  std::vector<double> re(n ? n : 1), im(n ? n : 1);
+  for (size_t i = 0; i < n; ++i) { re[i] = visData[i].real; im[i] = visData[i].imag; }
+  if (g_lib.d0.upload(grid_u, n, st) || g_lib.d1.upload(grid_v, n, st) || g_lib.d2.upload(re.data(), n, st) ||
+      g_lib.d3.upload(im.data(), n, st) || g_lib.d4.upload(variance, n, st) || g_lib.d5.ensure(n) ||
+      g_lib.d6.ensure(2))
+    return kBad;
+  if (launch_loglikelihood_r(ee1, ee2, scale, (int)n, g_lib.d4.p, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p,
+                             g_lib.d5.p, g_lib.d6.p, g_lib.opt.gaussian, st))
+    return kBad;
+  double L[2];
+  cudaMemcpyAsync(L, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(visM, g_lib.d5.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return L[0];
+}
+
+// likelihood.c:194-358
+int cross_correlation(unsigned long int n_uv_coords, double* grid_u, double* grid_v, complexd* visData,
+                      double* visMod, double* ho, double* det_sigma) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return 1;
+  const size_t n = n_uv_coords;
+  std::vector<double> re(n ? n : 1), im(n ? n : 1);
+  for (size_t i = 0; i < n; ++i) { re[i] = visData[i].real; im[i] = visData[i].imag; }
+  if (g_lib.d0.upload(grid_u, n, st) || g_lib.d1.upload(grid_v, n, st) || g_lib.d2.upload(re.data(), n, st) ||
+      g_lib.d3.upload(im.data(), n, st) || g_lib.d4.upload(visMod, n, st) || g_lib.d6.ensure(4))
+    return 1;
+  if (launch_cross_correlation((int)n, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p, g_lib.d4.p, g_lib.d6.p, st))
+    return 1;
+  double r[4];
+  cudaMemcpyAsync(r, g_lib.d6.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  *ho = r[0];
+  *det_sigma = r[1];
+  return (int)r[2];
+}
+
+// likelihood.c:106-149
+double loglikelihood(void* params, double ee1, double ee2, int* error) {
+  likelihood_params* par = (likelihood_params*)params;
+  cudaStream_t st;
+  *error = 1;
+  if (lib_stream(&st)) return kBad;
+  OneFacet f;
+  if (f.load(par, st) || g_lib.d6.ensure(2)) return kBad;
+  if (launch_loglikelihood(f.fb, ee1, ee2, g_lib.d6.p, nullptr, st)) return kBad;
+  double r[2];
+  cudaMemcpyAsync(r, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  *error = (int)r[1];
+  return r[0];
+}
+
+// likelihood.c:87-100
+double f_likelihood(const rlf_gsl_vector_layout* v, void* params) {
+  int error = 0;
+  const double e1 = v->data[0], e2 = v->data[v->stride];
+  double L;
+  if (e1 * e1 + e2 * e2 < 0.65) L = loglikelihood(params, e1, e2, &error);
+  else L = -1.e+10;
+  return -L;
+}
+
+// likelihood.c:428-554
+void likelihood_sampling(double* mes_e1, double* mes_e2, double maxL, void* params, int np_max, double* var_e1,
+                         double* var_e2, double* oneDimvar) {
+  likelihood_params* par = (likelihood_params*)params;
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  OneFacet f;
+  if (f.load(par, st) || g_lib.d6.ensure(5)) return;
+  if (launch_likelihood_sampling(f.fb, *mes_e1, *mes_e2, maxL, np_max, g_lib.d6.p, st)) return;
+  double r[5];
+  cudaMemcpyAsync(r, g_lib.d6.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  *mes_e1 = r[0]; *mes_e2 = r[1]; *var_e1 = r[2]; *var_e2 = r[3]; *oneDimvar = r[4];
+}
+
+// marginalise_r.c:29-64
+void rlf_set_posterior_values(int numR, double* L_r, double* rprior, double* Ro, double* xmarvals, double* ymarvals,
+                              int* numvals) {
+  cudaStream_t st;
+  *numvals = 0;
+  if (lib_stream(&st)) return;
+  if (g_lib.d0.upload(L_r, numR, st) || g_lib.d1.upload(rprior, numR, st) || g_lib.d2.upload(Ro, numR, st) ||
+      g_lib.d3.ensure(numR) || g_lib.d4.ensure(numR) || g_lib.i0.ensure(1))
+    return;
+  if (launch_set_posterior_values(numR, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p, g_lib.d4.p, g_lib.i0.p, st))
+    return;
+  int n = 0;
+  cudaMemcpyAsync(&n, g_lib.i0.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  cudaMemcpyAsync(xmarvals, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(ymarvals, g_lib.d4.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  *numvals = n;
+}
+
+// marginalise_r.c:81-223
+double rlf_marginalise_posterior_r(int num_marvals, double* xmarvals, double* ymarvals) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return kBad;
+  if (num_marvals < 3 || num_marvals > kMaxNodes) return kBad;
+  if (g_lib.d0.upload(xmarvals, num_marvals, st) || g_lib.d1.upload(ymarvals, num_marvals, st) || g_lib.d2.ensure(1))
+    return kBad;
+  if (launch_marginalise_posterior_r(num_marvals, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, st)) return kBad;
+  double L = kBad;
+  cudaMemcpyAsync(&L, g_lib.d2.p, sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(ymarvals, g_lib.d1.p, num_marvals * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  g_marf_x.assign(xmarvals, xmarvals + num_marvals);
+  g_marf_y.assign(ymarvals, ymarvals + num_marvals);
+  return L;
+}
+
+// marginalise_r.c:231-238: exp of the natural cubic spline through the last marginalised points
+double rlf_marf(double x, void* params) {
+  (void)params;
+  const int n = (int)g_marf_x.size();
+  if (n < 3 || x < g_marf_x[0] || x > g_marf_x[n - 1]) return 0.;
+  std::vector<double> c(n, 0.0), diag(n), off(n), g(n), alpha(n), gamma(n), z(n);
+  const int m = n - 2;
+  for (int i = 0; i < m; i++) {
+    const double h_i = g_marf_x[i + 1] - g_marf_x[i], h_ip1 = g_marf_x[i + 2] - g_marf_x[i + 1];
+    off[i] = h_ip1;
+    diag[i] = 2.0 * (h_ip1 + h_i);
+    g[i] = 3.0 * ((g_marf_y[i + 2] - g_marf_y[i + 1]) / h_ip1 - (g_marf_y[i + 1] - g_marf_y[i]) / h_i);
+  }
+  if (m == 1) c[1] = g[0] / diag[0];
+  else {
+    alpha[0] = diag[0];
+    gamma[0] = off[0] / alpha[0];
+    for (int i = 1; i < m - 1; i++) { alpha[i] = diag[i] - off[i - 1] * gamma[i - 1]; gamma[i] = off[i] / alpha[i]; }
+    alpha[m - 1] = diag[m - 1] - off[m - 2] * gamma[m - 2];
+    z[0] = g[0];
+    for (int i = 1; i < m; i++) z[i] = g[i] - gamma[i - 1] * z[i - 1];
+    for (int i = 0; i < m; i++) z[i] /= alpha[i];
+    c[m] = z[m - 1];
+    for (int k = m - 1; k-- > 0;) c[k + 1] = z[k] - gamma[k] * c[k + 2];
+  }
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) { int mid = (lo + hi) / 2; if (g_marf_x[mid] > x) hi = mid; else lo = mid; }
+  const double dx = g_marf_x[lo + 1] - g_marf_x[lo], dy = g_marf_y[lo + 1] - g_marf_y[lo], delx = x - g_marf_x[lo];
+  const double b = dy / dx - dx * (c[lo + 1] + 2.0 * c[lo]) / 3.0, d = (c[lo + 1] - c[lo]) / (3.0 * dx);
+  return exp(g_marf_y[lo] + delx * (b + delx * (c[lo] + delx * d)));
+}
+
+// galaxy_fitting.c:41-117
+int source_fitting(int rank, likelihood_params* par, double* mes_e1, double* mes_e2, double* var_e1, double* var_e2,
+                   double* oneDimvar, double* maxL) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return 1;
+  OneFacet f;
+  if (f.load(par, st) || g_lib.fo.ensure(1) || g_lib.i0.ensure(1)) return 1;
+  cudaMemsetAsync(g_lib.i0.p, 0, sizeof(int), st);
+  f.fb.out = g_lib.fo.p;
+  f.fb.queue = g_lib.i0.p;
+  if (fit_launch(f.fb, kF64, 1, st)) return 1;
+  FitOut o;
+  cudaMemcpyAsync(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  *mes_e1 = o.e1; *mes_e2 = o.e2; *var_e1 = o.var_e1; *var_e2 = o.var_e2; *oneDimvar = o.oneDimvar; *maxL = o.maxL;
+  if (g_lib.opt.verbose) {
+    if (o.maxL > -1.e+10) printf("rank %d: average: %f,%f variance: %e,%e 1Dvar: %e\n", rank, o.e1, o.e2, o.var_e1,
+                                 o.var_e2, o.oneDimvar);
+    else printf("rank %d: BAD - NO likelihood sampling!\n", rank);
+  }
+  return o.error;
+}
+
+// source_extraction.c:36-68 (FACET): visGal is used as scratch only
+void source_extraction(int rank, unsigned int facet, likelihood_params* par, complexd* facet_vis, double* facet_sigma2,
+                       double* sum_w, double l0, double m0, double flux, double mu, double e1, double e2,
+                       complexd* visSkyMod, complexd* visData, complexd* visGal, float* sigma2_vis, bool* flag,
+                       unsigned long int num_coords, double* uu_metres, double* vv_metres, double* ww_metres,
+                       double len) {
+  (void)rank;
+  (void)visGal;
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  rlf_observation* ob = obs_create((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres,
+                                   par->wavenumbers, par->spec, len, sigma2_vis, reinterpret_cast<const uint8_t*>(flag),
+                                   RLF_F64, st);
+  if (!ob) return;
+  const long long nv = ob->n_vis;
+  cudaMemcpyAsync(ob->data64.p, visData, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(ob->sky64.p, visSkyMod, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
+  FacetCache* fc = nullptr;
+  if (obs_facet(ob, facet, &fc, st)) { delete ob; return; }
+  GalaxyParams g;
+  g.l = l0; g.m = m0; g.flux = flux; g.scale = mu; g.e1 = e1; g.e2 = e2; g.facet = (int)facet; g.pad = 0;
+  DevBuf<GalaxyParams> dg;
+  DevBuf<int> dfac, doff, dnc;
+  DevBuf<const double*> dss, dsw;
+  DevBuf<double> cells;
+  const int F = (int)facet, nc = F * F;
+  const double* ssp = fc->ss.p;
+  const double* swp = fc->sw.p;
+  int zero = 0;
+  if (dg.upload(&g, 1, st) || dfac.upload(&F, 1, st) || doff.upload(&zero, 1, st) || dnc.ensure(1) ||
+      dss.upload(&ssp, 1, st) || dsw.upload(&swp, 1, st) || cells.ensure((size_t)5 * nc)) {
+    delete ob;
+    return;
+  }
+  const Observation o = ob->view();
+  if (launch_extract_f64(o, ob->data64.p, ob->sky64.p, fc->cell.p, dg.p, facet, g_lib.opt.gaussian, ob->partial.p,
+                         ob->n_part, st)) { delete ob; return; }
+  FacetOut fo;
+  fo.offset = doff.p;
+  fo.ncoords = dnc.p;
+  fo.gu = cells.p; fo.gv = cells.p + nc; fo.dre = cells.p + 2 * nc; fo.dim = cells.p + 3 * nc; fo.sig2 = cells.p + 4 * nc;
+  fo.as_float = 0;
+  if (launch_facet_finalize(1, dfac.p, ob->partial.p, ob->n_part, 0, dss.p, dsw.p, len, fo, st)) { delete ob; return; }
+  int n = 0;
+  std::vector<double> h((size_t)5 * nc);
+  cudaMemcpyAsync(&n, dnc.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(h.data(), cells.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(sum_w, fc->sw.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  for (int i = 0; i < n; ++i) {
+    facet_vis[i].real = h[(size_t)2 * nc + i];
+    facet_vis[i].imag = h[(size_t)3 * nc + i];
+    facet_sigma2[i] = h[(size_t)4 * nc + i];
+  }
+  delete ob;
+}
+
+// data_simulation.c:131-165 (SCALELENGTH_ON)
+void sky_model(double* wavenumbers, double* spec, double channel_bandwidth_hz, int time_acc, unsigned int num_channels,
+               unsigned int n_gal, double* gflux, double* gscale, double* l, double* m, unsigned long int num_coords,
+               double* uu_metres, double* vv_metres, double* ww_metres, complexd* visGal, complexd* visMod) {
+  (void)channel_bandwidth_hz;
+  (void)time_acc;
+  (void)visGal;
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  std::vector<float> s2((size_t)num_channels * num_coords, 1.0f);
+  rlf_observation* ob = obs_create((int)num_coords, (int)num_channels, uu_metres, vv_metres, ww_metres, wavenumbers,
+                                   spec, 1.0, s2.data(), nullptr, RLF_F64, st);
+  if (!ob) return;
+  cudaMemcpyAsync(ob->sky64.p, visMod, ob->n_vis * sizeof(double2), cudaMemcpyHostToDevice, st);
+  std::vector<GalaxyParams> g = make_gals((int)n_gal, gflux, gscale, nullptr, nullptr, l, m, 1.0, 0);
+  DevBuf<GalaxyParams> dg;
+  if (dg.upload(g.data(), g.size(), st)) { delete ob; return; }
+  const Observation o = ob->view();
+  for (unsigned g0 = 0; g0 < n_gal; g0 += 256) {
+    const int gn = (int)std::min<unsigned>(256, n_gal - g0);
+    if (launch_sky_model_f64(o, ob->sky64.p, dg.p + g0, gn, 0, g_lib.opt.gaussian, st)) { delete ob; return; }
+  }
+  cudaMemcpyAsync(visMod, ob->sky64.p, ob->n_vis * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  delete ob;
+}
+
+// data_processing.c:47-147: one pass over the catalogue (re_fitting = false) or the bad list
+void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, double len, unsigned int num_coords,
+                     FILE* pFile, likelihood_params* par, double* l, double* m, double* gflux, double* gscale,
+                     double* ge1, double* ge2, double* SNR_vis, double* sum_w, complexd* visGal, complexd* visSkyMod,
+                     complexd* visData, float* sigma2_vis, bool* flag, double* uu_metres, double* vv_metres,
+                     double* ww_metres, double* fitting_time, int* bad) {
+  (void)sum_w;
+  (void)visGal;
+  cudaStream_t st;
+  if (lib_stream(&st)) return;
+  const rlf_options opt = g_lib.opt;
+  rlf_observation* ob = obs_create((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres,
+                                   par->wavenumbers, par->spec, len, sigma2_vis, reinterpret_cast<const uint8_t*>(flag),
+                                   opt.precision, st);
+  if (!ob) return;
+  if (obs_put_c128(ob, reinterpret_cast<const double*>(visData), false, st) ||
+      obs_put_c128(ob, reinterpret_cast<const double*>(visSkyMod), true, st)) { delete ob; return; }
+  // galaxies: the catalogue (in order) or the bad list
+  std::vector<int> order(nsources > 0 ? nsources : 0);
+  for (int g = 0; g < nsources; ++g) order[g] = re_fitting ? (int)bad_list[g] : g;
+  int ncat = 0;
+  for (int g : order) ncat = std::max(ncat, g + 1);
+  const unsigned fmax = rlf::facet_size(kRMax, len);
+  std::vector<GalaxyParams> gals = make_gals(ncat, gflux, gscale, nullptr, nullptr, l, m, len, fmax);
+  std::vector<FitOut> out;
+  double ms3[3] = {0, 0, 0};
+  if (run_pass(ob, gals, order, par->numr, par->ro, opt, out, st, ms3)) { delete ob; return; }
+  int nbad = 0;
+  for (int g = 0; g < nsources; ++g) {
+    const int gal = order[g];
+    FitOut r = out[g];
+    if (opt.verbose) printf("n. %d flux = %f: measured e = %f , %f \n", gal, gflux[gal], r.e1, r.e2);
+    if (r.error) {
+      if (re_fitting) {
+        r.e1 = 0.;
+        r.e2 = 0.;
+        if (pFile)
+          fprintf(pFile, "%f | %f | %f | %f | %f | %f | %f | %f | %f | %f | %f \n", gflux[gal], ge1[gal], r.e1,
+                  sqrt(r.var_e1), ge2[gal], r.e2, sqrt(r.var_e2), r.oneDimvar, SNR_vis[gal], l[gal] / (kPi / 648000.0),
+                  m[gal] / (kPi / 648000.0));
+      } else {
+        bad_list[nbad] = (unsigned)gal;
+      }
+      nbad++;
+    } else if (pFile) {
+      fprintf(pFile, "%f | %f | %f | %f | %f | %f | %f | %f | %f | %f | %f \n", gflux[gal], ge1[gal], r.e1,
+              sqrt(r.var_e1), ge2[gal], r.e2, sqrt(r.var_e2), r.oneDimvar, SNR_vis[gal], l[gal] / (kPi / 648000.0),
+              m[gal] / (kPi / 648000.0));
+    }
+  }
+  *bad = nbad;
+  *fitting_time += ms3[1] / 1000.0;
+  obs_get_c128(ob, reinterpret_cast<double*>(visData), false, st);
+  obs_get_c128(ob, reinterpret_cast<double*>(visSkyMod), true, st);
+  delete ob;
+}
+
+}  // extern "C"
+
+// marginalise_r.h:24-27 declares these with C++ linkage
+void set_posterior_values(int numR, double* L_r, double* rprior, double* Ro, double* xmarvals, double* ymarvals,
+                          int* numvals) {
+  rlf_set_posterior_values(numR, L_r, rprior, Ro, xmarvals, ymarvals, numvals);
+}
+double marginalise_posterior_r(int num_marvals, double* xmarvals, double* ymarvals) {
+  return rlf_marginalise_posterior_r(num_marvals, xmarvals, ymarvals);
+}
+double marf(double x, void* params) { return rlf_marf(x, params); }

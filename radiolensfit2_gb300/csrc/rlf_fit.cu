@@ -1,0 +1,1125 @@
+// Facet likelihood, scalelength marginalisation and ellipticity fit on the GPU.
+//
+// One CTA fits one galaxy at a time, taking galaxies from a device work queue (persistent
+// kernel).  Inside a CTA:
+//   * warp w evaluates the likelihood at scalelength node w+1 (likelihood.c:117-131 runs these
+//     nodes as an OpenMP loop): facet model (galaxy_visibilities.c:59-91), cross-correlation and
+//     Newton search for the position shift (likelihood.c:194-358), analytic position
+//     marginalisation (likelihood.c:376-421);
+//   * warp 0 then marginalises over scalelength (marginalise_r.c:29-223): natural cubic spline of
+//     the log-posterior and adaptive Gauss-Kronrod 41 (QAG) quadrature of its exponential, the 41
+//     integrand points evaluated by the lanes in parallel;
+//   * the Nelder-Mead simplex (galaxy_fitting.c:41-82, GSL nmsimplex2) and the likelihood
+//     sampling (likelihood.c:428-554) run replicated in every thread, so every decision is taken
+//     identically by all threads and each likelihood evaluation is a CTA-collective call.
+//
+// Two arithmetic policies:
+//   F64   -- all double, the reference's arithmetic; the parity path and FP64 GPU oracle.
+//   Mixed -- FP32 cell arithmetic with compensated (Kahan per lane, double-float across lanes)
+//            sums, FP32 scalar arithmetic.  GB300 has little FP64 throughput, so the mixed path
+//            issues no FP64 instruction per likelihood evaluation.
+#include "rlf_fit.cuh"
+#include <stdio.h>
+
+namespace rlf {
+
+constexpr int kFitWarps = 24;
+constexpr int kFitThreads = kFitWarps * 32;
+constexpr int kQagCap = 256;       // intervals held by the device QAG
+constexpr int kNewtonMax = 50;     // likelihood.c:290
+constexpr int kSimplexMax = 50;    // galaxy_fitting.c:80
+
+struct FitConst {
+  int numr;
+  int gaussian;
+  int np_max;
+  int pad;
+  double ro[kMaxNodes];
+  float rof[kMaxNodes];
+};
+__constant__ FitConst c_fit;
+
+// 41-point Gauss-Kronrod rule (QUADPACK qk41): Kronrod abscissae, Kronrod weights and the
+// weights of the embedded 20-point Gauss rule (abscissae xgk[1], xgk[3], ...).
+__constant__ double c_xgk[21] = {
+    0.998859031588277663838315576545863, 0.993128599185094924786122388471320,
+    0.981507877450250259193342994720217, 0.963971927277913791267666131197277,
+    0.940822633831754753519982722212443, 0.912234428251325905867752441203298,
+    0.878276811252281976077442995113078, 0.839116971822218823394529061701521,
+    0.795041428837551198350638833272788, 0.746331906460150792614305070355642,
+    0.693237656334751384805490711845932, 0.636053680726515025452836696226286,
+    0.575140446819710315342946036586425, 0.510867001950827098004364050955251,
+    0.443593175238725103199992213492640, 0.373706088715419560672548177024927,
+    0.301627868114913004320555356858592, 0.227785851141645078080496195368575,
+    0.152605465240922675505220241022678, 0.076526521133497333754640409398838,
+    0.000000000000000000000000000000000};
+__constant__ double c_wgk[21] = {
+    0.003073583718520531501218293246031, 0.008600269855642942198661787950102,
+    0.014626169256971252983787960308868, 0.020388373461266523598010231432755,
+    0.025882133604951158834505067096153, 0.031287306777032798958543119323801,
+    0.036600169758200798030557240707211, 0.041668873327973686263788305936895,
+    0.046434821867497674720231880926108, 0.050944573923728691932707670050345,
+    0.055195105348285994744832372419777, 0.059111400880639572374967220648594,
+    0.062653237554781168025870122174255, 0.065834597133618422111563556969398,
+    0.068648672928521619345623411885368, 0.071054423553444068305790361723210,
+    0.073030690332786667495189417658913, 0.074582875400499188986581418362488,
+    0.075704497684556674659542775376617, 0.076377867672080736705502835038061,
+    0.076600711917999656445049901530102};
+__constant__ double c_wg[10] = {
+    0.017614007139152118311861962351853, 0.040601429800386941331039952274932,
+    0.062672048334109063569506535187042, 0.083276741576704748724758143222046,
+    0.101930119817240435036750135480350, 0.118194531961518417312377377711382,
+    0.131688638449176626898494499748163, 0.142096109318382051329298325067165,
+    0.149172986472603746787828737001969, 0.152753387130725850698084331955098};
+
+// ------------------------------------------------------------------ policies
+struct PolicyF64 {
+  using Cell = double;
+  using S = double;
+  static constexpr bool kMixed = false;
+};
+struct PolicyMixed {
+  using Cell = float;
+  using S = float;
+  static constexpr bool kMixed = true;
+};
+
+template <class S> struct Consts;
+template <> struct Consts<double> {
+  static __device__ __forceinline__ double dbl_eps() { return 2.2204460492503131e-16; }
+  static __device__ __forceinline__ double dbl_min() { return 2.2250738585072014e-308; }
+};
+template <> struct Consts<float> {
+  static __device__ __forceinline__ float dbl_eps() { return 1.1920929e-07f; }
+  static __device__ __forceinline__ float dbl_min() { return 1.17549435e-38f; }
+};
+
+__device__ __forceinline__ double s_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float s_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double s_log(double x) { return log(x); }
+__device__ __forceinline__ float s_log(float x) { return logf(x); }
+__device__ __forceinline__ double s_exp(double x) { return exp(x); }
+__device__ __forceinline__ float s_exp(float x) { return expf(x); }
+__device__ __forceinline__ double s_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float s_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double s_pow15(double x) { return pow(x, 1.5); }
+__device__ __forceinline__ float s_pow15(float x) { return x * sqrtf(x); }
+__device__ __forceinline__ void s_sincos(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ void s_sincos(float a, float* s, float* c) { sincosf(a, s, c); }
+
+// Uniform (lane-identical) warp sums.  Double: butterfly (a+b == b+a, so every lane ends with
+// the same bits).  Float: per-lane Kahan partials combined in double-float, operands ordered by
+// lane so both partners of a butterfly step compute identical bits.
+__device__ __forceinline__ double uwarp_sum(double v) { return warp_sum(v); }
+__device__ __forceinline__ float uwarp_sum_df(float hi, float lo) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    float ohi = __shfl_xor_sync(0xffffffffu, hi, m);
+    float olo = __shfl_xor_sync(0xffffffffu, lo, m);
+    const bool first = (lane & m) == 0;
+    float ahi = first ? hi : ohi, alo = first ? lo : olo;
+    float bhi = first ? ohi : hi, blo = first ? olo : lo;
+    f2 s = two_sum(ahi, bhi);
+    float e = s.lo + (alo + blo);
+    f2 r = quick_two_sum(s.hi, e);
+    hi = r.hi;
+    lo = r.lo;
+  }
+  return hi + lo;
+}
+
+template <class S> struct Acc;
+template <> struct Acc<double> {
+  double s;
+  __device__ __forceinline__ void zero() { s = 0.; }
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void sub(double x) { s -= x; }
+  __device__ __forceinline__ double reduce() const { return uwarp_sum(s); }
+};
+template <> struct Acc<float> {
+  float s, c;  // Kahan: running sum and compensation (true sum ~ s - c)
+  __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ void sub(float x) { add(-x); }
+  __device__ __forceinline__ float reduce() const { return uwarp_sum_df(s, -c); }
+};
+
+// ------------------------------------------------------- position marginal (FP32)
+// Same quantity as position_marginal() (likelihood.c:376-421) in FP32: Ei by its power series
+// (compensated) for x <= 25 and its asymptotic series above, the difference formed in the log
+// domain above 25 so that e^x never overflows single precision.
+__device__ __forceinline__ float ei_series_f(float x) {
+  float term = 1.f, s = 0.f, c = 0.f;
+  for (int k = 1; k < 200; ++k) {
+    term = term * x / (float)k;
+    float t = term / (float)k;
+    float y = t - c, u = s + y;
+    c = (u - s) - y;
+    s = u;
+    if (t < 1e-9f * s) break;
+  }
+  return (float)kEulerGamma + logf(x) + (s - c);
+}
+__device__ __forceinline__ float log_ei_asym_f(float x) {  // ln Ei(x), x >= 25
+  float term = 1.f, sum = 1.f;
+  for (int k = 1; k < 60; ++k) {
+    float next = term * (float)k / x;
+    if (next >= term || next < 1e-9f * sum) break;
+    term = next;
+    sum += term;
+  }
+  return x - logf(x) + logf(sum);
+}
+__device__ __forceinline__ float position_marginal_f(float x) {
+  const float Delta = 0.5f * 5.991f;
+  if (x <= Delta) return (float)kBad;
+  if (x > 100.f) return x - logf(Delta) - expf(-Delta);
+  if ((x - Delta) < 0.0001f) x = Delta + 0.0001f;
+  const float xd = x - Delta;
+  const float lden = logf(log1pf(Delta / xd));
+  if (xd <= 25.f) {
+    if (x <= 25.f) return logf(ei_series_f(x) - ei_series_f(xd)) - lden;
+    const float la = log_ei_asym_f(x);
+    const float eb = ei_series_f(xd);
+    return la + log1pf(-eb * expf(-la)) - lden;
+  }
+  const float la = log_ei_asym_f(x), lb = log_ei_asym_f(xd);
+  return la + log1pf(-expf(lb - la)) - lden;
+}
+__device__ __forceinline__ double pos_marg(double x) { return position_marginal(x); }
+__device__ __forceinline__ float pos_marg(float x) { return position_marginal_f(x); }
+
+// --------------------------------------------------------------- cell model
+template <class S>
+__device__ __forceinline__ S cell_shape(int gaussian, S a1, S a2, S a3, S u, S v, S sfw) {
+  S k1 = a1 * u + a2 * v;
+  S k2 = a2 * u + a3 * v;
+  S q = sfw * (k1 * k1 + k2 * k2);
+  if (gaussian) return s_exp(S(-0.5) * q);
+  S den = S(1) + q;
+  return S(1) / (den * s_sqrt(den));
+}
+
+// Warp-level likelihood at one scalelength node, likelihood.c:156-187 with the model of
+// galaxy_visibilities.c:59-91 and the cross-correlation of likelihood.c:194-358.
+// model_in (optional) replaces the computed model (cross_correlation's own entry point);
+// model_out (optional) receives the normalised model (loglikelihood_r writes visM).
+template <class P>
+__device__ typename P::S node_loglike(const typename P::Cell* gu, const typename P::Cell* gv,
+                                      const typename P::Cell* dre, const typename P::Cell* dim,
+                                      const typename P::Cell* sig2, int n, typename P::S e1,
+                                      typename P::S e2, typename P::S r, int gaussian, int* iters,
+                                      double* model_out,
+                                      const double* model_in, typename P::S* ho_out,
+                                      typename P::S* det_out) {
+  using S = typename P::S;
+  const int lane = threadIdx.x & 31;
+  const S a1 = S(1) + e1, a2 = e2, a3 = S(1) - e1;
+  // galaxy_visibilities.c:63-65 then the 4 pi^2 wave factor of :69
+  const S detA = S(1) - e1 * e1 - e2 * e2;
+  const S sc = r * S(kPi / 648000.0);
+  const S sfw = ((sc * sc) / (detA * detA)) * S(4 * kPi * kPi);
+  const S cc = S(2 * kPi);
+  S inv_s = S(1);
+  S s_norm = S(1);
+  if (!model_in) {
+    Acc<S> acc;
+    acc.zero();
+    for (int i = lane; i < n; i += 32) {
+      S m = cell_shape<S>(gaussian, a1, a2, a3, S(gu[i]), S(gv[i]), sfw);
+      acc.add(m * m / S(sig2[i]));
+    }
+    S sum = acc.reduce();
+    s_norm = s_sqrt(sum);
+    inv_s = S(1) / s_norm;
+  }
+  auto model_at = [&](int i) -> S {
+    if (model_in) return S(model_in[i]);
+    S m = cell_shape<S>(gaussian, a1, a2, a3, S(gu[i]), S(gv[i]), sfw);
+    if (P::kMixed) return m * inv_s;
+    return m / s_norm;  // the reference divides (galaxy_visibilities.c:90)
+  };
+  Acc<S> val, dx, dy, d2x, d2y, dxy;
+  val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
+  for (int i = lane; i < n; i += 32) {
+    S m = model_at(i);
+    if (model_out) model_out[i] = (double)m;
+    S hre = S(dre[i]) * m;
+    S him = -S(dim[i]) * m;
+    S u = cc * S(gu[i]);
+    S v = cc * S(gv[i]);
+    val.add(hre);
+    dx.sub(him * u);
+    dy.sub(him * v);
+    d2x.sub(hre * u * u);
+    d2y.sub(hre * v * v);
+    dxy.sub(hre * u * v);
+  }
+  S Sval = val.reduce(), Sdx = dx.reduce(), Sdy = dy.reduce();
+  S Sd2x = d2x.reduce(), Sd2y = d2y.reduce(), Sdxy = dxy.reduce();
+  S det = Sd2x * Sd2y - Sdxy * Sdxy;
+  S xo = S(0), yo = S(0), norm = S(1);
+  const S tol = S(1.e-7);
+  int iter = 0;
+  while (det > S(0) && (norm > tol) && iter < kNewtonMax) {
+    iter++;
+    S incx = (Sdx * Sd2y - Sdy * Sdxy) / det;
+    S incy = (Sdy * Sd2x - Sdx * Sdxy) / det;
+    xo -= incx;
+    yo -= incy;
+    val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
+    for (int i = lane; i < n; i += 32) {
+      S m = model_at(i);
+      S hre = S(dre[i]) * m;
+      S him = -S(dim[i]) * m;
+      S u = cc * S(gu[i]);
+      S v = cc * S(gv[i]);
+      S a = xo * u + yo * v;
+      S sa, ca;
+      s_sincos(a, &sa, &ca);
+      S rp = (hre * ca - him * sa);
+      S ip = (hre * sa + him * ca);
+      val.add(rp);
+      dx.sub(ip * u);
+      dy.sub(ip * v);
+      d2x.sub(rp * u * u);
+      d2y.sub(rp * v * v);
+      dxy.sub(rp * u * v);
+    }
+    Sval = val.reduce(); Sdx = dx.reduce(); Sdy = dy.reduce();
+    Sd2x = d2x.reduce(); Sd2y = d2y.reduce(); Sdxy = dxy.reduce();
+    det = Sd2x * Sd2y - Sdxy * Sdxy;
+    norm = s_sqrt(incx * incx + incy * incy);
+  }
+  // lane-uniform by construction; broadcast from lane 0 as a guard
+  Sval = __shfl_sync(0xffffffffu, Sval, 0);
+  det = __shfl_sync(0xffffffffu, det, 0);
+  *iters = iter;
+  if (ho_out) *ho_out = Sval;
+  if (det_out) *det_out = det;
+  if (det <= S(0)) return S(kBad);
+  S B = (Sval * Sval) * S(0.5);
+  S L = pos_marg(B);
+  if (isnan(L)) return S(kBad);
+  return L - S(0.5) * s_log(det);
+}
+
+// ------------------------------------------------------------- shared state
+template <class S>
+struct FitShared {
+  S Lr[kMaxNodes];
+  S rprior[kMaxNodes];
+  S xs[kMaxNodes], ys[kMaxNodes], cs[kMaxNodes];
+  S qa[kQagCap], qb[kQagCap], qr[kQagCap], qe[kQagCap];
+  S bcast_L;
+  int bcast_err;
+  int g;
+  int newton;
+  int status;
+  int numvals;
+};
+
+// ------------------------------------------------- scalelength marginalisation
+template <class S>
+__device__ __forceinline__ S spline_eval(const FitShared<S>& sh, int n, bool cubic, S x, bool* ok) {
+  if (x < sh.xs[0] || x > sh.xs[n - 1]) { *ok = false; return S(0); }
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (sh.xs[mid] > x) hi = mid; else lo = mid;
+  }
+  const S x_lo = sh.xs[lo], x_hi = sh.xs[lo + 1];
+  const S y_lo = sh.ys[lo], y_hi = sh.ys[lo + 1];
+  const S dx = x_hi - x_lo, dy = y_hi - y_lo, delx = x - x_lo;
+  *ok = true;
+  if (cubic) {
+    const S c_i = sh.cs[lo], c_ip1 = sh.cs[lo + 1];
+    const S b_i = (dy / dx) - dx * (c_ip1 + S(2) * c_i) / S(3);
+    const S d_i = (c_ip1 - c_i) / (S(3) * dx);
+    return y_lo + delx * (b_i + delx * (c_i + delx * d_i));
+  }
+  return y_lo + delx / dx * dy;
+}
+
+// integrand of marginalise_r.c:231-238: exp(spline(x)), 0 outside the nodes
+template <class S>
+__device__ __forceinline__ S marf(const FitShared<S>& sh, int n, bool cubic, S x) {
+  bool ok;
+  S y = spline_eval(sh, n, cubic, x, &ok);
+  return ok ? s_exp(y) : S(0);
+}
+
+template <class S>
+__device__ __forceinline__ S rescale_error(S err, S result_abs, S result_asc) {
+  err = s_abs(err);
+  if (result_asc != S(0) && err != S(0)) {
+    S scale = s_pow15(S(200) * err / result_asc);
+    err = (scale < S(1)) ? result_asc * scale : result_asc;
+  }
+  if (result_abs > Consts<S>::dbl_min() / (S(50) * Consts<S>::dbl_eps())) {
+    S min_err = S(50) * Consts<S>::dbl_eps() * result_abs;
+    if (min_err > err) err = min_err;
+  }
+  return err;
+}
+
+template <class S> __device__ __forceinline__ S wsum(S v);
+template <> __device__ __forceinline__ double wsum<double>(double v) { return uwarp_sum(v); }
+template <> __device__ __forceinline__ float wsum<float>(float v) { return uwarp_sum_df(v, 0.f); }
+
+// QUADPACK qk41 on one warp: lane j < 21 evaluates the integrand at centre -+ half*xgk[j].
+template <class S>
+__device__ __noinline__ void qk41_warp(const FitShared<S>& sh, int n, bool cubic, S a, S b, S* result, S* abserr,
+                          S* resabs, S* resasc) {
+  const int j = threadIdx.x & 31;
+  const S center = S(0.5) * (a + b);
+  const S half = S(0.5) * (b - a);
+  const S abs_half = s_abs(half);
+  S f1 = S(0), f2 = S(0);
+  if (j < 21) {
+    const S absc = half * S(c_xgk[j]);
+    f1 = marf(sh, n, cubic, center - absc);
+    f2 = (j == 20) ? f1 : marf(sh, n, cubic, center + absc);
+  }
+  const S fc = __shfl_sync(0xffffffffu, f1, 20);
+  const S wk = (j < 20) ? S(c_wgk[j]) : S(0);
+  const S wg = (j < 20 && (j & 1)) ? S(c_wg[j >> 1]) : S(0);
+  const S fsum = f1 + f2;
+  S rk = wsum<S>(wk * fsum) + fc * S(c_wgk[20]);
+  S rg = wsum<S>(wg * fsum);
+  S ra = wsum<S>(wk * (s_abs(f1) + s_abs(f2))) + s_abs(fc * S(c_wgk[20]));
+  const S mean = rk * S(0.5);
+  S rasc = wsum<S>(wk * (s_abs(f1 - mean) + s_abs(f2 - mean))) + S(c_wgk[20]) * s_abs(fc - mean);
+  const S err = (rk - rg) * half;
+  rk *= half;
+  ra *= abs_half;
+  rasc *= abs_half;
+  *result = rk;
+  *resabs = ra;
+  *resasc = rasc;
+  *abserr = rescale_error<S>(err, ra, rasc);
+}
+
+// QUADPACK qag (GSL gsl_integration_qag, key GSL_INTEG_GAUSS41, epsabs 0, epsrel 1e-3):
+// global adaptive bisection of the interval with the largest error.  Control is replicated in
+// the lanes of warp 0; interval lists live in shared memory (kQagCap entries).
+// Returns 0 on success, nonzero as GSL's status would be.
+template <class S>
+__device__ __noinline__ int qag_warp(FitShared<S>& sh, int n, bool cubic, S a, S b, S* out) {
+  const int lane = threadIdx.x & 31;
+  const S epsabs = S(0), epsrel = S(1.e-3);
+  S result0, abserr0, resabs0, resasc0;
+  qk41_warp<S>(sh, n, cubic, a, b, &result0, &abserr0, &resabs0, &resasc0);
+  S tolerance = fmax(epsabs, epsrel * s_abs(result0));
+  const S round_off = S(50) * Consts<S>::dbl_eps() * resabs0;
+  *out = result0;
+  if (abserr0 <= round_off && abserr0 > tolerance) return 18;        // GSL_EROUND
+  if ((abserr0 <= tolerance && abserr0 != resasc0) || abserr0 == S(0)) return 0;
+  if (lane == 0) { sh.qa[0] = a; sh.qb[0] = b; sh.qr[0] = result0; sh.qe[0] = abserr0; }
+  __syncwarp();
+  S area = result0, errsum = abserr0;
+  int nint = 1, iteration = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+  const int limit = 1000;
+  do {
+    // interval with the largest error (lowest index on ties)
+    S best = S(-1);
+    int bi = 0x7fffffff;
+    for (int k = lane; k < nint; k += 32) {
+      S e = sh.qe[k];
+      if (e > best) { best = e; bi = k; }
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+      S ob = __shfl_xor_sync(0xffffffffu, best, m);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, m);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int imax = bi;
+    const S a_i = sh.qa[imax], b_i = sh.qb[imax], r_i = sh.qr[imax], e_i = sh.qe[imax];
+    const S a1 = a_i, b1 = S(0.5) * (a_i + b_i), a2 = b1, b2 = b_i;
+    S area1, area2, error1, error2, resabs1, resabs2, resasc1, resasc2;
+    qk41_warp<S>(sh, n, cubic, a1, b1, &area1, &error1, &resabs1, &resasc1);
+    qk41_warp<S>(sh, n, cubic, a2, b2, &area2, &error2, &resabs2, &resasc2);
+    const S area12 = area1 + area2, error12 = error1 + error2;
+    errsum += (error12 - e_i);
+    area += area12 - r_i;
+    if (resasc1 != error1 && resasc2 != error2) {
+      const S delta = r_i - area12;
+      if (s_abs(delta) <= S(1.0e-5) * s_abs(area12) && error12 >= S(0.99) * e_i) roundoff1++;
+      if (iteration >= 10 && error12 > e_i) roundoff2++;
+    }
+    tolerance = fmax(epsabs, epsrel * s_abs(area));
+    if (errsum > tolerance) {
+      if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+      const S tmp = (S(1) + S(100) * Consts<S>::dbl_eps()) * (s_abs(a2) + S(1000) * Consts<S>::dbl_min());
+      if (s_abs(a1) <= tmp && s_abs(b2) <= tmp) error_type = 3;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      sh.qa[imax] = a1; sh.qb[imax] = b1; sh.qr[imax] = area1; sh.qe[imax] = error1;
+      sh.qa[nint] = a2; sh.qb[nint] = b2; sh.qr[nint] = area2; sh.qe[nint] = error2;
+    }
+    __syncwarp();
+    nint++;
+    iteration++;
+    if (nint >= kQagCap && errsum > tolerance && !error_type) {
+      if (lane == 0) sh.status |= 2;
+      error_type = 4;  // device interval capacity: reported like GSL_EMAXITER
+    }
+  } while (iteration < limit && !error_type && errsum > tolerance);
+  S sum = S(0);
+  for (int k = lane; k < nint; k += 32) sum += sh.qr[k];
+  sum = wsum<S>(sum);
+  *out = sum;
+  if (errsum <= tolerance) return 0;
+  if (error_type == 2) return 18;
+  if (error_type == 3) return 21;
+  return 11;
+}
+
+// marginalise_r.c:81-223 on warp 0; (xs, ys, numvals) already in shared memory.
+template <class S>
+__device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
+  const int lane = threadIdx.x & 31;
+  S ymax = S(-10.0);
+  int ymaxpos = 0;
+  for (int ii = 0; ii < n; ii++)
+    if (sh.ys[ii] > ymax) { ymax = sh.ys[ii]; ymaxpos = ii; }
+  S xmin, xmax;
+  xmin = xmax = sh.xs[ymaxpos];
+  if (ymaxpos < n - 1) xmax = sh.xs[ymaxpos + 1];
+  if (ymaxpos > 0) xmin = sh.xs[ymaxpos - 1];
+  for (int ii = 0; ii < n; ii++) {
+    if (sh.xs[ii] < xmin) xmin = sh.xs[ii];
+    if (sh.xs[ii] > xmax) xmax = sh.xs[ii];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (int ii = 0; ii < n; ii++) sh.ys[ii] -= ymax;
+    // natural cubic spline: c_0 = c_{n-1} = 0, interior from the symmetric tridiagonal
+    // system solved by LDL^T (as gsl_interp_cspline)
+    for (int ii = 0; ii < n; ii++) sh.cs[ii] = S(0);
+    const int m = n - 2;
+    S alpha[kMaxNodes], gamma[kMaxNodes], z[kMaxNodes], diag[kMaxNodes], off[kMaxNodes], g[kMaxNodes];
+    for (int i = 0; i < m; i++) {
+      const S h_i = sh.xs[i + 1] - sh.xs[i], h_ip1 = sh.xs[i + 2] - sh.xs[i + 1];
+      const S dy_i = sh.ys[i + 1] - sh.ys[i], dy_ip1 = sh.ys[i + 2] - sh.ys[i + 1];
+      const S g_i = (h_i != S(0)) ? S(1) / h_i : S(0);
+      const S g_ip1 = (h_ip1 != S(0)) ? S(1) / h_ip1 : S(0);
+      off[i] = h_ip1;
+      diag[i] = S(2) * (h_ip1 + h_i);
+      g[i] = S(3) * (dy_ip1 * g_ip1 - dy_i * g_i);
+    }
+    if (m == 1) {
+      sh.cs[1] = g[0] / diag[0];
+    } else if (m > 1) {
+      alpha[0] = diag[0];
+      gamma[0] = off[0] / alpha[0];
+      for (int i = 1; i < m - 1; i++) {
+        alpha[i] = diag[i] - off[i - 1] * gamma[i - 1];
+        gamma[i] = off[i] / alpha[i];
+      }
+      alpha[m - 1] = diag[m - 1] - off[m - 2] * gamma[m - 2];
+      z[0] = g[0];
+      for (int i = 1; i < m; i++) z[i] = g[i] - gamma[i - 1] * z[i - 1];
+      for (int i = 0; i < m; i++) z[i] = z[i] / alpha[i];
+      sh.cs[m] = z[m - 1];
+      for (int k = m - 1; k-- > 0;) sh.cs[k + 1] = z[k] - gamma[k] * sh.cs[k + 2];
+    }
+  }
+  __syncwarp();
+  if (xmax <= xmin) return S(kBad);  // the reference exits the process here
+  S sump;
+  int status = qag_warp<S>(sh, n, true, xmin, xmax, &sump);
+  if (status) status = qag_warp<S>(sh, n, false, xmin, xmax, &sump);
+  if (status) return S(kBad);
+  return s_log(sump) + ymax;
+}
+
+// CTA-collective loglikelihood(e1, e2) (likelihood.c:106-149).
+template <class P>
+__device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typename P::Cell* gu,
+                                      const typename P::Cell* gv, const typename P::Cell* dre,
+                                      const typename P::Cell* dim, const typename P::Cell* sig2,
+                                      int n, typename P::S e1, typename P::S e2, int* error) {
+  using S = typename P::S;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  const int numR = c_fit.numr;
+  for (int node = warp + 1; node < numR; node += nw) {
+    int it = 0;
+    const S r = P::kMixed ? S(c_fit.rof[node]) : S(c_fit.ro[node]);
+    S L = node_loglike<P>(gu, gv, dre, dim, sig2, n, e1, e2, r, c_fit.gaussian, &it, nullptr, nullptr,
+                          nullptr, nullptr);
+    if (lane == 0) {
+      sh.Lr[node] = L;
+      atomicAdd(&sh.newton, it);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // set_posterior_values (marginalise_r.c:29-64)
+    if (lane == 0) {
+      int num = 0, nRo = 1;
+      while (nRo < numR && (sh.Lr[nRo] <= S(kBad))) nRo++;
+      if (nRo < numR) {
+        for (nRo = 1; nRo < numR; nRo++) {
+          S lv = sh.Lr[nRo];
+          if (lv > S(kBad)) {
+            sh.xs[num] = P::kMixed ? S(c_fit.rof[nRo]) : S(c_fit.ro[nRo]);
+            sh.ys[num] = lv + sh.rprior[nRo];
+            num++;
+          }
+        }
+      }
+      sh.numvals = num;
+    }
+    __syncwarp();
+    const int num = sh.numvals;
+    S L_e;
+    int err = 0;
+    if (num > 4) {
+      L_e = marginalise_posterior_warp<S>(sh, num);
+    } else {
+      err = 1;
+      L_e = S(kBad);
+    }
+    if (L_e == S(kBad)) err = 1;
+    if (lane == 0) {
+      sh.bcast_L = L_e;
+      sh.bcast_err = err;
+    }
+  }
+  __syncthreads();
+  *error = sh.bcast_err;
+  return sh.bcast_L;
+}
+
+// -------------------------------------------------------------- galaxy fit
+template <class P>
+struct FitCtx {
+  FitShared<typename P::S>* sh;
+  const typename P::Cell *gu, *gv, *dre, *dim, *sig2;
+  int n;
+  int nevals;
+};
+
+template <class P>
+__device__ __noinline__ typename P::S loglike(FitCtx<P>& c, typename P::S e1, typename P::S e2,
+                                              int* error) {
+  c.nevals++;
+  return eval_loglike<P>(*c.sh, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, e1, e2, error);
+}
+
+// likelihood.c:87-100
+template <class P>
+__device__ __forceinline__ typename P::S f_likelihood(FitCtx<P>& c, typename P::S e1, typename P::S e2) {
+  using S = typename P::S;
+  int error = 0;
+  S L;
+  if (e1 * e1 + e2 * e2 < S(0.65)) L = loglike<P>(c, e1, e2, &error);
+  else L = S(-1.e+10);
+  return -L;
+}
+
+template <class S>
+__device__ __forceinline__ bool s_finite(S x) { return isfinite(x); }
+
+// GSL nmsimplex2 state for n = 2 (three vertices), replicated per thread.
+template <class S>
+struct Simplex {
+  S x[3][2];
+  S y[3];
+  S c[2];
+  S S2;
+  S size;
+};
+
+template <class S>
+__device__ __forceinline__ void nm_center(Simplex<S>& s) {
+  for (int j = 0; j < 2; ++j) {
+    S a = S(0);
+    for (int i = 0; i < 3; ++i) a += s.x[i][j];
+    s.c[j] = a * (S(1) / S(3));
+  }
+}
+template <class S>
+__device__ __forceinline__ S nm_size(Simplex<S>& s) {
+  S ss = S(0);
+  for (int i = 0; i < 3; ++i) {
+    S t2 = S(0);
+    for (int j = 0; j < 2; ++j) {
+      S d = s.x[i][j] - s.c[j];
+      t2 += d * d;
+    }
+    ss += t2;
+  }
+  s.S2 = ss / S(3);
+  return s_sqrt(s.S2);
+}
+template <class S>
+__device__ __forceinline__ void nm_update(Simplex<S>& s, int i, const S* xn, S val) {
+  const S P = S(3);
+  S dd = S(0), xmcd = S(0), dl[2];
+  for (int j = 0; j < 2; ++j) {
+    dl[j] = xn[j] - s.x[i][j];
+    S xmc = s.x[i][j] - s.c[j];
+    dd += dl[j] * dl[j];
+    xmcd += xmc * dl[j];
+  }
+  const S d = s_sqrt(dd);
+  s.S2 += (S(2) / P) * xmcd + ((P - S(1)) / P) * (d * d / P);
+  for (int j = 0; j < 2; ++j) s.c[j] += (S(1) / P) * dl[j];
+  for (int j = 0; j < 2; ++j) s.x[i][j] = xn[j];
+  s.y[i] = val;
+}
+
+template <class P>
+__device__ __forceinline__ typename P::S nm_corner(FitCtx<P>& c, Simplex<typename P::S>& s, typename P::S coeff,
+                                                   int corner, typename P::S* xc) {
+  using S = typename P::S;
+  const S Pn = S(3);
+  const S alpha = (S(1) - coeff) * Pn / (Pn - S(1));
+  const S beta = (Pn * coeff - S(1)) / (Pn - S(1));
+  for (int j = 0; j < 2; ++j) {
+    xc[j] = alpha * s.c[j];
+    xc[j] += beta * s.x[corner][j];
+  }
+  return f_likelihood<P>(c, xc[0], xc[1]);
+}
+
+// one nmsimplex2 iteration; returns 0 (GSL_SUCCESS) or 5 (GSL_EFAILED)
+template <class P>
+__device__ int nm_iterate(FitCtx<P>& c, Simplex<typename P::S>& s) {
+  using S = typename P::S;
+  S xc[2], xc2[2], val, val2;
+  int hi = 0, s_hi = 1, lo = 0;
+  S dhi = s.y[0], dlo = s.y[0], ds_hi = s.y[1];
+  for (int i = 1; i < 3; ++i) {
+    val = s.y[i];
+    if (val < dlo) { dlo = val; lo = i; }
+    else if (val > dhi) { ds_hi = dhi; s_hi = hi; dhi = val; hi = i; }
+    else if (val > ds_hi) { ds_hi = val; s_hi = i; }
+  }
+  val = nm_corner<P>(c, s, S(-1), hi, xc);
+  if (s_finite(val) && val < s.y[lo]) {
+    val2 = nm_corner<P>(c, s, S(-2), hi, xc2);
+    if (s_finite(val2) && val2 < s.y[lo]) nm_update(s, hi, xc2, val2);
+    else nm_update(s, hi, xc, val);
+  } else if (!s_finite(val) || val > s.y[s_hi]) {
+    if (s_finite(val) && val <= s.y[hi]) nm_update(s, hi, xc, val);
+    val2 = nm_corner<P>(c, s, S(0.5), hi, xc2);
+    if (s_finite(val2) && val2 <= s.y[hi]) {
+      nm_update(s, hi, xc2, val2);
+    } else {
+      bool bad = false;
+      for (int i = 0; i < 3; ++i) {
+        if (i == lo) continue;
+        for (int j = 0; j < 2; ++j) s.x[i][j] = S(0.5) * (s.x[i][j] + s.x[lo][j]);
+        S v = f_likelihood<P>(c, s.x[i][0], s.x[i][1]);
+        s.y[i] = v;
+        if (!s_finite(v)) bad = true;
+      }
+      nm_center(s);
+      nm_size(s);
+      if (bad) return 5;
+    }
+  }
+  if (s.S2 > S(0)) s.size = s_sqrt(s.S2);
+  else s.size = nm_size(s);
+  return 0;
+}
+
+template <class S>
+__device__ __forceinline__ int nm_lowest(const Simplex<S>& s) {
+  int lo = 0;
+  for (int i = 1; i < 3; ++i) if (s.y[i] < s.y[lo]) lo = i;
+  return lo;
+}
+
+// likelihood.c:428-554; sampling/edim/start are float as in the reference, the other reals are S
+// (double for F64, float for the mixed policy).
+template <class P>
+__device__ void likelihood_sampling(FitCtx<P>& c, typename P::S* mes_e1, typename P::S* mes_e2,
+                                    typename P::S maxL, int np_max, typename P::S* var_e1,
+                                    typename P::S* var_e2, typename P::S* oneDimvar) {
+  using S = typename P::S;
+  int error = 0;
+  int ie1, ie2, np;
+  S totL, L_e, average_1, average_2, cov, var1, var2, x_e1, x_e2;
+  S xL1, xL2, mod2 = S(0);
+  S L = S(1);
+  const S threshold = S(0.05);
+  const S max_e1 = *mes_e1, max_e2 = *mes_e2;
+  average_1 = max_e1;
+  average_2 = max_e2;
+  var1 = max_e1 * max_e1;
+  var2 = max_e2 * max_e2;
+  cov = max_e1 * max_e2;
+  totL = S(1);
+  np = 1;
+  float sampling = 0.05;
+  if (max_e1 < S(0)) sampling = -0.05;
+  int k1 = 0;
+  x_e1 = max_e1;
+  while (L > threshold && mod2 < S(1) && !error) {
+    x_e1 += sampling;
+    mod2 = x_e1 * x_e1 + max_e2 * max_e2;
+    if (mod2 < S(1)) {
+      L_e = loglike<P>(c, x_e1, max_e2, &error);
+      if (!error) { L = s_exp(L_e - maxL); k1++; }
+    }
+  }
+  if (L < threshold && k1 > 1) k1--;
+  L = S(1);
+  int k2 = 0;
+  sampling = 0.05;
+  if (max_e2 < S(0)) sampling = -0.05;
+  x_e2 = max_e2;
+  while (L > threshold && mod2 < S(1) && !error) {
+    x_e2 += sampling;
+    mod2 = x_e2 * x_e2 + max_e1 * max_e1;
+    if (mod2 < S(1)) {
+      L_e = loglike<P>(c, max_e1, x_e2, &error);
+      if (!error) { L = s_exp(L_e - maxL); k2++; }
+    }
+  }
+  if (L < threshold && k2 > 1) k2--;
+  sampling = 0.05;
+  float edim1 = k1 * sampling;
+  float edim2 = k2 * sampling;
+  float start1 = edim1;
+  float start2 = edim2;
+  while (np < np_max && sampling > kERes) {
+    for (ie1 = -start1 / sampling; ie1 <= start1 / sampling; ie1 += 2) {
+      for (ie2 = -start2 / sampling; ie2 <= start2 / sampling; ie2 += 2) {
+        if (ie1 != 0 || ie2 != 0) {
+          x_e1 = max_e1 + ie1 * sampling;
+          x_e2 = max_e2 + ie2 * sampling;
+          mod2 = x_e1 * x_e1 + x_e2 * x_e2;
+          if (mod2 < S(1)) {
+            L_e = loglike<P>(c, x_e1, x_e2, &error);
+            if (!error) {
+              L = s_exp(L_e - maxL);
+              if (L >= threshold && !isinf(L)) {
+                np++;
+                xL1 = x_e1 * L;
+                xL2 = x_e2 * L;
+                average_1 += xL1;
+                average_2 += xL2;
+                var1 += x_e1 * xL1;
+                var2 += x_e2 * xL2;
+                cov += x_e1 * xL2;
+                totL += L;
+              }
+            }
+          }
+        }
+      }
+    }
+    sampling *= 0.5;
+    start1 = edim1 - sampling;
+    start2 = edim2 - sampling;
+  }
+  average_1 /= totL;
+  average_2 /= totL;
+  var1 /= totL; var1 -= average_1 * average_1;
+  var2 /= totL; var2 -= average_2 * average_2;
+  cov /= totL; cov -= average_1 * average_2;
+  *mes_e1 = average_1;
+  *mes_e2 = average_2;
+  *var_e1 = var1;
+  *var_e2 = var2;
+  *oneDimvar = s_sqrt((var1) * (var2) - cov * cov);
+}
+
+// galaxy_fitting.c:41-117 with a configurable start point and step (reference: (0,0), 0.1)
+template <class P>
+__device__ FitOut fit_galaxy(FitCtx<P>& c, double start_e1, double start_e2, double step, int np_max) {
+  using S = typename P::S;
+  FitOut o;
+  Simplex<S> s;
+  int bad_start = 0;
+  // gsl_multimin_fminimizer_set: x0 and x0 + step along each axis
+  s.x[0][0] = S(start_e1); s.x[0][1] = S(start_e2);
+  s.y[0] = f_likelihood<P>(c, s.x[0][0], s.x[0][1]);
+  for (int i = 0; i < 2; ++i) {
+    s.x[i + 1][0] = S(start_e1); s.x[i + 1][1] = S(start_e2);
+    s.x[i + 1][i] = (i == 0 ? S(start_e1) : S(start_e2)) + S(step);
+    s.y[i + 1] = f_likelihood<P>(c, s.x[i + 1][0], s.x[i + 1][1]);
+  }
+  for (int i = 0; i < 3; ++i) if (!s_finite(s.y[i])) bad_start = 1;
+  nm_center(s);
+  s.size = nm_size(s);
+  int iter = 0, status = 0;
+  S fval = s.y[0];
+  int lo = 0;
+  if (!bad_start) {
+    do {
+      iter++;
+      status = nm_iterate<P>(c, s);
+      lo = nm_lowest(s);
+      fval = s.y[lo];
+      if (status) break;
+      status = (s.size < S(kTol)) ? 0 : -2;  // gsl_multimin_test_size
+    } while (status == -2 && iter < kSimplexMax && fval < S(0));
+  }
+  S e1 = s.x[lo][0], e2 = s.x[lo][1];
+  S maxL = -fval;
+  if (e1 * e1 + e2 * e2 > S(0.65)) maxL = S(-1e+10);
+  int error = 0;
+  S v1 = S(0), v2 = S(0), od = S(0);
+  if (bad_start) maxL = S(-1e+10);
+  if (maxL > S(-1.e+10)) {
+    likelihood_sampling<P>(c, &e1, &e2, maxL, np_max, &v1, &v2, &od);
+    if (v1 < S(kVar) || v2 < S(kVar) || od < S(kVar)) error = 1;
+  } else {
+    error = 1;
+  }
+  o.e1 = e1; o.e2 = e2; o.var_e1 = v1; o.var_e2 = v2; o.oneDimvar = od; o.maxL = maxL;
+  o.error = error; o.iters = iter; o.nevals = c.nevals;
+  o.status = bad_start ? 4 : 0;
+  return o;
+}
+
+// ------------------------------------------------------------------ kernels
+template <class P>
+__device__ __forceinline__ size_t cells_smem_bytes(int max_cells) {
+  return (size_t)5 * max_cells * sizeof(typename P::Cell);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kFitThreads, 1) k_fit(FacetBatch b) {
+  using Cell = typename P::Cell;
+  using S = typename P::S;
+  __shared__ FitShared<S> sh;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  Cell* gu = reinterpret_cast<Cell*>(dyn);
+  Cell* gv = gu + b.max_cells;
+  Cell* dre = gv + b.max_cells;
+  Cell* dim = dre + b.max_cells;
+  Cell* sig2 = dim + b.max_cells;
+  const int tid = threadIdx.x;
+  while (true) {
+    if (tid == 0) sh.g = atomicAdd(b.queue, 1);
+    __syncthreads();
+    const int g = sh.g;
+    if (g >= b.n_gal) break;
+    if (b.active && !b.active[g]) {
+      __syncthreads();
+      continue;
+    }
+    const int off = b.offset[g];
+    const int n = b.count[g];
+    const Cell* Gu = reinterpret_cast<const Cell*>(b.gu) + off;
+    const Cell* Gv = reinterpret_cast<const Cell*>(b.gv) + off;
+    const Cell* Dr = reinterpret_cast<const Cell*>(b.dre) + off;
+    const Cell* Di = reinterpret_cast<const Cell*>(b.dim) + off;
+    const Cell* Sg = reinterpret_cast<const Cell*>(b.sig2) + off;
+    for (int i = tid; i < n; i += blockDim.x) {
+      gu[i] = Gu[i]; gv[i] = Gv[i]; dre[i] = Dr[i]; dim[i] = Di[i]; sig2[i] = Sg[i];
+    }
+    for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[(size_t)g * kMaxNodes + i]);
+    if (tid == 0) { sh.newton = 0; sh.status = 0; }
+    __syncthreads();
+    double se1 = 0., se2 = 0., step = 0.1;
+    if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
+    FitCtx<P> c{&sh, gu, gv, dre, dim, sig2, n, 0};
+    FitOut o = fit_galaxy<P>(c, se1, se2, step, c_fit.np_max);
+    __syncthreads();
+    if (tid == 0) {
+      o.newton_iters = sh.newton;
+      o.status |= sh.status;
+      o.ncoords = n;
+      b.out[g] = o;
+    }
+    __syncthreads();
+  }
+}
+
+// one loglikelihood evaluation of galaxy 0 of the batch (C entry point loglikelihood)
+template <class P>
+__global__ void __launch_bounds__(kFitThreads, 1) k_loglike_once(FacetBatch b, double e1, double e2,
+                                                                  double* out2, double* node_L) {
+  using Cell = typename P::Cell;
+  using S = typename P::S;
+  __shared__ FitShared<S> sh;
+  const int n = b.count[0];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
+  if (tid == 0) { sh.newton = 0; sh.status = 0; }
+  __syncthreads();
+  int err = 0;
+  S L = eval_loglike<P>(sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
+                        reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
+                        reinterpret_cast<const Cell*>(b.sig2), n, S(e1), S(e2), &err);
+  if (tid == 0) { out2[0] = (double)L; out2[1] = (double)err; }
+  if (node_L && tid < kMaxNodes) node_L[tid] = (tid >= 1 && tid < c_fit.numr) ? (double)sh.Lr[tid] : 0.0;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, double e1, double e2,
+                                                                   double maxL, int np_max, double* out5) {
+  using Cell = typename P::Cell;
+  using S = typename P::S;
+  __shared__ FitShared<S> sh;
+  const int n = b.count[0];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
+  if (tid == 0) { sh.newton = 0; sh.status = 0; }
+  __syncthreads();
+  FitCtx<P> c{&sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
+              reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
+              reinterpret_cast<const Cell*>(b.sig2), n, 0};
+  S m1 = S(e1), m2 = S(e2), v1, v2, od;
+  likelihood_sampling<P>(c, &m1, &m2, S(maxL), np_max, &v1, &v2, &od);
+  if (tid == 0) { out5[0] = m1; out5[1] = m2; out5[2] = v1; out5[3] = v2; out5[4] = od; }
+}
+
+// loglikelihood_r (likelihood.c:156-187): one warp, writes the normalised model to visM
+__global__ void k_loglike_r(double e1, double e2, double scale, int n, const double* variance,
+                            const double* gu, const double* gv, const double* dre, const double* dim,
+                            double* visM, double* out_L, int gaussian) {
+  int it;
+  double L = node_loglike<PolicyF64>(gu, gv, dre, dim, variance, n, e1, e2, scale, gaussian, &it, visM,
+                                     nullptr, nullptr, nullptr);
+  if (threadIdx.x == 0) { out_L[0] = L; out_L[1] = it; }
+}
+
+// cross_correlation (likelihood.c:194-358) with a caller-supplied model: out = (ho, det, error)
+__global__ void k_xcorr(int n, const double* gu, const double* gv, const double* dre, const double* dim,
+                        const double* visMod, double* out3) {
+  int it;
+  double ho = 0, det = 0;
+  node_loglike<PolicyF64>(gu, gv, dre, dim, nullptr, n, 0., 0., 1., 0, &it, nullptr, visMod, &ho, &det);
+  if (threadIdx.x == 0) { out3[0] = ho; out3[1] = det; out3[2] = (det <= 0) ? 1.0 : 0.0; out3[3] = it; }
+}
+
+__global__ void k_marginalise_once(int n, const double* x, double* y, double* out1) {
+  __shared__ FitShared<double> sh;
+  const int lane = threadIdx.x;
+  if (lane == 0) { sh.status = 0; for (int i = 0; i < n; ++i) { sh.xs[i] = x[i]; sh.ys[i] = y[i]; } }
+  __syncwarp();
+  double L = marginalise_posterior_warp<double>(sh, n);
+  __syncwarp();
+  if (lane == 0) { out1[0] = L; for (int i = 0; i < n; ++i) y[i] = sh.ys[i]; }
+}
+
+__global__ void k_set_posterior(int numR, const double* Lr, const double* rprior, const double* ro,
+                                double* x, double* y, int* numvals) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int num = 0, nRo = 1;
+  while (nRo < numR && (Lr[nRo] <= kBad)) nRo++;
+  if (nRo < numR) {
+    for (nRo = 1; nRo < numR; nRo++) {
+      double lv = Lr[nRo];
+      if (lv > kBad) { x[num] = ro[nRo]; y[num] = lv + rprior[nRo]; num++; }
+    }
+  }
+  *numvals = num;
+}
+
+__global__ void k_position_marginal(int n, const double* x, double* y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = position_marginal(x[i]);
+}
+
+// ----------------------------------------------------------------- launchers
+static int check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "rlf: %s: %s\n", what, cudaGetErrorString(e));
+    return (int)e;
+  }
+  return 0;
+}
+
+int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
+  FitConst h;
+  memset(&h, 0, sizeof(h));
+  h.numr = cfg.numr;
+  h.gaussian = cfg.gaussian;
+  h.np_max = cfg.np_max;
+  for (int i = 0; i < kMaxNodes; ++i) {
+    h.ro[i] = (i < cfg.numr) ? cfg.ro[i] : 0.0;
+    h.rof[i] = (float)h.ro[i];
+  }
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_fit, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) { fprintf(stderr, "rlf: fit config: %s\n", cudaGetErrorString(e)); return (int)e; }
+  return 0;
+}
+
+template <class P>
+static int fit_launch_t(const FacetBatch& b, int grid, cudaStream_t st) {
+  size_t dyn = (size_t)5 * (b.max_cells > 0 ? b.max_cells : 1) * sizeof(typename P::Cell);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_fit<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    attr_set = true;
+  }
+  if (dyn > 160 * 1024) { fprintf(stderr, "rlf: facet too large for the fit kernel\n"); return 1; }
+  k_fit<P><<<grid, kFitThreads, dyn, st>>>(b);
+  return check("k_fit");
+}
+
+int fit_launch(const FacetBatch& b, Precision p, int grid, cudaStream_t st) {
+  if (b.n_gal <= 0) return 0;
+  if (grid > b.n_gal) grid = b.n_gal;
+  if (grid < 1) grid = 1;
+  return p == kF64 ? fit_launch_t<PolicyF64>(b, grid, st) : fit_launch_t<PolicyMixed>(b, grid, st);
+}
+
+int fit_max_grid(Precision p) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per = 1;
+  if (p == kF64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit<PolicyF64>, kFitThreads, 5 * 1156 * 8);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit<PolicyMixed>, kFitThreads, 5 * 1156 * 4);
+  if (per < 1) per = 1;
+  return sms * per;
+}
+
+int launch_loglikelihood_r(double e1, double e2, double scale, int n, const double* variance,
+                           const double* gu, const double* gv, const double* dre, const double* dim,
+                           double* visM, double* out_L, int gaussian, cudaStream_t st) {
+  k_loglike_r<<<1, 32, 0, st>>>(e1, e2, scale, n, variance, gu, gv, dre, dim, visM, out_L, gaussian);
+  return check("k_loglike_r");
+}
+int launch_cross_correlation(int n, const double* gu, const double* gv, const double* dre,
+                             const double* dim, const double* visMod, double* out3, cudaStream_t st) {
+  k_xcorr<<<1, 32, 0, st>>>(n, gu, gv, dre, dim, visMod, out3);
+  return check("k_xcorr");
+}
+int launch_loglikelihood(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
+                         cudaStream_t st) {
+  k_loglike_once<PolicyF64><<<1, kFitThreads, 0, st>>>(b, e1, e2, out2, node_L);
+  return check("k_loglike_once");
+}
+int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
+                               double* out5, cudaStream_t st) {
+  k_sampling_once<PolicyF64><<<1, kFitThreads, 0, st>>>(b, e1, e2, maxL, np_max, out5);
+  return check("k_sampling_once");
+}
+int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st) {
+  k_marginalise_once<<<1, 32, 0, st>>>(n, x, y, out1);
+  return check("k_marginalise_once");
+}
+int launch_set_posterior_values(int numR, const double* Lr, const double* rprior, const double* ro,
+                                double* x, double* y, int* numvals, cudaStream_t st) {
+  k_set_posterior<<<1, 32, 0, st>>>(numR, Lr, rprior, ro, x, y, numvals);
+  return check("k_set_posterior");
+}
+int launch_position_marginal(int n, const double* x, double* y, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_position_marginal<<<(n + 127) / 128, 128, 0, st>>>(n, x, y);
+  return check("k_position_marginal");
+}
+
+}  // namespace rlf
