@@ -25,6 +25,7 @@ typedef struct {
   int newton_iters;  /* Newton iterations over all nodes and evaluations */
   int status;        /* 0, or device-side limits reached (2: QAG intervals, 4: bad simplex start) */
   int ncoords;       /* facet cells */
+  double max_e1, max_e2;  /* simplex maximum, before the likelihood sampling */
 } rlf_fit_result;
 
 typedef struct {
@@ -73,6 +74,13 @@ int rlf_obs_restore(rlf_observation *obs);
 int rlf_obs_process(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
                     const double *l, const double *m, int numr, const double *ro,
                     const rlf_options *opt, rlf_fit_result *out, int *n_bad);
+/* extraction only (source_extraction + evaluate_facet_coords of every galaxy against the current
+ * data and sky model, `batch` galaxies per pass): facets[g][5][stride] receives the cell centres
+ * (u, v), the facet visibilities divided by their variances (re, im) and the variances;
+ * ncoords[g] the number of cells */
+int rlf_obs_extract(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                    const double *l, const double *m, int batch, double *facets, int stride,
+                    int *ncoords);
 /* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
  * [total, extract, fit, remove] */
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);

@@ -558,6 +558,8 @@ int orc_source_fitting(orc_params *par, double start_e1, double start_e2, double
     status = gsl_multimin_test_size(size, ORC_TOL);
   } while (status == GSL_CONTINUE && iter < 50 && s->fval < 0.);
   double e1 = gsl_vector_get(s->x, 0), e2 = gsl_vector_get(s->x, 1), maxL = -s->fval;
+  out->max_e1 = e1;
+  out->max_e2 = e2;
   if (e1 * e1 + e2 * e2 > 0.65) maxL = -1e+10;
   int error = 0;
   double v1 = 0., v2 = 0., od = 0.;

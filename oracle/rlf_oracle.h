@@ -38,6 +38,7 @@ typedef struct {
   int error;      /* source_fitting return value */
   int iters;      /* simplex iterations */
   long nevals;    /* likelihood evaluations (simplex + sampling) */
+  double max_e1, max_e2;  /* simplex maximum, before the sampling */
 } orc_fit_result;
 
 unsigned int orc_facet_size(double theta_med, double len);

@@ -27,7 +27,8 @@ class FitResult(C.Structure):
     """rlf_fit_result (include/rlf_gb300.h)"""
     _fields_ = [("e1", D), ("e2", D), ("var_e1", D), ("var_e2", D), ("oneDimvar", D), ("maxL", D),
                 ("error", C.c_int), ("iters", C.c_int), ("nevals", C.c_int),
-                ("newton_iters", C.c_int), ("status", C.c_int), ("ncoords", C.c_int)]
+                ("newton_iters", C.c_int), ("status", C.c_int), ("ncoords", C.c_int),
+                ("max_e1", D), ("max_e2", D)]
 
 
 class Options(C.Structure):
@@ -63,6 +64,7 @@ def load():
         "rlf_obs_process": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.c_int, PD,
                                       C.POINTER(Options), C.POINTER(FitResult), PI]),
         "rlf_obs_last_timing": (C.c_int, [C.c_void_p, PD]),
+        "rlf_obs_extract": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.c_int, PD, C.c_int, PI]),
         # reference-named drop-in entry points
         "facet_size": (C.c_uint, [D, D]),
         "evaluate_uv_grid_size": (C.c_uint, [C.c_int, C.c_int, D, PD, C.c_uint, C.c_uint, PD, PD, C.c_uint, PU8]),
@@ -106,7 +108,7 @@ EXPORTED = [
     "rlf_version", "rlf_device_count", "rlf_configure", "rlf_obs_create", "rlf_obs_destroy",
     "rlf_obs_set_vis", "rlf_obs_set_data_c64", "rlf_obs_get_vis", "rlf_obs_simulate",
     "rlf_obs_sky_model", "rlf_obs_snapshot", "rlf_obs_restore", "rlf_obs_process",
-    "rlf_obs_last_timing", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
+    "rlf_obs_last_timing", "rlf_obs_extract", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
     "gridding_visibilities", "average_facets", "gaussian_shape", "sersic_shape",
     "model_galaxy_visibilities_at_zero", "data_galaxy_visibilities", "data_visibilities_phase_shift",
     "f_likelihood", "loglikelihood", "loglikelihood_r", "cross_correlation",

@@ -13,6 +13,7 @@
 #include "rlf_device.cuh"
 #include "rlf_fit.cuh"
 #include "rlf_vis.cuh"
+#include "rlf_batch.cuh"
 #include "../../include/rlf_gb300.h"
 
 typedef struct {
@@ -153,6 +154,9 @@ struct rlf_observation {
   rlf::DevBuf<float2> data32, sky32, data32_0, sky32_0;
   std::map<unsigned, rlf::FacetCache*> facets;
   rlf::DevBuf<double> partial;
+  rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
+  rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
+  double max_delay_m = 0;
   int n_part = 0;
   double ms[4] = {0, 0, 0, 0};
   ~rlf_observation() {
@@ -253,7 +257,8 @@ static std::vector<GalaxyParams> make_gals(int n, const double* flux, const doub
 // waits once at the end.  With batch = 1 the order of operations is the reference's.
 static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, const std::vector<int>& order,
                     int numr, const double* ro, const rlf_options& opt, std::vector<FitOut>& out,
-                    cudaStream_t st, double* ms3) {
+                    cudaStream_t st, double* ms3, double* facets_out = nullptr, int* ncoords_out = nullptr,
+                    int facets_stride = 0) {
   const int n = (int)order.size();
   out.assign(n, FitOut{});
   if (n == 0) return 0;
@@ -325,11 +330,64 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   std::vector<cudaEvent_t> ev((size_t)nbatches * 3 + 1);
   for (auto& e : ev) RLF_CUDA(cudaEventCreate(&e));
   const int grid_fit = fit_max_grid(prec);
+  // batched extraction/removal: mixed precision, batch > 1, evenly spaced channels
+  bool batched = prec == kMixed && B > 1;
+  if (batched) {
+    const int bc = batch_set_channels(ob->n_ch, ob->wavenumbers.data(), ob->spec.data(), ob->max_delay_m, st);
+    if (bc < 0) batched = false;
+    else if (bc > 0) return bc;
+  }
+  if (batched && !ob->rows.p) {
+    RLF_OK(ob->rows.ensure(ob->n_rows));
+    RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
+  }
+  const int ctas_per_group = std::max(1, std::min(1024, (ob->n_rows + 4095) / 4096));
+  DevBuf<int> dgidx;
   RLF_CUDA(cudaEventRecord(ev[0], st));
   for (int bi = 0; bi < nbatches; ++bi) {
     const int b0 = bi * B;
     const int bn = std::min(B, n - b0);
-    for (int k = 0; k < bn; ++k) {
+    FacetOut fo;
+    fo.offset = doff.p;
+    fo.ncoords = dnc.p + b0;
+    fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
+    fo.as_float = prec == kMixed;
+    std::vector<int> single;  // galaxies extracted one at a time
+    if (batched) {
+      // group the batch by facet size, 32 galaxies per warp-group
+      std::map<int, std::vector<int>> byF;
+      for (int k = 0; k < bn; ++k) {
+        const int F = facets[b0 + k];
+        if ((unsigned)F <= kBatchMaxFacet) byF[F].push_back(k);
+        else single.push_back(k);
+      }
+      std::vector<int> hgidx;
+      std::vector<std::pair<int, std::pair<int, int>>> launches;  // F -> (first group, n_groups)
+      for (auto& kv : byF) {
+        const int ng = ((int)kv.second.size() + 31) / 32;
+        launches.push_back({kv.first, {(int)hgidx.size() / 32, ng}});
+        for (int j = 0; j < ng * 32; ++j) hgidx.push_back(j < (int)kv.second.size() ? kv.second[j] : -1);
+      }
+      if (!hgidx.empty()) {
+        RLF_OK(dgidx.upload(hgidx.data(), hgidx.size(), st));
+        size_t need = 0;
+        for (auto& L : launches) need = std::max(need, (size_t)L.second.second * ctas_per_group * L.first * L.first * 32);
+        RLF_OK(ob->bpartial.ensure(need));
+        for (auto& L : launches) {
+          const int F = L.first, g0 = L.second.first, ng = L.second.second;
+          FacetCache* fcF = nullptr;
+          RLF_OK(obs_facet(ob, (unsigned)F, &fcF, st));
+          RLF_OK(launch_extract_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, fcF->cell.p, dg.p + b0,
+                                      dgidx.p + (size_t)g0 * 32, ng, F, ctas_per_group, opt.gaussian, ob->bpartial.p,
+                                      st));
+          RLF_OK(launch_finalize_batch(ng, ctas_per_group, F, ob->bpartial.p, dgidx.p + (size_t)g0 * 32, fcF->ss.p,
+                                       fcF->sw.p, ob->len, fo, st));
+        }
+      }
+    } else {
+      for (int k = 0; k < bn; ++k) single.push_back(k);
+    }
+    for (int k : single) {
       const int i = b0 + k;
       const unsigned F = (unsigned)facets[i];
       if (prec == kF64)
@@ -338,15 +396,35 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       else
         RLF_OK(launch_extract_mixed(o, ob->data32.p, ob->sky32.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
                                     ob->partial.p, ob->n_part, st));
-      FacetOut fo;
-      fo.offset = doff.p + k;
-      fo.ncoords = dnc.p + i;
-      fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
-      fo.as_float = prec == kMixed;
-      RLF_OK(launch_facet_finalize(1, dfac.p + i, ob->partial.p, ob->n_part, 0, dss.p + i, dsw.p + i, ob->len,
-                                   fo, st));
+      FacetOut f1 = fo;
+      f1.offset = doff.p + k;
+      f1.ncoords = dnc.p + i;
+      double* sums = ob->partial.p + (size_t)ob->n_part * 2 * F * F;
+      RLF_OK(launch_reduce_partials(ob->partial.p, ob->n_part, 2 * F * F, sums, st));
+      RLF_OK(launch_facet_finalize(1, dfac.p + i, sums, 1, 0, dss.p + i, dsw.p + i, ob->len, f1, st));
     }
     RLF_CUDA(cudaEventRecord(ev[3 * bi + 1], st));
+    if (facets_out) {
+      // extraction only: hand the packed facets of this batch back as doubles
+      std::vector<int> nc(bn);
+      RLF_CUDA(cudaMemcpyAsync(nc.data(), dnc.p + b0, bn * sizeof(int), cudaMemcpyDeviceToHost, st));
+      std::vector<unsigned char> h(5 * plane);
+      RLF_CUDA(cudaMemcpyAsync(h.data(), cells.p, h.size(), cudaMemcpyDeviceToHost, st));
+      RLF_CUDA(cudaStreamSynchronize(st));
+      for (int k = 0; k < bn; ++k) {
+        ncoords_out[b0 + k] = nc[k];
+        for (int a = 0; a < 5; ++a)
+          for (int c = 0; c < nc[k] && c < facets_stride; ++c) {
+            const size_t src = (size_t)a * plane + ((size_t)k * max_cells + c) * esz;
+            const double v = esz == sizeof(double) ? *reinterpret_cast<const double*>(&h[src])
+                                                   : (double)*reinterpret_cast<const float*>(&h[src]);
+            facets_out[((size_t)(b0 + k) * 5 + a) * facets_stride + c] = v;
+          }
+      }
+      RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
+      RLF_CUDA(cudaEventRecord(ev[3 * bi + 3], st));
+      continue;
+    }
     FacetBatch fb;
     fb.n_gal = bn;
     fb.max_cells = max_cells;
@@ -360,14 +438,19 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fb.queue = dqueue.p + bi;
     RLF_OK(fit_launch(fb, prec, std::min(grid_fit, bn), st));
     RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
-    for (int k = 0; k < bn; ++k) {
-      const int i = b0 + k;
-      const double* e12 = &dout.p[i].e1;
-      const int* err = &dout.p[i].error;
-      if (prec == kF64)
-        RLF_OK(launch_remove_f64(o, ob->data64.p, ob->sky64.p, dg.p + i, e12, err, opt.gaussian, st));
-      else
-        RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
+    if (batched) {
+      RLF_OK(launch_remove_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, dg.p + b0, dout.p + b0, bn,
+                                 opt.gaussian, st));
+    } else {
+      for (int k = 0; k < bn; ++k) {
+        const int i = b0 + k;
+        const double* e12 = &dout.p[i].e1;
+        const int* err = &dout.p[i].error;
+        if (prec == kF64)
+          RLF_OK(launch_remove_f64(o, ob->data64.p, ob->sky64.p, dg.p + i, e12, err, opt.gaussian, st));
+        else
+          RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
+      }
     }
     RLF_CUDA(cudaEventRecord(ev[3 * bi + 3], st));
   }
@@ -443,7 +526,9 @@ static rlf_observation* obs_create(int n_rows, int n_ch, const double* uu, const
   ob->len = len;
   ob->wavenumbers.assign(wavenumbers, wavenumbers + n_ch);
   ob->spec.assign(spec, spec + n_ch);
-  ob->n_part = grid_partial_blocks();
+  ob->n_part = grid_partial_blocks(n_rows);
+  for (int i = 0; i < n_rows; ++i)
+    ob->max_delay_m = std::max(ob->max_delay_m, fabs(uu[i]) + fabs(vv[i]) + fabs(ww[i]));
   int r = ob->uu.upload(uu, n_rows, st);
   if (!r) r = ob->vv.upload(vv, n_rows, st);
   if (!r) r = ob->ww.upload(ww, n_rows, st);
@@ -709,6 +794,22 @@ int rlf_obs_process(rlf_observation* obs, int n_gal, const double* flux, const d
   return process(obs, n_gal, flux, scale, l, m, numr, ro, o, out, n_bad, st);
 }
 
+int rlf_obs_extract(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* l,
+                    const double* m, int batch, double* facets, int stride, int* ncoords) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  const unsigned fmax = rlf::facet_size(kRMax, obs->len);
+  std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, fmax);
+  std::vector<int> order(n_gal);
+  for (int i = 0; i < n_gal; ++i) order[i] = i;
+  rlf_options o = g_lib.opt;
+  o.batch = batch;
+  std::vector<FitOut> out;
+  std::vector<double> ro(kMaxNodes, 1.0);
+  return run_pass(obs, gals, order, 24, ro.data(), o, out, st, nullptr, facets, ncoords, stride);
+}
+
 int rlf_obs_last_timing(rlf_observation* obs, double* ms4) {
   for (int k = 0; k < 4; ++k) ms4[k] = obs->ms[k];
   return 0;
@@ -780,7 +881,7 @@ void gridding_visibilities(double* wavenumbers, unsigned int num_channels, unsig
   if (lib_stream(&st)) return;
   if (set_channels((int)num_channels, wavenumbers, nullptr, st)) return;
   const size_t nv = (size_t)num_channels * ncoords, nc = (size_t)sizeg * sizeg;
-  const int n_part = grid_partial_blocks();
+  const int n_part = grid_partial_blocks((int)ncoords);
   Observation o;
   o.n_rows = (int)ncoords; o.n_ch = (int)num_channels; o.lay.s_row = 1; o.lay.s_ch = ncoords; o.len = len;
   if (g_lib.d0.upload(u, ncoords, st) || g_lib.d1.upload(v, ncoords, st)) return;
@@ -1084,7 +1185,9 @@ void source_extraction(int rank, unsigned int facet, likelihood_params* par, com
   fo.ncoords = dnc.p;
   fo.gu = cells.p; fo.gv = cells.p + nc; fo.dre = cells.p + 2 * nc; fo.dim = cells.p + 3 * nc; fo.sig2 = cells.p + 4 * nc;
   fo.as_float = 0;
-  if (launch_facet_finalize(1, dfac.p, ob->partial.p, ob->n_part, 0, dss.p, dsw.p, len, fo, st)) { delete ob; return; }
+  double* sums = ob->partial.p + (size_t)ob->n_part * 2 * nc;
+  if (launch_reduce_partials(ob->partial.p, ob->n_part, 2 * nc, sums, st) ||
+      launch_facet_finalize(1, dfac.p, sums, 1, 0, dss.p, dsw.p, len, fo, st)) { delete ob; return; }
   int n = 0;
   std::vector<double> h((size_t)5 * nc);
   cudaMemcpyAsync(&n, dnc.p, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -150,33 +150,84 @@ template <> struct Acc<float> {
   __device__ __forceinline__ float reduce() const { return uwarp_sum_df(s, -c); }
 };
 
-// ------------------------------------------------------- position marginal (FP32)
-// Same quantity as position_marginal() (likelihood.c:376-421) in FP32: Ei by its power series
-// (compensated) for x <= 25 and its asymptotic series above, the difference formed in the log
-// domain above 25 so that e^x never overflows single precision.
-__device__ __forceinline__ float ei_series_f(float x) {
-  float term = 1.f, s = 0.f, c = 0.f;
-  for (int k = 1; k < 200; ++k) {
-    term = term * x / (float)k;
-    float t = term / (float)k;
-    float y = t - c, u = s + y;
-    c = (u - s) - y;
-    s = u;
-    if (t < 1e-9f * s) break;
+// ----------------------------------------------------------- position marginal
+// likelihood.c:376-421 evaluated by a whole warp (every lane calls it with the same x).  Ei(x)
+// comes from its power series  gamma + ln x + sum_k a_k / k,  a_k = x^k / k!,  or, for large x,
+// from the asymptotic series  e^x / x sum_k k! / x^k  stopped before its smallest term.  The
+// 32 lanes take 32 consecutive k per round and form a_k as a prefix product of x/k across the
+// warp (Hillis-Steele scan), so a series of up to ~100 terms costs 4 rounds instead of 100
+// dependent steps with divisions.  The FP32 form keeps the asymptotic branch in the log domain
+// (e^x overflows single precision above 88).
+template <class S> __device__ __forceinline__ S wsum(S v);
+template <> __device__ __forceinline__ double wsum<double>(double v) { return uwarp_sum(v); }
+template <> __device__ __forceinline__ float wsum<float>(float v) { return uwarp_sum_df(v, 0.f); }
+
+template <class S>
+__device__ __forceinline__ S warp_prefix_prod(S f) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const S g = __shfl_up_sync(0xffffffffu, f, o);
+    if (lane >= o) f *= g;
   }
-  return (float)kEulerGamma + logf(x) + (s - c);
+  return f;
+}
+
+// sum_{k>=1} x^k / (k k!)
+template <class S>
+__device__ __forceinline__ S ei_series_sum_warp(S x, S eps) {
+  const int lane = threadIdx.x & 31;
+  S base = S(1), sum = S(0);
+  for (int j = 0; j < 12; ++j) {
+    const S k = S(32 * j + lane + 1);
+    const S a = base * warp_prefix_prod<S>(x / k);
+    const S t = a / k;
+    sum += wsum<S>(t);
+    base = __shfl_sync(0xffffffffu, a, 31);
+    const S last = __shfl_sync(0xffffffffu, t, 31);
+    if (S(32 * j + 32) > x && last < eps * sum) break;
+  }
+  return sum;
+}
+
+// sum_{k>=0} k!/x^k over the decreasing part of the asymptotic series
+template <class S>
+__device__ __forceinline__ S ei_asym_sum_warp(S x, S eps) {
+  const int lane = threadIdx.x & 31;
+  S base = S(1), sum = S(1);
+  for (int j = 0; j < 8; ++j) {
+    const S k = S(32 * j + lane + 1);
+    const S b = base * warp_prefix_prod<S>(k / x);
+    const bool keep = (k < x) && (b >= eps);
+    sum += wsum<S>(keep ? b : S(0));
+    base = __shfl_sync(0xffffffffu, b, 31);
+    if (!(S(32 * j + 32) < x) || base < eps) break;
+  }
+  return sum;
+}
+
+__device__ __forceinline__ double ei_warp(double x) {
+  if (x <= 40.0) return kEulerGamma + log(x) + ei_series_sum_warp<double>(x, 1e-18);
+  return exp(x) / x * ei_asym_sum_warp<double>(x, 1e-18);
+}
+
+__device__ double pos_marg(double x) {
+  const double Delta = 0.5 * 5.991;
+  if (x <= Delta) return kBad;
+  if (x > 100.) return x - log(Delta) - exp(-Delta);
+  if ((x - Delta) < 0.0001) x = Delta + 0.0001;
+  const double yc = ei_warp(x), ys = ei_warp(x - Delta);
+  return log((yc - ys) / log(x / (x - Delta)));
+}
+
+__device__ __forceinline__ float ei_series_f(float x) {
+  return (float)kEulerGamma + logf(x) + ei_series_sum_warp<float>(x, 1e-9f);
 }
 __device__ __forceinline__ float log_ei_asym_f(float x) {  // ln Ei(x), x >= 25
-  float term = 1.f, sum = 1.f;
-  for (int k = 1; k < 60; ++k) {
-    float next = term * (float)k / x;
-    if (next >= term || next < 1e-9f * sum) break;
-    term = next;
-    sum += term;
-  }
-  return x - logf(x) + logf(sum);
+  return x - logf(x) + logf(ei_asym_sum_warp<float>(x, 1e-9f));
 }
-__device__ __forceinline__ float position_marginal_f(float x) {
+
+__device__ float pos_marg(float x) {
   const float Delta = 0.5f * 5.991f;
   if (x <= Delta) return (float)kBad;
   if (x > 100.f) return x - logf(Delta) - expf(-Delta);
@@ -192,8 +243,6 @@ __device__ __forceinline__ float position_marginal_f(float x) {
   const float la = log_ei_asym_f(x), lb = log_ei_asym_f(xd);
   return la + log1pf(-expf(lb - la)) - lden;
 }
-__device__ __forceinline__ double pos_marg(double x) { return position_marginal(x); }
-__device__ __forceinline__ float pos_marg(float x) { return position_marginal_f(x); }
 
 // --------------------------------------------------------------- cell model
 template <class S>
@@ -368,10 +417,6 @@ __device__ __forceinline__ S rescale_error(S err, S result_abs, S result_asc) {
   }
   return err;
 }
-
-template <class S> __device__ __forceinline__ S wsum(S v);
-template <> __device__ __forceinline__ double wsum<double>(double v) { return uwarp_sum(v); }
-template <> __device__ __forceinline__ float wsum<float>(float v) { return uwarp_sum_df(v, 0.f); }
 
 // QUADPACK qk41 on one warp: lane j < 21 evaluates the integrand at centre -+ half*xgk[j].
 template <class S>
@@ -882,6 +927,8 @@ __device__ FitOut fit_galaxy(FitCtx<P>& c, double start_e1, double start_e2, dou
   } else {
     error = 1;
   }
+  o.max_e1 = (double)s.x[lo][0];
+  o.max_e2 = (double)s.x[lo][1];
   o.e1 = e1; o.e2 = e2; o.var_e1 = v1; o.var_e2 = v2; o.oneDimvar = od; o.maxL = maxL;
   o.error = error; o.iters = iter; o.nevals = c.nevals;
   o.status = bad_start ? 4 : 0;

@@ -14,6 +14,7 @@ struct FitOut {
   int newton_iters;  // Newton iterations summed over scalelength nodes and evaluations
   int status;        // 0 ok; bit 1: QAG interval capacity reached; bit 2: non-finite simplex start
   int ncoords;       // facet cells used
+  double max_e1, max_e2;  // simplex maximum (before the sampling of likelihood.c:428-554)
 };
 
 enum Precision { kF64 = 0, kMixed = 1 };

@@ -24,6 +24,9 @@ struct ChanConst {
 __constant__ ChanConst c_ch[kMaxCh];
 __constant__ int c_nch;
 
+#define RLF_VIS_OK(call) do { int r_ = (call); if (r_) return r_; } while (0)
+int launch_reduce_partials(const double* partial, int n_part, int len, double* sums, cudaStream_t st);
+
 static int check(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -61,11 +64,34 @@ int set_channels(int n_ch, const double* wavenumbers, const double* spec, cudaSt
   return 0;
 }
 
-int grid_partial_blocks() {
+int grid_partial_blocks(int n_rows) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms * 4;
+  // ~2048 rows per CTA at most 4 CTAs per SM: few partials for small observations
+  const int want = (n_rows + 2047) / 2048;
+  return want < 1 ? 1 : (want > sms * 4 ? sms * 4 : want);
+}
+
+// partial [n_part][arrays * nc] -> sums [arrays * nc], one CTA per value, fixed-order tree
+__global__ void k_reduce_partials(const double* __restrict__ partial, int n_part, int len, double* __restrict__ sums) {
+  __shared__ double ws[8];
+  const int c = blockIdx.x;
+  double s = 0.0;
+  for (int p = threadIdx.x; p < n_part; p += blockDim.x) s += partial[(size_t)p * len + c];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+    sums[c] = t;
+  }
+}
+
+int launch_reduce_partials(const double* partial, int n_part, int len, double* sums, cudaStream_t st) {
+  k_reduce_partials<<<len, 256, 0, st>>>(partial, n_part, len, sums);
+  return check("k_reduce_partials");
 }
 
 // ------------------------------------------------------------- cell index
@@ -142,8 +168,11 @@ int launch_grid_weights(const Observation& o, const uint16_t* cell, const float*
   k_grid_weights<<<n_part, 256, facet_smem(F, 2, (const void*)k_grid_weights), st>>>(o, cell, sigma2, F, partial);
   int e = check("k_grid_weights");
   if (e) return e;
-  k_reduce_pairs<<<(nc + 255) / 256, 256, 0, st>>>(partial, n_part, nc, sum_sigma2, sum_w);
-  return check("k_reduce_pairs");
+  double* sums = partial + (size_t)n_part * 2 * nc;
+  RLF_VIS_OK(launch_reduce_partials(partial, n_part, 2 * nc, sums, st));
+  cudaMemcpyAsync(sum_sigma2, sums, nc * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(sum_w, sums + nc, nc * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  return check("grid_weights copy");
 }
 
 // --------------------------------------------------------- extraction F64
@@ -786,7 +815,7 @@ int launch_grid_vis_finalize(const double* partial, int n_part, unsigned F, doub
                              double* sum_w, cudaStream_t st) {
   const int nc = F * F;
   double* sums = const_cast<double*>(partial) + (size_t)n_part * 4 * nc;  // scratch after the partials
-  k_grid_vis_reduce<<<(4 * nc + 255) / 256, 256, 0, st>>>(partial, n_part, nc, sums);
+  RLF_VIS_OK(launch_reduce_partials(partial, n_part, 4 * nc, sums, st));
   k_grid_vis_compact<<<1, 32, 0, st>>>(sums, nc, new_vis, new_sigma2, sum_w);
   return check("k_grid_vis_finalize");
 }

@@ -47,7 +47,9 @@ int launch_cell_index(const Observation& o, const uint8_t* flag, unsigned F, uin
 int launch_grid_weights(const Observation& o, const uint16_t* cell, const float* sigma2,
                         unsigned F, double* partial, int n_part, double* sum_sigma2,
                         double* sum_w, cudaStream_t st);
-int grid_partial_blocks();
+int grid_partial_blocks(int n_rows);
+// partial [n_part][len] -> sums [len] (fixed-order reduction, one CTA per element)
+int launch_reduce_partials(const double* partial, int n_part, int len, double* sums, cudaStream_t st);
 
 // source extraction of one galaxy into per-CTA facet partials (F64 or mixed data)
 int launch_extract_f64(const Observation& o, const double2* data, const double2* sky,

@@ -23,7 +23,7 @@ def _d(a):
 RESULT_DTYPE = np.dtype([("e1", "f8"), ("e2", "f8"), ("var_e1", "f8"), ("var_e2", "f8"),
                          ("oneDimvar", "f8"), ("maxL", "f8"), ("error", "i4"), ("iters", "i4"),
                          ("nevals", "i4"), ("newton_iters", "i4"), ("status", "i4"),
-                         ("ncoords", "i4")])
+                         ("ncoords", "i4"), ("max_e1", "f8"), ("max_e2", "f8")])
 
 
 @dataclass
@@ -128,3 +128,21 @@ class DeviceObservation:
         ms = (C.c_double * 4)()
         self.lib.rlf_obs_last_timing(self.h, ms)
         return ProcessResult(res, nbad.value, tuple(ms))
+
+    def extract(self, cat: Catalogue, *, batch: int = 1):
+        """Facets of every galaxy against the current data and sky model (no fit, no removal).
+        Returns a list of (u, v, vis/sigma2, sigma2) arrays per galaxy."""
+        fmax = K.facet_size(K.RMAX, self.obs.len_lambda)
+        stride = fmax * fmax
+        arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
+        buf = np.zeros((cat.n, 5, stride))
+        nc = np.zeros(cat.n, np.int32)
+        self._check(self.lib.rlf_obs_extract(self.h, cat.n, *[p for _, p in arrs], int(batch),
+                                             buf.ctypes.data_as(_lib.PD), stride, nc.ctypes.data_as(_lib.PI)),
+                    "rlf_obs_extract")
+        out = []
+        for g in range(cat.n):
+            n = int(nc[g])
+            out.append((buf[g, 0, :n].copy(), buf[g, 1, :n].copy(), buf[g, 2, :n] + 1j * buf[g, 3, :n],
+                        buf[g, 4, :n].copy()))
+        return out

@@ -41,7 +41,8 @@ class OrcParams(C.Structure):
 
 class OrcFitResult(C.Structure):
     _fields_ = [("e1", D), ("e2", D), ("var_e1", D), ("var_e2", D), ("oneDimvar", D),
-                ("maxL", D), ("error", C.c_int), ("iters", C.c_int), ("nevals", C.c_long)]
+                ("maxL", D), ("error", C.c_int), ("iters", C.c_int), ("nevals", C.c_long),
+                ("max_e1", D), ("max_e2", D)]
 
 
 def _build_oracle():
@@ -62,6 +63,9 @@ def load_oracle():
     lib.orc_gridding.argtypes = [PD, C.c_uint, C.c_uint, PD, PD, PC, PF, D, C.c_uint, PC, PD, PU8, PD]
     lib.orc_average_facets.restype = None
     lib.orc_average_facets.argtypes = [C.c_ulong, PC, PD, PD]
+    for nm in ("orc_sersic_shape", "orc_gaussian_shape"):
+        getattr(lib, nm).restype = D
+        getattr(lib, nm).argtypes = [D, D, D, D]
     lib.orc_model_at_zero.restype = None
     lib.orc_model_at_zero.argtypes = [D, D, D, C.c_uint, PD, PD, PD, PD, C.c_int]
     lib.orc_data_galaxy_vis.restype = None

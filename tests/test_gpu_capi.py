@@ -195,13 +195,13 @@ def test_likelihood_functions(lib, orc, case, sky):
     # loglikelihood and f_likelihood
     for e1, e2 in [(0.0, 0.0), (0.1, 0.05), (-0.3, 0.2), (0.5, 0.5)]:
         err1, err2 = C.c_int(0), C.c_int(0)
-        a = lib.loglikelihood(C.cast(C.byref(p), C.c_void_p), e1, e2, C.byref(err1))
+        a = lib.loglikelihood(C.c_void_p(C.addressof(p)), e1, e2, C.byref(err1))
         b = orc.orc_loglikelihood(C.byref(op), e1, e2, C.byref(err2))
         assert err1.value == err2.value
         assert a == pytest.approx(b, rel=1e-10, abs=1e-9)
         x = np.array([e1, e2])
         v = GslVector(2, 1, dptr(x), None, 0)
-        assert lib.f_likelihood(C.byref(v), C.cast(C.byref(p), C.c_void_p)) == pytest.approx(-b, rel=1e-10, abs=1e-9)
+        assert lib.f_likelihood(C.byref(v), C.c_void_p(C.addressof(p))) == pytest.approx(-b, rel=1e-10, abs=1e-9)
 
 
 def test_marginalise_posterior(lib, orc):
@@ -249,7 +249,7 @@ def test_source_fitting_and_sampling(lib, orc, case, sky):
         v1 = [C.c_double() for _ in range(3)]
         v2 = [C.c_double() for _ in range(3)]
         maxL = orc.orc_loglikelihood(C.byref(op), 0.05, -0.02, C.byref(C.c_int()))
-        lib.likelihood_sampling(C.byref(m1[0]), C.byref(m1[1]), maxL, C.cast(C.byref(p), C.c_void_p), 30,
+        lib.likelihood_sampling(C.byref(m1[0]), C.byref(m1[1]), maxL, C.c_void_p(C.addressof(p)), 30,
                                 *[C.byref(x) for x in v1])
         orc.orc_likelihood_sampling(C.byref(m2[0]), C.byref(m2[1]), maxL, C.byref(op), 30, *[C.byref(x) for x in v2])
         assert m1[0].value == pytest.approx(m2[0].value, abs=1e-9)
