@@ -171,6 +171,86 @@ def cpu_baseline_sample(obs, cat, galaxies=1):
     return ns
 
 
+def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup):
+    """Galaxies/s through the reference-facing entry point data_processing() with pinned host
+    buffers: catalogue pass + re-fit pass (RadioLensfit2.cpp:597-606), copies inside the timing."""
+    import torch
+    from radiolensfit2_gb300 import _lib
+    from radiolensfit2_gb300.abi import LikelihoodParams, dptr, fptr, cptr, bptr
+    opt = _lib.Options()
+    opt.precision, opt.batch, opt.refit = _lib.RLF_MIXED, B, 1
+    lib.rlf_configure(C.byref(opt))
+    n_vis = obs.n_vis
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    d0, s0 = pin(data_h), pin(sky_h)
+    d, s = pin(data_h), pin(sky_h)
+    sigma2 = pin(np.full(n_vis, np.float32(obs.sigma2), np.float32))
+    flag = pin(np.zeros(n_vis, np.uint8))
+    uu, vv, ww = pin(obs.uu), pin(obs.vv), pin(obs.ww)
+    gal = np.zeros(1, np.complex128)
+    ro = np.array(K.ro_grid())
+    rprior = np.zeros(len(ro))
+    p = LikelihoodParams()
+    p.numr, p.ro, p.rprior, p.nchannels = len(ro), dptr(ro), dptr(rprior), obs.n_ch
+    p.spec, p.wavenumbers = dptr(obs.spec), dptr(obs.wavenumbers)
+    fmax = K.facet_size(K.RMAX, obs.len_lambda)
+    sumw = np.zeros(fmax * fmax)
+    snr = np.zeros(cat.n)
+    flux, scale, l, m, e1, e2 = (np.ascontiguousarray(x) for x in (cat.flux, cat.scale, cat.l, cat.m, cat.e1, cat.e2))
+    times = []
+    nbad_final = 0
+    for it in range(warmup + steps):
+        np.copyto(d, d0)
+        np.copyto(s, s0)
+        bad_list = np.zeros(cat.n, np.uint32)
+        bad = C.c_int(0)
+        ft = C.c_double(0)
+        args = [C.byref(p), dptr(l), dptr(m), dptr(flux), dptr(scale), dptr(e1), dptr(e2), dptr(snr), dptr(sumw),
+                cptr(gal), cptr(s), cptr(d), fptr(sigma2), bptr(flag), dptr(uu), dptr(vv), dptr(ww), C.byref(ft),
+                C.byref(bad)]
+        t0 = time.perf_counter()
+        lib.data_processing(False, bad_list.ctypes.data_as(_lib.PU), cat.n, obs.len_lambda, obs.n_rows, None, *args)
+        nb = bad.value
+        lib.data_processing(True, bad_list.ctypes.data_as(_lib.PU), nb, obs.len_lambda, obs.n_rows, None, *args)
+        dt = time.perf_counter() - t0
+        nbad_final = bad.value
+        if it >= warmup:
+            times.append(dt)
+    per_call_in = 2 * 16 * n_vis + 4 * n_vis + n_vis + 24 * obs.n_rows
+    per_call_out = 2 * 16 * n_vis
+    t = float(np.mean(times))
+    return {"value": cat.n / t, "unit": "galaxies/s", "h2d_bytes_per_step": 2 * per_call_in,
+            "d2h_bytes_per_step": 2 * per_call_out, "ms_per_step": t * 1e3,
+            "path": "data_processing() x2 (catalogue + re-fit pass), host complex128 buffers, mixed, batch %d" % B,
+            "bad_after_refit": nbad_final}
+
+
+def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
+    """The oracle (reference arithmetic, OpenMP over all host cores as the reference) on the
+    first n_sample galaxies of the workload: extraction + fit + removal, first pass."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+    orc = O.load_oracle()
+    sub = cat.subset(range(n_sample))
+    d, s = data_h.copy(), sky_h.copy()
+    gal = np.zeros(obs.n_vis, np.complex128)
+    sigma2 = np.full(obs.n_vis, np.float32(obs.sigma2), np.float32)
+    flag = np.zeros(obs.n_vis, np.uint8)
+    ro = np.array(K.ro_grid())
+    fmax = K.facet_size(K.RMAX, obs.len_lambda)
+    out = (O.OrcFitResult * sub.n)()
+    bl = np.zeros(sub.n, np.uint32)
+    bad = C.c_int(0)
+    t0 = time.perf_counter()
+    orc.orc_data_processing(0, bl.ctypes.data_as(O.PU), sub.n, obs.len_lambda, obs.n_rows, obs.n_ch, O.dp(obs.spec),
+                            O.dp(obs.wavenumbers), len(ro), O.dp(ro), O.dp(sub.l), O.dp(sub.m), O.dp(sub.flux),
+                            O.dp(sub.scale), O.dp(np.zeros(fmax * fmax)), O.cp(gal), O.cp(s), O.cp(d), O.fp(sigma2),
+                            O.bp(flag), O.dp(obs.uu), O.dp(obs.vv), O.dp(obs.ww), 0, out, C.byref(bad))
+    dt = time.perf_counter() - t0
+    res = np.array([(r.e1, r.e2, r.error) for r in out])
+    return sub.n / dt, dt, res
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -180,8 +260,7 @@ def main():
         return
     import torch
     from radiolensfit2_gb300 import _lib
-    from radiolensfit2_gb300.pipeline import DeviceObservation, RESULT_DTYPE
-    from radiolensfit2_gb300.abi import LikelihoodParams, dptr, fptr, cptr, bptr
+    from radiolensfit2_gb300.pipeline import DeviceObservation
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -208,6 +287,7 @@ def main():
         torch.distributed.barrier()
     clocks = ClockSampler()
     clocks.start()
+    l0 = lib.rlf_launch_count()
     t0 = time.perf_counter()
     stage = np.zeros(4)
     res = None
@@ -218,23 +298,74 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     elapsed = time.perf_counter() - t0
+    launches = int(lib.rlf_launch_count() - l0)
     ck = clocks.stop()
     if world > 1:
         t = torch.tensor([elapsed], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed = float(t.item())
     value = cat.n * args.steps * world / elapsed
+    batched = res.results
+    stage_ms = {"extract": stage[1] / args.steps, "fit": stage[2] / args.steps, "remove": stage[3] / args.steps}
+    peaks, peak_kind = measured_peaks()
+    fp32_peak = float(lib.rlf_fp32_peak_gflops())  # measured here, GFLOP/s
+    # algorithmic work of the batched visibility passes (per galaxy-visibility pair, FP32 FLOPs,
+    # FMA = 2): extraction 24 (Horner 8, round profile 8, segment/anchor share 8),
+    # removal 40 (recurrence 8, two profiles 16, four FMAs 8, anchor share 8); see the design doc
+    pairs = float(obs.n_vis) * cat.n
+    n_good = int(np.sum(batched["error"] == 0))
+    pairs_remove = float(obs.n_vis) * n_good
+    dominant = max(stage_ms, key=stage_ms.get)
+    if dominant == "remove":
+        flops, t_ms = 40.0 * pairs_remove, stage_ms["remove"]
+    elif dominant == "extract":
+        flops, t_ms = 24.0 * pairs, stage_ms["extract"]
+    else:
+        flops, t_ms = None, stage_ms["fit"]
+    roofline = {"kernel": {"remove": "k_remove_batch", "extract": "k_extract_batch", "fit": "k_fit"}[dominant],
+                "bound": "fp32", "unit": "TFLOP/s",
+                "achieved": (flops / (t_ms * 1e-3) / 1e12) if flops else None,
+                "peak": fp32_peak / 1e3, "peak_kind": "measured FP32 FMA probe (rlf_fp32_peak_gflops)",
+                "traffic": None}
+    if roofline["achieved"]:
+        roofline["frac"] = roofline["achieved"] / roofline["peak"]
     out = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (FP64 phase argument)",
            "data": "synthetic (seeded array, catalogue and noise)",
            "config": {"workload": args.workload, "antennas": w["n_ant"], "rows": obs.n_rows, "channels": obs.n_ch,
                       "n_vis": obs.n_vis, "galaxies": cat.n, "batch": B, "precision": "mixed",
-                      "l2_policy": "inputs larger than L2 (data + sky model 2.4 GB)"},
-           "stage_ms_per_step": {"extract": stage[1] / args.steps, "fit": stage[2] / args.steps,
-                                 "remove": stage[3] / args.steps},
-           "bad_galaxies": int(res.n_bad), "clocks": ck}
-    batched = res.results
+                      "l2_policy": "inputs larger than L2 (data + sky model %.1f GB)" % (16 * obs.n_vis / 1e9)},
+           "stage_ms_per_step": stage_ms, "bad_galaxies": int(res.n_bad), "gpu_launches": launches,
+           "roofline": roofline, "clocks": ck,
+           "hbm_peak_gbs": peaks.get("hbm_gbs"), "peaks": peak_kind}
+    if rank == 0 and not args.no_plain:
+        dev.restore()
+        t1 = time.perf_counter()
+        pr = dev.process(cat, batch=1, refit=True)
+        tp = time.perf_counter() - t1
+        pl = pr.results
+        ok = (pl["error"] == 0) & (batched["error"] == 0)
+        de = np.maximum(np.abs(pl["e1"][ok] - batched["e1"][ok]), np.abs(pl["e2"][ok] - batched["e2"][ok]))
+        out["plain_gpu"] = {"value": cat.n / tp, "unit": "galaxies/s", "ms": tp * 1e3,
+                            "stage_ms": dict(zip(("extract", "fit", "remove"), pr.ms[1:])),
+                            "speedup_batched_vs_plain": value / (cat.n / tp),
+                            "abs_de_vs_batched": {"max": float(de.max()) if de.size else None,
+                                                  "median": float(np.median(de)) if de.size else None,
+                                                  "frac_le_1e-3": float(np.mean(de <= 1e-3)) if de.size else None,
+                                                  "n": int(de.size)}}
+    data_h = sky_h = None
+    if rank == 0 and (not args.no_e2e or args.cpu_sample_galaxies > 0):
+        dev.restore()
+        data_h, sky_h = dev.get_vis()
+    if rank == 0 and not args.no_e2e:
+        out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps=1, warmup=1)
+    if rank == 0 and args.cpu_sample_galaxies > 0:
+        v, dt, _ = cpu_baseline(obs, cat, data_h, sky_h, args.cpu_sample_galaxies)
+        out["cpu_baseline"] = {"value": v, "unit": "galaxies/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"first {args.cpu_sample_galaxies} galaxies of {cat.n}, full "
+                                         f"{obs.n_vis}-visibility arrays, extraction+fit+removal, first pass "
+                                         f"({dt:.1f} s)"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     dev.close()

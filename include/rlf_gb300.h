@@ -42,6 +42,10 @@ typedef struct {
 int rlf_configure(const rlf_options *opt);
 const char *rlf_version(void);
 int rlf_device_count(void);
+/* number of CUDA kernels this library has launched since it was loaded */
+long long rlf_launch_count(void);
+/* measured FP32 FMA throughput of the current GPU, GFLOP/s (an FMA counts 2), for rooflines */
+double rlf_fp32_peak_gflops(void);
 
 /* -------- device-resident observation -------- */
 typedef struct rlf_observation rlf_observation;
@@ -81,6 +85,11 @@ int rlf_obs_process(rlf_observation *obs, int n_gal, const double *flux, const d
 int rlf_obs_extract(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
                     const double *l, const double *m, int batch, double *facets, int stride,
                     int *ncoords);
+/* Debugging aid: source_fitting of one facet given as likelihood_params (datatype.h:49-74) in
+ * the given precision, recording (e1, e2, L, error) of every likelihood evaluation into
+ * trace[cap][4]; out6 = (e1, e2, simplex max e1, max e2, maxL, evaluations). */
+int rlf_debug_fit_trace(void *likelihood_params_facet, double *trace, int cap, double *out6,
+                        int precision);
 /* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
  * [total, extract, fit, remove] */
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);

@@ -421,6 +421,10 @@ static double loglikelihood_impl(orc_params *par, double e1, double e2, int *err
   if (numvals > 4) L_e = orc_marginalise_posterior_r(numvals, xm, ym);
   else { *error = 1; L_e = -1.e+10; }
   if (L_e == -1.e+10) *error = 1;
+  if (par->trace && par->nevals <= par->trace_cap) {
+    double *t = par->trace + 4 * (par->nevals - 1);
+    t[0] = e1; t[1] = e2; t[2] = L_e; t[3] = *error;
+  }
   return L_e;
 }
 

@@ -31,6 +31,8 @@ typedef struct {
   int gaussian;             /* 0: exponential (Sersic n=1) profile, 1: Gaussian */
   long nevals;              /* loglikelihood() calls */
   long newton_iters;        /* Newton iterations summed over all cross-correlations */
+  double *trace;            /* optional [trace_cap][4]: (e1, e2, L, error) per evaluation */
+  long trace_cap;
 } orc_params;
 
 typedef struct {

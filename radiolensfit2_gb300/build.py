@@ -65,7 +65,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
-        run([cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        # static CUDA runtime: the library keeps its own runtime even when the host process has
+        # loaded another libcudart (e.g. the one bundled with torch)
+        run([cc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs])
     return LIB
 
 

@@ -32,6 +32,7 @@ __constant__ float c_il0_hi, c_il0_lo, c_dil_hi, c_dil_lo;  // inv_lambda(0) and
 __constant__ int c_bnch;
 
 static int check(const char* what) {
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     fprintf(stderr, "rlf: %s: %s\n", what, cudaGetErrorString(e));
@@ -282,8 +283,8 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
     if (flagc) {
       const int pos = off + before + inwarp;
       const int i = c % F, j = c / F;
-      ((float*)out.gu)[pos] = (float)((i + 0.5) * inc - len);
-      ((float*)out.gv)[pos] = (float)((j + 0.5) * inc - len);
+      ((float*)out.gu)[pos] = (float)__dsub_rn(__dmul_rn(i + 0.5, inc), len);
+      ((float*)out.gv)[pos] = (float)__dsub_rn(__dmul_rn(j + 0.5, inc), len);
       ((float*)out.dre)[pos] = (float)vre;
       ((float*)out.dim)[pos] = (float)vim;
       ((float*)out.sig2)[pos] = (float)sg;

@@ -7,6 +7,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <execinfo.h>
+#include <signal.h>
+#include <unistd.h>
+
 #include <map>
 #include <vector>
 
@@ -436,6 +440,8 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fb.active = nullptr;
     fb.out = dout.p + b0;
     fb.queue = dqueue.p + bi;
+    fb.trace = nullptr;
+    fb.trace_cap = 0;
     RLF_OK(fit_launch(fb, prec, std::min(grid_fit, bn), st));
     RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
     if (batched) {
@@ -633,12 +639,31 @@ struct OneFacet {
     fb.active = nullptr;
     fb.out = nullptr;
     fb.queue = nullptr;
+    fb.trace = nullptr;
+    fb.trace_cap = 0;
     return 0;
   }
 };
 
 // last spline built by marginalise_posterior_r, for marf (marginalise_r.c:231-238)
 static std::vector<double> g_marf_x, g_marf_y;
+
+// Opt-in native backtrace on a fatal signal (RLF_DEBUG_SEGV=1), for diagnosing host crashes.
+static void segv_trace(int sig) {
+  void* buf[64];
+  const int n = backtrace(buf, 64);
+  static const char msg[] = "rlf: fatal signal, native backtrace:\n";
+  if (write(2, msg, sizeof(msg) - 1) < 0) {}
+  backtrace_symbols_fd(buf, n, 2);
+  signal(sig, SIG_DFL);
+  raise(sig);
+}
+__attribute__((constructor)) static void install_segv_trace() {
+  if (getenv("RLF_DEBUG_SEGV")) {
+    signal(SIGSEGV, segv_trace);
+    signal(SIGBUS, segv_trace);
+  }
+}
 
 }  // namespace rlf
 
@@ -648,6 +673,17 @@ using namespace rlf;
 extern "C" {
 
 const char* rlf_version(void) { return "rlf-gb300 0.1 (sm_103a)"; }
+
+long long rlf_launch_count(void) { return rlf::launch_count(); }
+
+double rlf_fp32_peak_gflops(void) {
+  cudaStream_t st;
+  if (lib_stream(&st)) return 0.0;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return rlf::fp32_probe_gflops(sms * 8, 20000, st);
+}
 
 int rlf_device_count(void) {
   int n = 0;
@@ -1141,6 +1177,47 @@ int source_fitting(int rank, likelihood_params* par, double* mes_e1, double* mes
     else printf("rank %d: BAD - NO likelihood sampling!\n", rank);
   }
   return o.error;
+}
+
+// source_fitting with a record of every likelihood evaluation (e1, e2, L, error) for debugging
+int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int precision) {
+  likelihood_params* par = (likelihood_params*)pv;
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  OneFacet f;
+  DevBuf<double> dt;
+  RLF_OK(f.load(par, st));
+  DevBuf<float> fcells;
+  if (precision == RLF_MIXED) {  // the same facet as FP32 cells for the mixed fit
+    const int n = (int)par->ncoords;
+    std::vector<float> h((size_t)5 * n);
+    for (int i = 0; i < n; ++i) {
+      h[i] = (float)par->uu[i];
+      h[n + i] = (float)par->vv[i];
+      h[2 * n + i] = (float)par->data[i].real;
+      h[3 * n + i] = (float)par->data[i].imag;
+      h[4 * n + i] = (float)par->sigma2[i];
+    }
+    RLF_OK(fcells.upload(h.data(), h.size(), st));
+    f.fb.gu = fcells.p; f.fb.gv = fcells.p + n; f.fb.dre = fcells.p + 2 * n; f.fb.dim = fcells.p + 3 * n;
+    f.fb.sig2 = fcells.p + 4 * n;
+  }
+  RLF_OK(g_lib.fo.ensure(1));
+  RLF_OK(g_lib.i0.ensure(1));
+  RLF_OK(dt.ensure((size_t)cap * 4));
+  RLF_CUDA(cudaMemsetAsync(dt.p, 0, (size_t)cap * 4 * sizeof(double), st));
+  RLF_CUDA(cudaMemsetAsync(g_lib.i0.p, 0, sizeof(int), st));
+  f.fb.out = g_lib.fo.p;
+  f.fb.queue = g_lib.i0.p;
+  f.fb.trace = dt.p;
+  f.fb.trace_cap = cap;
+  RLF_OK(fit_launch(f.fb, precision == RLF_MIXED ? kMixed : kF64, 1, st));
+  FitOut o;
+  RLF_CUDA(cudaMemcpyAsync(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(cudaMemcpyAsync(trace, dt.p, (size_t)cap * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  out6[0] = o.e1; out6[1] = o.e2; out6[2] = o.max_e1; out6[3] = o.max_e2; out6[4] = o.maxL; out6[5] = o.nevals;
+  return 0;
 }
 
 // source_extraction.c:36-68 (FACET): visGal is used as scratch only

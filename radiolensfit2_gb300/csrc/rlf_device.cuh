@@ -12,6 +12,10 @@
 
 namespace rlf {
 
+// kernels launched by this library since load (incremented by every launch-site check)
+void count_launch();
+long long launch_count();
+
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kC0 = 299792458.0;
 constexpr int kPsfNat = 38;

@@ -653,13 +653,20 @@ struct FitCtx {
   const typename P::Cell *gu, *gv, *dre, *dim, *sig2;
   int n;
   int nevals;
+  double* trace;   // optional evaluation record (thread 0 writes)
+  int trace_cap;
 };
 
 template <class P>
 __device__ __noinline__ typename P::S loglike(FitCtx<P>& c, typename P::S e1, typename P::S e2,
                                               int* error) {
   c.nevals++;
-  return eval_loglike<P>(*c.sh, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, e1, e2, error);
+  const typename P::S L = eval_loglike<P>(*c.sh, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, e1, e2, error);
+  if (c.trace && threadIdx.x == 0 && c.nevals <= c.trace_cap) {
+    double* t = c.trace + 4 * (size_t)(c.nevals - 1);
+    t[0] = (double)e1; t[1] = (double)e2; t[2] = (double)L; t[3] = (double)*error;
+  }
+  return L;
 }
 
 // likelihood.c:87-100
@@ -791,7 +798,7 @@ __device__ __forceinline__ int nm_lowest(const Simplex<S>& s) {
 // likelihood.c:428-554; sampling/edim/start are float as in the reference, the other reals are S
 // (double for F64, float for the mixed policy).
 template <class P>
-__device__ void likelihood_sampling(FitCtx<P>& c, typename P::S* mes_e1, typename P::S* mes_e2,
+__device__ __noinline__ void likelihood_sampling(FitCtx<P>& c, typename P::S* mes_e1, typename P::S* mes_e2,
                                     typename P::S maxL, int np_max, typename P::S* var_e1,
                                     typename P::S* var_e2, typename P::S* oneDimvar) {
   using S = typename P::S;
@@ -836,14 +843,22 @@ __device__ void likelihood_sampling(FitCtx<P>& c, typename P::S* mes_e1, typenam
     }
   }
   if (L < threshold && k2 > 1) k2--;
+  if (c.trace && threadIdx.x == 0 && c.trace_cap > 0) {  // debugging record: line-search extents
+    double* t = c.trace + 4 * (size_t)(c.trace_cap - 1);
+    t[0] = k1; t[1] = k2; t[2] = (double)L; t[3] = (double)np_max;
+  }
   sampling = 0.05;
   float edim1 = k1 * sampling;
   float edim2 = k2 * sampling;
   float start1 = edim1;
   float start2 = edim2;
   while (np < np_max && sampling > kERes) {
-    for (ie1 = -start1 / sampling; ie1 <= start1 / sampling; ie1 += 2) {
-      for (ie2 = -start2 / sampling; ie2 <= start2 / sampling; ie2 += 2) {
+    // loop bounds of likelihood.c:504-506, in float as there: first index -start/sampling
+    // converted to int, last index while (float)ie <= start/sampling
+    const float q1 = start1 / sampling, q2 = start2 / sampling;
+    const int lo1 = (int)(-start1 / sampling), lo2 = (int)(-start2 / sampling);
+    for (ie1 = lo1; (float)ie1 <= q1; ie1 += 2) {
+      for (ie2 = lo2; (float)ie2 <= q2; ie2 += 2) {
         if (ie1 != 0 || ie2 != 0) {
           x_e1 = max_e1 + ie1 * sampling;
           x_e2 = max_e2 + ie2 * sampling;
@@ -886,7 +901,7 @@ __device__ void likelihood_sampling(FitCtx<P>& c, typename P::S* mes_e1, typenam
 
 // galaxy_fitting.c:41-117 with a configurable start point and step (reference: (0,0), 0.1)
 template <class P>
-__device__ FitOut fit_galaxy(FitCtx<P>& c, double start_e1, double start_e2, double step, int np_max) {
+__device__ __noinline__ FitOut fit_galaxy(FitCtx<P>& c, double start_e1, double start_e2, double step, int np_max) {
   using S = typename P::S;
   FitOut o;
   Simplex<S> s;
@@ -977,7 +992,8 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_fit(FacetBatch b) {
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
-    FitCtx<P> c{&sh, gu, gv, dre, dim, sig2, n, 0};
+    FitCtx<P> c{&sh, gu, gv, dre, dim, sig2, n, 0,
+                b.trace ? b.trace + (size_t)g * b.trace_cap * 4 : nullptr, b.trace_cap};
     FitOut o = fit_galaxy<P>(c, se1, se2, step, c_fit.np_max);
     __syncthreads();
     if (tid == 0) {
@@ -1023,7 +1039,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, 
   __syncthreads();
   FitCtx<P> c{&sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
               reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
-              reinterpret_cast<const Cell*>(b.sig2), n, 0};
+              reinterpret_cast<const Cell*>(b.sig2), n, 0, b.trace, b.trace_cap};
   S m1 = S(e1), m2 = S(e2), v1, v2, od;
   likelihood_sampling<P>(c, &m1, &m2, S(maxL), np_max, &v1, &v2, &od);
   if (tid == 0) { out5[0] = m1; out5[1] = m2; out5[2] = v1; out5[3] = v2; out5[4] = od; }
@@ -1079,6 +1095,7 @@ __global__ void k_position_marginal(int n, const double* x, double* y) {
 
 // ----------------------------------------------------------------- launchers
 static int check(const char* what) {
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     fprintf(stderr, "rlf: %s: %s\n", what, cudaGetErrorString(e));

@@ -36,6 +36,8 @@ struct FacetBatch {
   const int* active;       // [n_gal] nonzero = fit this galaxy, or nullptr for all
   FitOut* out;             // [n_gal]
   int* queue;              // work counter, zeroed before launch
+  double* trace;           // optional [n_gal][trace_cap][4]: (e1, e2, L, error) per evaluation
+  int trace_cap;
 };
 
 struct FitConfigHost {

@@ -14,6 +14,47 @@
 
 namespace rlf {
 
+static long long g_launches = 0;
+void count_launch() { __atomic_add_fetch(&g_launches, 1, __ATOMIC_RELAXED); }
+long long launch_count() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread, no memory traffic in the loop
+__global__ void k_fp32_probe(int iters, float* out) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+  float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+  const float b = 0.999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+      a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+    }
+  }
+  const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678f) out[0] = s;  // keeps the chains live
+}
+
+// FP32 FLOP/s (an FMA counts 2) measured with CUDA events on `blocks` x 256 threads
+double fp32_probe_gflops(int blocks, int iters, cudaStream_t st) {
+  float* d = nullptr;
+  cudaMalloc(&d, sizeof(float));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_fp32_probe<<<blocks, 256, 0, st>>>(iters / 4, d);  // warm-up
+  cudaEventRecord(a, st);
+  k_fp32_probe<<<blocks, 256, 0, st>>>(iters, d);
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(d);
+  const double flops = 2.0 * 8 * 16 * (double)iters * blocks * 256;
+  return flops / (ms * 1e-3) / 1e9;
+}
+
 struct ChanConst {
   double wn;          // wavenumber 2 pi nu / c
   double spec;        // (nu / 1.4 GHz)^-0.7
@@ -28,6 +69,7 @@ __constant__ int c_nch;
 int launch_reduce_partials(const double* partial, int n_part, int len, double* sums, cudaStream_t st);
 
 static int check(const char* what) {
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     fprintf(stderr, "rlf: %s: %s\n", what, cudaGetErrorString(e));
@@ -400,7 +442,8 @@ __global__ void k_facet_finalize(const int* facets, const double* partial, int n
     if (flagc) {
       const int pos = off + before + inwarp;
       const int i = c % F, j = c / F;
-      const double gu = (i + 0.5) * inc - len, gv = (j + 0.5) * inc - len;
+      // evaluate_uv_grid.c:125-126 without a fused multiply-add
+      const double gu = __dsub_rn(__dmul_rn(i + 0.5, inc), len), gv = __dsub_rn(__dmul_rn(j + 0.5, inc), len);
       if (out.as_float) {
         ((float*)out.gu)[pos] = (float)gu; ((float*)out.gv)[pos] = (float)gv;
         ((float*)out.dre)[pos] = (float)vre; ((float*)out.dim)[pos] = (float)vim;
@@ -727,8 +770,8 @@ __global__ void k_facet_coords(double* gu, double* gv, double len, unsigned F, c
   for (unsigned p = 0; p < F * F; ++p) {
     if (count_w[p]) {
       unsigned j = p / F, i = p % F;
-      gu[n] = (i + 0.5) * inc - len;
-      gv[n] = (j + 0.5) * inc - len;
+      gu[n] = __dsub_rn(__dmul_rn(i + 0.5, inc), len);
+      gv[n] = __dsub_rn(__dmul_rn(j + 0.5, inc), len);
       n++;
     }
   }

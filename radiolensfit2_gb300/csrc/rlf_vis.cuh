@@ -36,6 +36,8 @@ struct GalaxyParams {
   int pad;
 };
 
+double fp32_probe_gflops(int blocks, int iters, cudaStream_t st);
+
 int set_channels(int n_ch, const double* wavenumbers, const double* spec, cudaStream_t st);
 
 // cell index of every visibility for facet size F (0xFFFF = flagged or outside the grid),

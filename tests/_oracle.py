@@ -36,7 +36,8 @@ PC = C.POINTER(OrcComplex)
 class OrcParams(C.Structure):
     _fields_ = [("numr", C.c_int), ("ro", PD), ("rprior", PD), ("ncoords", C.c_uint),
                 ("uu", PD), ("vv", PD), ("data", PC), ("sigma2", PD), ("mod", PD),
-                ("gaussian", C.c_int), ("nevals", C.c_long), ("newton_iters", C.c_long)]
+                ("gaussian", C.c_int), ("nevals", C.c_long), ("newton_iters", C.c_long),
+                ("trace", PD), ("trace_cap", C.c_long)]
 
 
 class OrcFitResult(C.Structure):

@@ -15,11 +15,16 @@ def pytest_configure(config):
 
 
 def _has_gpu():
+    """GPU present (nvidia-smi lists one); torch is not imported into the test process."""
+    import shutil
+    import subprocess
+    if not shutil.which("nvidia-smi"):
+        return False
     try:
-        import torch
-        return torch.cuda.is_available()
+        out = subprocess.run(["nvidia-smi", "-L"], capture_output=True, text=True, timeout=30).stdout
     except Exception:
         return False
+    return "GPU" in out
 
 
 def pytest_collection_modifyitems(config, items):

@@ -6,7 +6,6 @@ import socket
 
 import numpy as np
 import pytest
-import torch.multiprocessing as mp
 
 from radiolensfit2_gb300 import shard, constants as K
 
@@ -59,6 +58,7 @@ def test_channel_shards_partition():
 
 
 def test_two_rank_facet_reduction_matches_unsharded():
+    import torch.multiprocessing as mp
     import _oracle as O
     from _cases import Case
     ctx = mp.get_context("spawn")
