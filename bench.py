@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--workload", default="c1_ska_mid_16ch")
     ap.add_argument("--galaxies", type=int, default=0)
     ap.add_argument("--batch", type=int, default=1000)
+    ap.add_argument("--fit-precision", default="f64", choices=["f64", "mixed"],
+                    help="arithmetic of the fit (visibility passes are always mixed)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample-galaxies", type=int, default=2)
@@ -171,14 +173,14 @@ def cpu_baseline_sample(obs, cat, galaxies=1):
     return ns
 
 
-def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup):
+def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec):
     """Galaxies/s through the reference-facing entry point data_processing() with pinned host
     buffers: catalogue pass + re-fit pass (RadioLensfit2.cpp:597-606), copies inside the timing."""
     import torch
     from radiolensfit2_gb300 import _lib
     from radiolensfit2_gb300.abi import LikelihoodParams, dptr, fptr, cptr, bptr
     opt = _lib.Options()
-    opt.precision, opt.batch, opt.refit = _lib.RLF_MIXED, B, 1
+    opt.precision, opt.batch, opt.refit, opt.fit_precision = _lib.RLF_MIXED, B, 1, fit_prec
     lib.rlf_configure(C.byref(opt))
     n_vis = obs.n_vis
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -251,6 +253,42 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
     return sub.n / dt, dt, res
 
 
+def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak):
+    """Roofline of the dominant stage of a step.
+
+    Algorithmic bytes (streaming passes of the batched path): extraction reads data and sky model
+    (2 x 8 B FP32 complex) per visibility and 24 B of uvw per row once per group of up to 32
+    galaxies of one facet size; removal reads and writes data and sky model (32 B) per visibility
+    and the uvw row once per batch.  Algorithmic FP32 work per galaxy-visibility pair: extraction
+    24 FLOP, removal 40 FLOP (FMA = 2).  The fit stage reads only facets (kilobytes) and is
+    reported by FLOP-free time only."""
+    n_vis, n_rows = float(obs.n_vis), float(obs.n_rows)
+    good = int(np.sum(batched["error"] == 0))
+    st = res.stats  # passes of the last step (both passes), counted by the library
+    dominant = max(stage_ms, key=stage_ms.get)
+    t = stage_ms[dominant] * 1e-3
+    if dominant == "extract":
+        nbytes = (st["extract_groups"] + st["extract_single"]) * (16.0 * n_vis + 24.0 * n_rows)
+        flops = 24.0 * n_vis * st["fitted"]
+    elif dominant == "remove":
+        nbytes = (st["remove_batches"] + st["remove_single"]) * (32.0 * n_vis + 24.0 * n_rows)
+        flops = 40.0 * n_vis * good
+    else:
+        nbytes, flops = None, None
+    kernel = {"remove": "k_remove_batch", "extract": "k_extract_batch", "fit": "k_fit"}[dominant]
+    r = {"kernel": kernel, "bound": "hbm", "unit": "GB/s",
+         "achieved": nbytes / t / 1e9 if nbytes else None, "peak": hbm_peak,
+         "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+         "traffic": None, "time_ms_per_step": stage_ms[dominant], "passes": st}
+    r["frac"] = r["achieved"] / hbm_peak if r["achieved"] else None
+    if flops:
+        # the batched passes are FP32-pipe bound (sincos + FMAs), not HBM bound
+        r["compute"] = {"bound": "fp32", "unit": "TFLOP/s", "achieved": flops / t / 1e12,
+                        "peak": fp32_peak / 1e3, "peak_kind": "measured FP32 FMA probe kernel",
+                        "frac": flops / t / 1e12 / (fp32_peak / 1e3)}
+    return r
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -275,10 +313,11 @@ def main():
     dev.sky_model(cat)
     dev.snapshot()
     B = max(1, args.batch)
+    fit_prec = _lib.RLF_F64 if args.fit_precision == "f64" else _lib.RLF_MIXED
 
     def step():
         dev.restore()
-        return dev.process(cat, batch=B, refit=True)
+        return dev.process(cat, batch=B, refit=True, fit_precision=fit_prec)
 
     for _ in range(args.warmup):
         step()
@@ -289,7 +328,7 @@ def main():
     clocks.start()
     l0 = lib.rlf_launch_count()
     t0 = time.perf_counter()
-    stage = np.zeros(4)
+    stage = np.zeros(4)  # device time from CUDA events on the library's stream: total, extract, fit, remove
     res = None
     for _ in range(args.steps):
         res = step()
@@ -297,9 +336,10 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    elapsed = time.perf_counter() - t0
+    wall = time.perf_counter() - t0
     launches = int(lib.rlf_launch_count() - l0)
     ck = clocks.stop()
+    elapsed = stage[0] * 1e-3  # seconds of device time over the K timed steps
     if world > 1:
         t = torch.tensor([elapsed], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -308,41 +348,25 @@ def main():
     batched = res.results
     stage_ms = {"extract": stage[1] / args.steps, "fit": stage[2] / args.steps, "remove": stage[3] / args.steps}
     peaks, peak_kind = measured_peaks()
-    fp32_peak = float(lib.rlf_fp32_peak_gflops())  # measured here, GFLOP/s
-    # algorithmic work of the batched visibility passes (per galaxy-visibility pair, FP32 FLOPs,
-    # FMA = 2): extraction 24 (Horner 8, round profile 8, segment/anchor share 8),
-    # removal 40 (recurrence 8, two profiles 16, four FMAs 8, anchor share 8); see the design doc
-    pairs = float(obs.n_vis) * cat.n
-    n_good = int(np.sum(batched["error"] == 0))
-    pairs_remove = float(obs.n_vis) * n_good
-    dominant = max(stage_ms, key=stage_ms.get)
-    if dominant == "remove":
-        flops, t_ms = 40.0 * pairs_remove, stage_ms["remove"]
-    elif dominant == "extract":
-        flops, t_ms = 24.0 * pairs, stage_ms["extract"]
-    else:
-        flops, t_ms = None, stage_ms["fit"]
-    roofline = {"kernel": {"remove": "k_remove_batch", "extract": "k_extract_batch", "fit": "k_fit"}[dominant],
-                "bound": "fp32", "unit": "TFLOP/s",
-                "achieved": (flops / (t_ms * 1e-3) / 1e12) if flops else None,
-                "peak": fp32_peak / 1e3, "peak_kind": "measured FP32 FMA probe (rlf_fp32_peak_gflops)",
-                "traffic": None}
-    if roofline["achieved"]:
-        roofline["frac"] = roofline["achieved"] / roofline["peak"]
+    hbm_peak = float(peaks.get("hbm_gbs") or 6800.0)
+    fp32_peak = float(lib.rlf_fp32_peak_gflops())  # measured here by an FMA probe kernel, GFLOP/s
+    roofline = roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak)
     out = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (FP64 phase argument)",
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp32 visibilities (FP64 phase argument), %s fit" % args.fit_precision,
            "data": "synthetic (seeded array, catalogue and noise)",
            "config": {"workload": args.workload, "antennas": w["n_ant"], "rows": obs.n_rows, "channels": obs.n_ch,
                       "n_vis": obs.n_vis, "galaxies": cat.n, "batch": B, "precision": "mixed",
-                      "l2_policy": "inputs larger than L2 (data + sky model %.1f GB)" % (16 * obs.n_vis / 1e9)},
+                      "fit_precision": args.fit_precision,
+                      "l2_policy": "inputs larger than L2 (data + sky model %.1f GB)" % (16 * obs.n_vis / 1e9),
+                      "timing": "CUDA events on the library stream around both passes of each step"},
+           "wall_ms_per_step": wall / args.steps * 1e3,
            "stage_ms_per_step": stage_ms, "bad_galaxies": int(res.n_bad), "gpu_launches": launches,
-           "roofline": roofline, "clocks": ck,
-           "hbm_peak_gbs": peaks.get("hbm_gbs"), "peaks": peak_kind}
+           "roofline": roofline, "clocks": ck, "peaks": peak_kind}
     if rank == 0 and not args.no_plain:
         dev.restore()
         t1 = time.perf_counter()
-        pr = dev.process(cat, batch=1, refit=True)
+        pr = dev.process(cat, batch=1, refit=True, fit_precision=fit_prec)
         tp = time.perf_counter() - t1
         pl = pr.results
         ok = (pl["error"] == 0) & (batched["error"] == 0)
@@ -359,7 +383,7 @@ def main():
         dev.restore()
         data_h, sky_h = dev.get_vis()
     if rank == 0 and not args.no_e2e:
-        out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps=1, warmup=1)
+        out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps=1, warmup=1, fit_prec=fit_prec)
     if rank == 0 and args.cpu_sample_galaxies > 0:
         v, dt, _ = cpu_baseline(obs, cat, data_h, sky_h, args.cpu_sample_galaxies)
         out["cpu_baseline"] = {"value": v, "unit": "galaxies/s", "cores": os.cpu_count(), "kind": "port",

@@ -29,12 +29,17 @@ typedef struct {
 } rlf_fit_result;
 
 typedef struct {
-  int precision;     /* RLF_F64 (reference arithmetic) or RLF_MIXED */
+  int precision;     /* visibility passes (extraction, removal): RLF_F64 (reference arithmetic) or
+                        RLF_MIXED (FP32 visibilities, FP64 phase argument) */
   int batch;         /* galaxies extracted/fitted/removed together; 1 = the reference's order */
   int gaussian;      /* 0 exponential profile (default), 1 Gaussian (the -DGAUSSIAN build) */
   int refit;         /* rlf_obs_process: 1 = run the re-fit pass over bad galaxies */
   int verbose;
   const double *start;  /* optional [n_gal*3] simplex start (e1, e2, step); NULL = (0, 0, 0.1) */
+  int fit_precision; /* the fit: RLF_F64 (default; the reference's fit arithmetic, so the fitted
+                        ellipticities follow the reference's simplex path) or RLF_MIXED (FP32 cell
+                        arithmetic: faster, log-likelihood within ~2e-7 relative, but rounding
+                        noise can change simplex decisions, moving e by up to ~1e-3) */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -90,9 +95,30 @@ int rlf_obs_extract(rlf_observation *obs, int n_gal, const double *flux, const d
  * trace[cap][4]; out6 = (e1, e2, simplex max e1, max e2, maxL, evaluations). */
 int rlf_debug_fit_trace(void *likelihood_params_facet, double *trace, int cap, double *out6,
                         int precision);
+/* Debugging aid: one loglikelihood evaluation of a facet in the given precision; out2 = (L, error),
+ * node_L[1..numr-1] = the per-scalelength-node log-likelihoods before the marginalisation. */
+int rlf_debug_loglike_nodes(void *likelihood_params_facet, double e1, double e2, int precision,
+                            double *out2, double *node_L);
 /* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
  * [total, extract, fit, remove] */
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
+
+/* Work counters of the last rlf_obs_process (both passes), for throughput and roofline figures:
+ * stats[RLF_STAT_EXTRACT_GROUPS]  batched extraction passes over all visibilities (one per group
+ *                                 of up to 32 galaxies of one facet size),
+ * stats[RLF_STAT_EXTRACT_SINGLE]  one-galaxy extraction passes,
+ * stats[RLF_STAT_REMOVE_BATCHES]  batched removal passes (one per batch),
+ * stats[RLF_STAT_REMOVE_SINGLE]   one-galaxy removal passes,
+ * stats[RLF_STAT_FITTED]          galaxies fitted. */
+enum {
+  RLF_STAT_EXTRACT_GROUPS = 0,
+  RLF_STAT_EXTRACT_SINGLE = 1,
+  RLF_STAT_REMOVE_BATCHES = 2,
+  RLF_STAT_REMOVE_SINGLE = 3,
+  RLF_STAT_FITTED = 4,
+  RLF_NSTATS = 8
+};
+int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ class FitResult(C.Structure):
 class Options(C.Structure):
     """rlf_options (include/rlf_gb300.h)"""
     _fields_ = [("precision", C.c_int), ("batch", C.c_int), ("gaussian", C.c_int),
-                ("refit", C.c_int), ("verbose", C.c_int), ("start", PD)]
+                ("refit", C.c_int), ("verbose", C.c_int), ("start", PD), ("fit_precision", C.c_int)]
 
 
 _lib = None
@@ -66,8 +66,10 @@ def load():
         "rlf_obs_process": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.c_int, PD,
                                       C.POINTER(Options), C.POINTER(FitResult), PI]),
         "rlf_obs_last_timing": (C.c_int, [C.c_void_p, PD]),
+        "rlf_obs_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
         "rlf_obs_extract": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.c_int, PD, C.c_int, PI]),
         "rlf_debug_fit_trace": (C.c_int, [C.c_void_p, PD, C.c_int, PD, C.c_int]),
+        "rlf_debug_loglike_nodes": (C.c_int, [C.c_void_p, D, D, C.c_int, PD, PD]),
         # reference-named drop-in entry points
         "facet_size": (C.c_uint, [D, D]),
         "evaluate_uv_grid_size": (C.c_uint, [C.c_int, C.c_int, D, PD, C.c_uint, C.c_uint, PD, PD, C.c_uint, PU8]),
@@ -111,7 +113,7 @@ EXPORTED = [
     "rlf_version", "rlf_device_count", "rlf_launch_count", "rlf_fp32_peak_gflops", "rlf_configure", "rlf_obs_create", "rlf_obs_destroy",
     "rlf_obs_set_vis", "rlf_obs_set_data_c64", "rlf_obs_get_vis", "rlf_obs_simulate",
     "rlf_obs_sky_model", "rlf_obs_snapshot", "rlf_obs_restore", "rlf_obs_process",
-    "rlf_obs_last_timing", "rlf_obs_extract", "rlf_debug_fit_trace", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
+    "rlf_obs_last_timing", "rlf_obs_last_stats", "rlf_obs_extract", "rlf_debug_fit_trace", "rlf_debug_loglike_nodes", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
     "gridding_visibilities", "average_facets", "gaussian_shape", "sersic_shape",
     "model_galaxy_visibilities_at_zero", "data_galaxy_visibilities", "data_visibilities_phase_shift",
     "f_likelihood", "loglikelihood", "loglikelihood_r", "cross_correlation",

@@ -283,11 +283,17 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
     if (flagc) {
       const int pos = off + before + inwarp;
       const int i = c % F, j = c / F;
-      ((float*)out.gu)[pos] = (float)__dsub_rn(__dmul_rn(i + 0.5, inc), len);
-      ((float*)out.gv)[pos] = (float)__dsub_rn(__dmul_rn(j + 0.5, inc), len);
-      ((float*)out.dre)[pos] = (float)vre;
-      ((float*)out.dim)[pos] = (float)vim;
-      ((float*)out.sig2)[pos] = (float)sg;
+      // evaluate_uv_grid.c:125-126 without a fused multiply-add
+      const double gu = __dsub_rn(__dmul_rn(i + 0.5, inc), len), gv = __dsub_rn(__dmul_rn(j + 0.5, inc), len);
+      if (out.as_float) {
+        ((float*)out.gu)[pos] = (float)gu; ((float*)out.gv)[pos] = (float)gv;
+        ((float*)out.dre)[pos] = (float)vre; ((float*)out.dim)[pos] = (float)vim;
+        ((float*)out.sig2)[pos] = (float)sg;
+      } else {
+        ((double*)out.gu)[pos] = gu; ((double*)out.gv)[pos] = gv;
+        ((double*)out.dre)[pos] = vre; ((double*)out.dim)[pos] = vim;
+        ((double*)out.sig2)[pos] = sg;
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {

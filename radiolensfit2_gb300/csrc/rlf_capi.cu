@@ -107,7 +107,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -163,6 +163,8 @@ struct rlf_observation {
   double max_delay_m = 0;
   int n_part = 0;
   double ms[4] = {0, 0, 0, 0};
+  // streaming passes over the visibilities in the last process() call (RLF_STAT_*)
+  long long stats[RLF_NSTATS] = {};
   ~rlf_observation() {
     for (auto& kv : facets) delete kv.second;
   }
@@ -267,7 +269,8 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   out.assign(n, FitOut{});
   if (n == 0) return 0;
   if (numr < 2 || numr > kMaxNodes) { fprintf(stderr, "rlf: %d scalelength nodes unsupported\n", numr); return 1; }
-  const Precision prec = (ob->precision == RLF_F64) ? kF64 : kMixed;
+  const Precision prec = (ob->precision == RLF_F64) ? kF64 : kMixed;   // visibility passes
+  const Precision fprec = (opt.fit_precision == RLF_MIXED) ? kMixed : kF64;  // the fit
   const int B = opt.batch > 0 ? opt.batch : 1;
   const Observation o = ob->view();
   unsigned fmax = 0;
@@ -321,7 +324,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   RLF_OK(dnc.ensure(n));
   RLF_OK(dqueue.ensure(nbatches));
   RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, nbatches * sizeof(int), st));
-  const size_t esz = prec == kF64 ? sizeof(double) : sizeof(float);
+  const size_t esz = fprec == kF64 ? sizeof(double) : sizeof(float);
   DevBuf<unsigned char> cells;
   const size_t plane = (size_t)nb * max_cells * esz;
   RLF_OK(cells.ensure(5 * plane));
@@ -333,7 +336,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   RLF_OK(ob->partial.ensure((size_t)ob->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
   std::vector<cudaEvent_t> ev((size_t)nbatches * 3 + 1);
   for (auto& e : ev) RLF_CUDA(cudaEventCreate(&e));
-  const int grid_fit = fit_max_grid(prec);
+  const int grid_fit = fit_max_grid(fprec);
   // batched extraction/removal: mixed precision, batch > 1, evenly spaced channels
   bool batched = prec == kMixed && B > 1;
   if (batched) {
@@ -355,7 +358,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fo.offset = doff.p;
     fo.ncoords = dnc.p + b0;
     fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
-    fo.as_float = prec == kMixed;
+    fo.as_float = fprec == kMixed;
     std::vector<int> single;  // galaxies extracted one at a time
     if (batched) {
       // group the batch by facet size, 32 galaxies per warp-group
@@ -381,6 +384,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
           const int F = L.first, g0 = L.second.first, ng = L.second.second;
           FacetCache* fcF = nullptr;
           RLF_OK(obs_facet(ob, (unsigned)F, &fcF, st));
+          ob->stats[RLF_STAT_EXTRACT_GROUPS] += ng;
           RLF_OK(launch_extract_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, fcF->cell.p, dg.p + b0,
                                       dgidx.p + (size_t)g0 * 32, ng, F, ctas_per_group, opt.gaussian, ob->bpartial.p,
                                       st));
@@ -391,6 +395,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     } else {
       for (int k = 0; k < bn; ++k) single.push_back(k);
     }
+    ob->stats[RLF_STAT_EXTRACT_SINGLE] += (long long)single.size();
     for (int k : single) {
       const int i = b0 + k;
       const unsigned F = (unsigned)facets[i];
@@ -442,12 +447,15 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fb.queue = dqueue.p + bi;
     fb.trace = nullptr;
     fb.trace_cap = 0;
-    RLF_OK(fit_launch(fb, prec, std::min(grid_fit, bn), st));
+    RLF_OK(fit_launch(fb, fprec, std::min(grid_fit, bn), st));
     RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
+    ob->stats[RLF_STAT_FITTED] += bn;
     if (batched) {
+      ob->stats[RLF_STAT_REMOVE_BATCHES] += 1;
       RLF_OK(launch_remove_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, dg.p + b0, dout.p + b0, bn,
                                  opt.gaussian, st));
     } else {
+      ob->stats[RLF_STAT_REMOVE_SINGLE] += bn;
       for (int k = 0; k < bn; ++k) {
         const int i = b0 + k;
         const double* e12 = &dout.p[i].e1;
@@ -484,6 +492,7 @@ static int process(rlf_observation* ob, int n_gal, const double* flux, const dou
   std::vector<int> order(n_gal);
   for (int i = 0; i < n_gal; ++i) order[i] = i;
   double ms3[3] = {0, 0, 0};
+  for (auto& x : ob->stats) x = 0;
   cudaEvent_t e0, e1;
   RLF_CUDA(cudaEventCreate(&e0));
   RLF_CUDA(cudaEventCreate(&e1));
@@ -846,6 +855,12 @@ int rlf_obs_extract(rlf_observation* obs, int n_gal, const double* flux, const d
   return run_pass(obs, gals, order, 24, ro.data(), o, out, st, nullptr, facets, ncoords, stride);
 }
 
+int rlf_obs_last_stats(rlf_observation* obs, long long* stats) {
+  if (!obs || !stats) return 1;
+  for (int k = 0; k < RLF_NSTATS; ++k) stats[k] = obs->stats[k];
+  return 0;
+}
+
 int rlf_obs_last_timing(rlf_observation* obs, double* ms4) {
   for (int k = 0; k < 4; ++k) ms4[k] = obs->ms[k];
   return 0;
@@ -1180,6 +1195,24 @@ int source_fitting(int rank, likelihood_params* par, double* mes_e1, double* mes
 }
 
 // source_fitting with a record of every likelihood evaluation (e1, e2, L, error) for debugging
+// the facet of a likelihood_params as FP32 cells (the layout the mixed policy reads)
+static int upload_mixed_cells(const likelihood_params* par, DevBuf<float>& fcells, FacetBatch& fb, cudaStream_t st) {
+  const int n = (int)par->ncoords;
+  std::vector<float> h((size_t)5 * (n > 0 ? n : 1));
+  for (int i = 0; i < n; ++i) {
+    h[i] = (float)par->uu[i];
+    h[n + i] = (float)par->vv[i];
+    h[2 * n + i] = (float)par->data[i].real;
+    h[3 * n + i] = (float)par->data[i].imag;
+    h[4 * n + i] = (float)par->sigma2[i];
+  }
+  RLF_OK(fcells.upload(h.data(), h.size(), st));
+  fb.gu = fcells.p; fb.gv = fcells.p + n; fb.dre = fcells.p + 2 * n; fb.dim = fcells.p + 3 * n;
+  fb.sig2 = fcells.p + 4 * n;
+  RLF_CUDA(cudaStreamSynchronize(st));  // h is released on return
+  return 0;
+}
+
 int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int precision) {
   likelihood_params* par = (likelihood_params*)pv;
   cudaStream_t st;
@@ -1188,20 +1221,7 @@ int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int prec
   DevBuf<double> dt;
   RLF_OK(f.load(par, st));
   DevBuf<float> fcells;
-  if (precision == RLF_MIXED) {  // the same facet as FP32 cells for the mixed fit
-    const int n = (int)par->ncoords;
-    std::vector<float> h((size_t)5 * n);
-    for (int i = 0; i < n; ++i) {
-      h[i] = (float)par->uu[i];
-      h[n + i] = (float)par->vv[i];
-      h[2 * n + i] = (float)par->data[i].real;
-      h[3 * n + i] = (float)par->data[i].imag;
-      h[4 * n + i] = (float)par->sigma2[i];
-    }
-    RLF_OK(fcells.upload(h.data(), h.size(), st));
-    f.fb.gu = fcells.p; f.fb.gv = fcells.p + n; f.fb.dre = fcells.p + 2 * n; f.fb.dim = fcells.p + 3 * n;
-    f.fb.sig2 = fcells.p + 4 * n;
-  }
+  if (precision == RLF_MIXED) RLF_OK(upload_mixed_cells(par, fcells, f.fb, st));
   RLF_OK(g_lib.fo.ensure(1));
   RLF_OK(g_lib.i0.ensure(1));
   RLF_OK(dt.ensure((size_t)cap * 4));
@@ -1217,6 +1237,25 @@ int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int prec
   RLF_CUDA(cudaMemcpyAsync(trace, dt.p, (size_t)cap * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   out6[0] = o.e1; out6[1] = o.e2; out6[2] = o.max_e1; out6[3] = o.max_e2; out6[4] = o.maxL; out6[5] = o.nevals;
+  return 0;
+}
+
+int rlf_debug_loglike_nodes(void* pv, double e1, double e2, int precision, double* out2, double* node_L) {
+  likelihood_params* par = (likelihood_params*)pv;
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  OneFacet f;
+  RLF_OK(f.load(par, st));
+  DevBuf<float> fcells;
+  if (precision == RLF_MIXED) RLF_OK(upload_mixed_cells(par, fcells, f.fb, st));
+  DevBuf<double> d;
+  RLF_OK(d.ensure(2 + kMaxNodes));
+  RLF_OK(launch_loglikelihood_prec(f.fb, e1, e2, d.p, d.p + 2, precision == RLF_MIXED ? kMixed : kF64, st));
+  double h[2 + kMaxNodes];
+  RLF_CUDA(cudaMemcpyAsync(h, d.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  out2[0] = h[0]; out2[1] = h[1];
+  for (int k = 0; k < par->numr && k < kMaxNodes; ++k) node_L[k] = h[2 + k];
   return 0;
 }
 

@@ -15,9 +15,12 @@
 //
 // Two arithmetic policies:
 //   F64   -- all double, the reference's arithmetic; the parity path and FP64 GPU oracle.
-//   Mixed -- FP32 cell arithmetic with compensated (Kahan per lane, double-float across lanes)
-//            sums, FP32 scalar arithmetic.  GB300 has little FP64 throughput, so the mixed path
-//            issues no FP64 instruction per likelihood evaluation.
+//   Mixed -- FP32 cell arithmetic (model, products, phase rotations: the work that scales with
+//            the facet size) with compensated sums (Kahan per lane, double-float across lanes,
+//            reduced into double).  The per-node scalars (Newton step, determinant, position
+//            marginal), the marginalisation over scalelength and the simplex/sampling logic run in
+//            FP64: a few hundred lane-uniform operations per evaluation, small beside the cell
+//            loops, and they keep the log-likelihood within 1e-6 relative of the FP64 result.
 #include "rlf_fit.cuh"
 #include <stdio.h>
 
@@ -35,7 +38,6 @@ struct FitConst {
   int np_max;
   int pad;
   double ro[kMaxNodes];
-  float rof[kMaxNodes];
 };
 __constant__ FitConst c_fit;
 
@@ -80,7 +82,7 @@ struct PolicyF64 {
 };
 struct PolicyMixed {
   using Cell = float;
-  using S = float;
+  using S = double;
   static constexpr bool kMixed = true;
 };
 
@@ -111,7 +113,8 @@ __device__ __forceinline__ void s_sincos(float a, float* s, float* c) { sincosf(
 // the same bits).  Float: per-lane Kahan partials combined in double-float, operands ordered by
 // lane so both partners of a butterfly step compute identical bits.
 __device__ __forceinline__ double uwarp_sum(double v) { return warp_sum(v); }
-__device__ __forceinline__ float uwarp_sum_df(float hi, float lo) {
+// butterfly of (hi, lo) double-float partials; afterwards every lane holds the same pair
+__device__ __forceinline__ void df_butterfly(float& hi, float& lo) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int m = 16; m > 0; m >>= 1) {
@@ -126,7 +129,11 @@ __device__ __forceinline__ float uwarp_sum_df(float hi, float lo) {
     hi = r.hi;
     lo = r.lo;
   }
-  return hi + lo;
+}
+// double-float warp sum returned as double, keeping the compensated low part
+__device__ __forceinline__ double uwarp_sum_dfd(float hi, float lo) {
+  df_butterfly(hi, lo);
+  return (double)hi + (double)lo;
 }
 
 template <class S> struct Acc;
@@ -147,7 +154,7 @@ template <> struct Acc<float> {
     s = t;
   }
   __device__ __forceinline__ void sub(float x) { add(-x); }
-  __device__ __forceinline__ float reduce() const { return uwarp_sum_df(s, -c); }
+  __device__ __forceinline__ double reduce() const { return uwarp_sum_dfd(s, -c); }
 };
 
 // ----------------------------------------------------------- position marginal
@@ -156,11 +163,9 @@ template <> struct Acc<float> {
 // from the asymptotic series  e^x / x sum_k k! / x^k  stopped before its smallest term.  The
 // 32 lanes take 32 consecutive k per round and form a_k as a prefix product of x/k across the
 // warp (Hillis-Steele scan), so a series of up to ~100 terms costs 4 rounds instead of 100
-// dependent steps with divisions.  The FP32 form keeps the asymptotic branch in the log domain
-// (e^x overflows single precision above 88).
+// dependent steps with divisions.
 template <class S> __device__ __forceinline__ S wsum(S v);
 template <> __device__ __forceinline__ double wsum<double>(double v) { return uwarp_sum(v); }
-template <> __device__ __forceinline__ float wsum<float>(float v) { return uwarp_sum_df(v, 0.f); }
 
 template <class S>
 __device__ __forceinline__ S warp_prefix_prod(S f) {
@@ -220,30 +225,6 @@ __device__ double pos_marg(double x) {
   return log((yc - ys) / log(x / (x - Delta)));
 }
 
-__device__ __forceinline__ float ei_series_f(float x) {
-  return (float)kEulerGamma + logf(x) + ei_series_sum_warp<float>(x, 1e-9f);
-}
-__device__ __forceinline__ float log_ei_asym_f(float x) {  // ln Ei(x), x >= 25
-  return x - logf(x) + logf(ei_asym_sum_warp<float>(x, 1e-9f));
-}
-
-__device__ float pos_marg(float x) {
-  const float Delta = 0.5f * 5.991f;
-  if (x <= Delta) return (float)kBad;
-  if (x > 100.f) return x - logf(Delta) - expf(-Delta);
-  if ((x - Delta) < 0.0001f) x = Delta + 0.0001f;
-  const float xd = x - Delta;
-  const float lden = logf(log1pf(Delta / xd));
-  if (xd <= 25.f) {
-    if (x <= 25.f) return logf(ei_series_f(x) - ei_series_f(xd)) - lden;
-    const float la = log_ei_asym_f(x);
-    const float eb = ei_series_f(xd);
-    return la + log1pf(-eb * expf(-la)) - lden;
-  }
-  const float la = log_ei_asym_f(x), lb = log_ei_asym_f(xd);
-  return la + log1pf(-expf(lb - la)) - lden;
-}
-
 // --------------------------------------------------------------- cell model
 template <class S>
 __device__ __forceinline__ S cell_shape(int gaussian, S a1, S a2, S a3, S u, S v, S sfw) {
@@ -257,6 +238,9 @@ __device__ __forceinline__ S cell_shape(int gaussian, S a1, S a2, S a3, S u, S v
 
 // Warp-level likelihood at one scalelength node, likelihood.c:156-187 with the model of
 // galaxy_visibilities.c:59-91 and the cross-correlation of likelihood.c:194-358.
+// Cell arithmetic runs in P::Cell (the per-cell model, products and phase rotations); the six
+// cross-correlation sums are reduced into P::S, and the Newton step, determinant, position
+// marginal and log terms are evaluated in P::S (double in both policies).
 // model_in (optional) replaces the computed model (cross_correlation's own entry point);
 // model_out (optional) receives the normalised model (loglikelihood_r writes visM).
 template <class P>
@@ -268,41 +252,43 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
                                       const double* model_in, typename P::S* ho_out,
                                       typename P::S* det_out) {
   using S = typename P::S;
+  using T = typename P::Cell;
   const int lane = threadIdx.x & 31;
-  const S a1 = S(1) + e1, a2 = e2, a3 = S(1) - e1;
+  const T a1 = T(S(1) + e1), a2 = T(e2), a3 = T(S(1) - e1);
   // galaxy_visibilities.c:63-65 then the 4 pi^2 wave factor of :69
   const S detA = S(1) - e1 * e1 - e2 * e2;
   const S sc = r * S(kPi / 648000.0);
-  const S sfw = ((sc * sc) / (detA * detA)) * S(4 * kPi * kPi);
-  const S cc = S(2 * kPi);
-  S inv_s = S(1);
+  const T sfw = T(((sc * sc) / (detA * detA)) * S(4 * kPi * kPi));
+  const T cc = T(2 * kPi);
   S s_norm = S(1);
+  T inv_s = T(1);
   if (!model_in) {
-    Acc<S> acc;
+    Acc<T> acc;
     acc.zero();
     for (int i = lane; i < n; i += 32) {
-      S m = cell_shape<S>(gaussian, a1, a2, a3, S(gu[i]), S(gv[i]), sfw);
-      acc.add(m * m / S(sig2[i]));
+      T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+      acc.add(m * m / T(sig2[i]));
     }
-    S sum = acc.reduce();
+    const S sum = acc.reduce();
     s_norm = s_sqrt(sum);
-    inv_s = S(1) / s_norm;
+    inv_s = T(S(1) / s_norm);
   }
-  auto model_at = [&](int i) -> S {
-    if (model_in) return S(model_in[i]);
-    S m = cell_shape<S>(gaussian, a1, a2, a3, S(gu[i]), S(gv[i]), sfw);
+  const T t_norm = T(s_norm);
+  auto model_at = [&](int i) -> T {
+    if (model_in) return T(model_in[i]);
+    T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
     if (P::kMixed) return m * inv_s;
-    return m / s_norm;  // the reference divides (galaxy_visibilities.c:90)
+    return m / t_norm;  // the reference divides (galaxy_visibilities.c:90)
   };
-  Acc<S> val, dx, dy, d2x, d2y, dxy;
+  Acc<T> val, dx, dy, d2x, d2y, dxy;
   val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
   for (int i = lane; i < n; i += 32) {
-    S m = model_at(i);
+    T m = model_at(i);
     if (model_out) model_out[i] = (double)m;
-    S hre = S(dre[i]) * m;
-    S him = -S(dim[i]) * m;
-    S u = cc * S(gu[i]);
-    S v = cc * S(gv[i]);
+    T hre = T(dre[i]) * m;
+    T him = -T(dim[i]) * m;
+    T u = cc * T(gu[i]);
+    T v = cc * T(gv[i]);
     val.add(hre);
     dx.sub(him * u);
     dy.sub(him * v);
@@ -322,18 +308,19 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
     S incy = (Sdy * Sd2x - Sdx * Sdxy) / det;
     xo -= incx;
     yo -= incy;
+    const T txo = T(xo), tyo = T(yo);
     val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
     for (int i = lane; i < n; i += 32) {
-      S m = model_at(i);
-      S hre = S(dre[i]) * m;
-      S him = -S(dim[i]) * m;
-      S u = cc * S(gu[i]);
-      S v = cc * S(gv[i]);
-      S a = xo * u + yo * v;
-      S sa, ca;
+      T m = model_at(i);
+      T hre = T(dre[i]) * m;
+      T him = -T(dim[i]) * m;
+      T u = cc * T(gu[i]);
+      T v = cc * T(gv[i]);
+      T a = txo * u + tyo * v;
+      T sa, ca;
       s_sincos(a, &sa, &ca);
-      S rp = (hre * ca - him * sa);
-      S ip = (hre * sa + him * ca);
+      T rp = (hre * ca - him * sa);
+      T ip = (hre * sa + him * ca);
       val.add(rp);
       dx.sub(ip * u);
       dy.sub(ip * v);
@@ -599,7 +586,7 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typena
   const int numR = c_fit.numr;
   for (int node = warp + 1; node < numR; node += nw) {
     int it = 0;
-    const S r = P::kMixed ? S(c_fit.rof[node]) : S(c_fit.ro[node]);
+    const S r = S(c_fit.ro[node]);
     S L = node_loglike<P>(gu, gv, dre, dim, sig2, n, e1, e2, r, c_fit.gaussian, &it, nullptr, nullptr,
                           nullptr, nullptr);
     if (lane == 0) {
@@ -617,7 +604,7 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typena
         for (nRo = 1; nRo < numR; nRo++) {
           S lv = sh.Lr[nRo];
           if (lv > S(kBad)) {
-            sh.xs[num] = P::kMixed ? S(c_fit.rof[nRo]) : S(c_fit.ro[nRo]);
+            sh.xs[num] = S(c_fit.ro[nRo]);
             sh.ys[num] = lv + sh.rprior[nRo];
             num++;
           }
@@ -782,6 +769,8 @@ __device__ int nm_iterate(FitCtx<P>& c, Simplex<typename P::S>& s) {
       nm_size(s);
       if (bad) return 5;
     }
+  } else {
+    nm_update(s, hi, xc, val);  // plain reflection accepted
   }
   if (s.S2 > S(0)) s.size = s_sqrt(s.S2);
   else s.size = nm_size(s);
@@ -1112,7 +1101,6 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
   h.np_max = cfg.np_max;
   for (int i = 0; i < kMaxNodes; ++i) {
     h.ro[i] = (i < cfg.numr) ? cfg.ro[i] : 0.0;
-    h.rof[i] = (float)h.ro[i];
   }
   cudaError_t e = cudaMemcpyToSymbolAsync(c_fit, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: fit config: %s\n", cudaGetErrorString(e)); return (int)e; }
@@ -1165,6 +1153,14 @@ int launch_loglikelihood(const FacetBatch& b, double e1, double e2, double* out2
                          cudaStream_t st) {
   k_loglike_once<PolicyF64><<<1, kFitThreads, 0, st>>>(b, e1, e2, out2, node_L);
   return check("k_loglike_once");
+}
+int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
+                              Precision prec, cudaStream_t st) {
+  if (prec == kMixed) {
+    k_loglike_once<PolicyMixed><<<1, kFitThreads, 0, st>>>(b, e1, e2, out2, node_L);
+    return check("k_loglike_once<mixed>");
+  }
+  return launch_loglikelihood(b, e1, e2, out2, node_L, st);
 }
 int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
                                double* out5, cudaStream_t st) {

@@ -60,6 +60,9 @@ int launch_cross_correlation(int n, const double* gu, const double* gv, const do
                              const double* dim, const double* visMod, double* out3, cudaStream_t st);
 int launch_loglikelihood(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
                          cudaStream_t st);
+// the same evaluation in either arithmetic policy (the facet cells must be of that policy's type)
+int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
+                              Precision prec, cudaStream_t st);
 int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
                                double* out5, cudaStream_t st);
 int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st);

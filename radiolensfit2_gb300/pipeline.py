@@ -31,6 +31,7 @@ class ProcessResult:
     results: np.ndarray       # RESULT_DTYPE [n_gal]
     n_bad: int
     ms: tuple                 # (total, extract, fit, remove) milliseconds, CUDA events
+    stats: dict = None        # streaming passes and fitted galaxies (rlf_obs_last_stats)
 
 
 class DeviceObservation:
@@ -107,7 +108,7 @@ class DeviceObservation:
         self._check(self.lib.rlf_obs_restore(self.h), "rlf_obs_restore")
 
     def process(self, cat: Catalogue, *, batch: int = 1, refit: bool = True, gaussian: int = 0,
-                start=None, verbose: int = 0) -> ProcessResult:
+                start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64) -> ProcessResult:
         ro, pro = _d(K.ro_grid())
         arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
         opt = _lib.Options()
@@ -116,6 +117,7 @@ class DeviceObservation:
         opt.gaussian = gaussian
         opt.refit = 1 if refit else 0
         opt.verbose = verbose
+        opt.fit_precision = int(fit_precision)
         st = None
         if start is not None:
             st = np.ascontiguousarray(start, dtype=np.float64).reshape(-1)
@@ -127,7 +129,11 @@ class DeviceObservation:
         res = np.frombuffer(out, dtype=RESULT_DTYPE, count=cat.n).copy()
         ms = (C.c_double * 4)()
         self.lib.rlf_obs_last_timing(self.h, ms)
-        return ProcessResult(res, nbad.value, tuple(ms))
+        sv = (C.c_longlong * 8)()
+        self.lib.rlf_obs_last_stats(self.h, sv)
+        stats = dict(zip(("extract_groups", "extract_single", "remove_batches", "remove_single", "fitted"),
+                         (int(x) for x in sv[:5])))
+        return ProcessResult(res, nbad.value, tuple(ms), stats)
 
     def extract(self, cat: Catalogue, *, batch: int = 1):
         """Facets of every galaxy against the current data and sky model (no fit, no removal).

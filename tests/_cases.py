@@ -61,7 +61,8 @@ def oracle_data_processing(orc, case, data, sky, re_fitting=False, bad_list=None
                             O.dp(sumw), O.cp(gal), O.cp(sky), O.cp(data), O.fp(case.sigma2),
                             O.bp(case.flag), O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), 0, out,
                             C.byref(bad))
-    res = [(r.e1, r.e2, r.var_e1, r.var_e2, r.oneDimvar, r.maxL, r.error, r.nevals) for r in out]
+    res = [(r.e1, r.e2, r.var_e1, r.var_e2, r.oneDimvar, r.maxL, r.error, r.nevals, r.max_e1, r.max_e2)
+           for r in out]
     return data, sky, bad.value, bad_list, res
 
 

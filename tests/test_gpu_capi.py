@@ -152,8 +152,10 @@ def _params(case, gi, F, n, gu, gv, fvis, fs2):
     op.vv = O.dp(gv)
     op.data = O.cp(fvis)
     op.sigma2 = O.dp(fs2)
-    op.mod = O.dp(np.zeros_like(mod))
-    keep.append(op.mod)
+    # a struct field keeps only the address: the scratch array itself must stay referenced
+    omod = np.zeros_like(mod)
+    keep.append(omod)
+    op.mod = O.dp(omod)
     return p, op, keep
 
 
@@ -286,7 +288,9 @@ def test_data_processing_f64(lib, orc, case, sky):
     assert bad.value == bad_ref
     assert np.array_equal(bad_list[:bad_ref], bl_ref[:bad_ref])
     assert rel(data, d_ref) < 1e-11
-    assert rel(skym, s_ref) < 1e-11
+    # every galaxy's round model has been subtracted: both sky models are left at rounding level,
+    # so the difference is measured against the scale of the sky model before the loop
+    assert np.max(np.abs(skym - s_ref)) < 1e-11 * np.max(np.abs(sky))
 
 
 def test_device_pipeline_f64_matches_oracle(orc, case, sky):
@@ -302,4 +306,5 @@ def test_device_pipeline_f64_matches_oracle(orc, case, sky):
         assert pr.results["maxL"][gi] == pytest.approx(r[5], rel=1e-9, abs=1e-9)
         assert pr.results["nevals"][gi] == r[7]
     d, s = dev.get_vis()
-    assert rel(d, d_ref) < 1e-11 and rel(s, s_ref) < 1e-11
+    assert rel(d, d_ref) < 1e-11
+    assert np.max(np.abs(s - s_ref)) < 1e-11 * np.max(np.abs(sky))

@@ -57,30 +57,49 @@ def test_facets_against_oracle(orc, case, sky, precision, batch, tol):
 
 
 def test_pipeline_modes(orc, case, sky):
+    """Sequential modes against the oracle's data_processing (first pass, catalogue order).
+
+    f64        FP64 everywhere: the reference's arithmetic, bit-for-bit simplex path.
+    mixed      FP32 visibility passes, FP64 fit: the FP32 facet error is a smooth perturbation of
+               the likelihood surface, so the fit follows the reference's simplex path and the
+               fitted ellipticities stay within 1e-4 (log-likelihood within 1e-6 relative).
+    mixed-fit  FP32 visibility passes and FP32 fit cells: the log-likelihood stays within 1e-6
+               relative, but its rounding noise varies with (e1, e2) and can change nmsimplex2
+               decisions, so e agrees only statistically (checked on the median).
+    """
     d_ref, s_ref, bad_ref, bl_ref, ref = oracle_data_processing(orc, case, case.data, sky)
     e_ref = np.array([(r[0], r[1]) for r in ref])
     L_ref = np.array([r[5] for r in ref])
     err_ref = np.array([r[6] for r in ref])
     out = {}
-    for name, prec, batch in (("f64", _lib.RLF_F64, 1), ("mixed", _lib.RLF_MIXED, 1), ("batched", _lib.RLF_MIXED, 16)):
+    modes = (("f64", _lib.RLF_F64, _lib.RLF_F64, 1), ("mixed", _lib.RLF_MIXED, _lib.RLF_F64, 1),
+             ("mixed-fit", _lib.RLF_MIXED, _lib.RLF_MIXED, 1))
+    for name, prec, fprec, batch in modes:
         dev = _dev(case, sky, prec)
-        pr = dev.process(case.cat, batch=batch, refit=False)
+        pr = dev.process(case.cat, batch=batch, refit=False, fit_precision=fprec)
         out[name] = pr.results
         dev.close()
     f = out["f64"]
     assert np.array_equal(f["error"], err_ref)
     good = err_ref == 0
-    assert np.allclose(f["max_e1"][good], [r for r in f["max_e1"][good]])
+    # simplex maxima before the sampling step: same iterates as the oracle's nmsimplex2
+    assert np.max(np.abs(f["max_e1"][good] - np.array([r[8] for r in ref])[good])) < 1e-9
+    assert np.max(np.abs(f["max_e2"][good] - np.array([r[9] for r in ref])[good])) < 1e-9
     assert np.max(np.abs(f["e1"][good] - e_ref[good, 0])) < 1e-7
     assert np.max(np.abs(f["e2"][good] - e_ref[good, 1])) < 1e-7
     assert np.allclose(f["maxL"][good], L_ref[good], rtol=1e-9)
-    for name in ("mixed", "batched"):
+    stats = {}
+    for name in ("mixed", "mixed-fit"):
         r = out[name]
         ok = good & (r["error"] == 0)
         de = np.maximum(np.abs(r["e1"][ok] - e_ref[ok, 0]), np.abs(r["e2"][ok] - e_ref[ok, 1]))
         dL = np.abs(r["maxL"][ok] - L_ref[ok]) / np.abs(L_ref[ok])
+        stats[name] = (de, dL, int(np.sum(r["error"] != err_ref)))
         print(f"{name}: |de| max {de.max():.2e} median {np.median(de):.2e}; |dL/L| max {dL.max():.2e}; "
               f"errors {int(r['error'].sum())} vs {int(err_ref.sum())}")
-        assert np.sum(r["error"] != err_ref) <= 1
-        assert np.median(de) < 1e-4
-        assert np.max(dL) < 1e-5
+    de, dL, nerr = stats["mixed"]
+    assert nerr == 0
+    assert de.max() < 1e-4 and dL.max() < 1e-6
+    de, dL, nerr = stats["mixed-fit"]
+    assert nerr <= 1
+    assert np.median(de) < 1e-3 and dL.max() < 1e-5
