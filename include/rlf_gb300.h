@@ -120,6 +120,29 @@ enum {
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
 
+/* -------- gridding without device allocation --------
+ * No counterpart in the reference.  The gridding of gridding_visibilities (evaluate_uv_grid.c),
+ * for callers that cannot allocate device memory: code inside a framework that owns the device
+ * heap (a caching allocator or a fixed pool) and real-time callers that forbid allocation after
+ * start-up.  It calls no cudaMalloc/cudaFree and no allocating library routine.
+ *   u, v [ncoords], vis [num_channels*ncoords] complex128 (channel-major), sigma2, flag (may be
+ *   NULL): DEVICE pointers; wavenumbers [num_channels]: a host array.  Outputs (DEVICE pointers,
+ *   the layout of gridding_visibilities): new_vis [sizeg^2] complex128 and new_sigma2 [sizeg^2],
+ *   both compacted to the non-empty cells in row-major order; sum_w [sizeg^2].
+ *   stream: a cudaStream_t (NULL = the legacy default stream); the call waits for that stream.
+ * Limits: sizeg <= RLF_NOALLOC_MAX_FACET, 1 <= num_channels <= 512; other sizes return an error.
+ * The partial sums live in one fixed 4.6 MiB array of this library's device memory that every
+ * GPU loading the library holds until exit.  The first call on a device looks up that array's
+ * device address, so make a first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other threads or streams) race and must be serialised by the
+ * caller.  Returns 0, or non-zero with a message on stderr. */
+#define RLF_NOALLOC_MAX_FACET 48
+int rlf_gridding_visibilities_noalloc(const double *wavenumbers, unsigned int num_channels,
+                                      unsigned int ncoords, const double *u, const double *v,
+                                      const double *vis, const float *sigma2, const uint8_t *flag,
+                                      double len, unsigned int sizeg, double *new_vis,
+                                      double *new_sigma2, double *sum_w, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
