@@ -163,19 +163,43 @@ __device__ __forceinline__ float round_shape(float sfq) {
 }
 
 // ------------------------------------------------------------- extraction
-// grid: (ctas_per_group, n_groups); block: kBatchWarps * 32; galaxies of group j are
+// grid: (ctas_per_group, n_groups); block: up to kBatchWarps warps; galaxies of group j are
 // gals[gidx[j*32 + lane]] (index < 0 = empty lane).  Shared memory: one facet per CTA,
 // [F*F][32] float2 (lane = galaxy), updated with shared-memory atomics (warps of a CTA collide
-// only when they hit the same cell of the same galaxy at the same time).
+// only when they hit the same cell of the same galaxy at the same time), then one staging tile
+// per warp.
+//
+// Each warp walks its span of rows in tiles of kTileRows rows x kChunk channels.  The tile is
+// staged with coalesced loads (lane -> row, half of the channels) as {data - sky, wn^2 |uv|^2,
+// spec} per visibility plus the row's delay coordinates, and two 16-bit masks per row: valid
+// channels and channels that start a run of one cell.  The 32 lanes (galaxies) then read every
+// staged value as a shared-memory broadcast, so the per-visibility work is the Horner step and
+// the round-model shape; the phase set-up is per row and the anchor + facet update per run.
 // partial: [n_groups][ctas_per_group][F*F][32] float2
+constexpr int kTileRows = 16;
+constexpr int kChunk = 16;
+constexpr uint32_t kFullRun = 0x0001FFFFu;  // all kChunk channels valid, one run from channel 0
+
+struct __align__(16) ExtractTile {
+  float4 v[kChunk][kTileRows];       // (re, im) of data - sky, wn^2 (u^2 + v^2), spec
+  RowF row[kTileRows];
+  uint16_t cell[kChunk][kTileRows];
+  uint32_t mask[kTileRows];          // bits 0-15: valid channel; bits 16-31: run starts here
+};
+
+__host__ __device__ constexpr size_t extract_facet_bytes(int F) { return (size_t)F * F * 32 * sizeof(float2); }
+
 template <int GAUSS>
 __global__ void __launch_bounds__(kBatchWarps * 32) k_extract_batch(
     int n_rows, const RowF* __restrict__ rows, const float2* __restrict__ data, const float2* __restrict__ sky,
     const uint16_t* __restrict__ cell, const GalaxyParams* __restrict__ gals, const int* __restrict__ gidx,
     int F, float2* __restrict__ partial) {
-  extern __shared__ float2 acc[];  // [cell][lane]
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [cell][lane]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
   const int nc = F * F;
+  ExtractTile& tile = reinterpret_cast<ExtractTile*>(smem_raw + ((extract_facet_bytes(F) + 15) & ~(size_t)15))[warp];
   const int group = blockIdx.y;
   for (int i = threadIdx.x; i < nc * 32; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
   __syncthreads();
@@ -189,48 +213,121 @@ __global__ void __launch_bounds__(kBatchWarps * 32) k_extract_batch(
   const long long per_cta = ((long long)n_rows + gridDim.x - 1) / gridDim.x;
   const long long r_begin = blockIdx.x * per_cta;
   const long long r_end = min((long long)n_rows, r_begin + per_cta);
-  const long long per_warp = (r_end - r_begin + kBatchWarps - 1) / kBatchWarps;
+  const long long per_warp = (r_end - r_begin + nwarps - 1) / nwarps;
   const long long w_begin = r_begin + warp * per_warp;
   const long long w_end = min(r_end, w_begin + per_warp);
-  for (long long r = w_begin; r < w_end; ++r) {
-    const RowF rw = rows[r];
-    const f2 p = delay_df(rw, g);
-    const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
-    const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
-    float ws, wc;
-    sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
-    const float wr = wc, wi = -ws;  // w = exp(-2 pi i dT)
-    int ch = 0;
-    while (ch < nch) {
-      const uint16_t c = cell[(size_t)ch * n_rows + r];
-      if (c == kNoCell) { ++ch; continue; }
-      int end = ch + 1;
-      while (end < nch && end - ch < 16 && cell[(size_t)end * n_rows + r] == c) ++end;
-      // Horner over the run [ch, end): S = sum_k R_k w^(k-ch)
-      float sr = 0.f, si = 0.f, rs = 0.f;
-      for (int k = end - 1; k >= ch; --k) {
-        const float2 d = data[(size_t)k * n_rows + r];
-        const float2 s = sky[(size_t)k * n_rows + r];
-        const float Rr = d.x - s.x, Ri = d.y - s.y;
-        const float nr = fmaf(sr, wr, fmaf(-si, wi, Rr));
-        const float ni = fmaf(sr, wi, fmaf(si, wr, Ri));
-        sr = nr;
-        si = ni;
-        const BatchChan bc = c_bch[k];
-        const float x = g.sf0 * bc.wn2 * rw.q;
-        const float sh = GAUSS ? __expf(-0.5f * x) : round_shape(x);
-        rs = fmaf(sh, bc.spec, rs);
+  const int srow = lane & (kTileRows - 1);   // staging: row of this lane
+  const int shalf = lane >> 4;               // staging: channel half (8 channels)
+  for (long long r0 = w_begin; r0 < w_end; r0 += kTileRows) {
+    const int nr = (int)min((long long)kTileRows, w_end - r0);
+    const long long rs_row = r0 + srow;
+    const bool row_ok = srow < nr;
+    if (shalf == 0 && row_ok) tile.row[srow] = rows[rs_row];
+    const float q = row_ok ? rows[rs_row].q : 0.f;
+    for (int c0 = 0; c0 < nch; c0 += kChunk) {
+      // ---- stage kTileRows rows x kChunk channels
+#pragma unroll
+      for (int t = 0; t < kChunk / 2; ++t) {
+        const int k = shalf * (kChunk / 2) + t;
+        const int ch = c0 + k;
+        uint16_t c = kNoCell;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row_ok && ch < nch) {
+          const size_t idx = (size_t)ch * n_rows + rs_row;
+          c = cell[idx];
+          const float2 d = data[idx], sk = sky[idx];
+          const BatchChan bc = c_bch[ch];
+          v = make_float4(d.x - sk.x, d.y - sk.y, bc.wn2 * q, bc.spec);
+        }
+        tile.v[k][srow] = v;
+        tile.cell[k][srow] = c;
       }
-      float zs, zc;
-      sincospif(2.f * turns_at(T0, dT, ch), &zs, &zc);
-      const float zr = zc, zi = -zs;  // exp(-2 pi i T(ch))
-      const float cr = fmaf(sr, zr, fmaf(-si, zi, rs * g.flux));
-      const float ci = fmaf(sr, zi, si * zr);
-      if (g.active) {
-        atomicAdd(my + (size_t)c * 64, cr);
-        atomicAdd(my + (size_t)c * 64 + 1, ci);
+      __syncwarp();
+      if (shalf == 0) {
+        uint32_t valid = 0, start = 0;
+        uint16_t prev = kNoCell;
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+          const uint16_t c = tile.cell[k][srow];
+          if (c != kNoCell) {
+            valid |= 1u << k;
+            if (c != prev) start |= 1u << k;
+          }
+          prev = c;
+        }
+        tile.mask[srow] = valid | (start << 16);
       }
-      ch = end;
+      __syncwarp();
+      // ---- every lane (galaxy) walks the staged rows
+      for (int j = 0; j < nr; ++j) {
+        const uint32_t m = tile.mask[j];
+        if (m == 0) continue;
+        const RowF rw = tile.row[j];
+        const f2 p = delay_df(rw, g);
+        const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
+        const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
+        float ws, wc;
+        sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
+        const float wr = wc, wi = -ws;  // w = exp(-2 pi i dT)
+        float sr = 0.f, si = 0.f, rsum = 0.f;
+        if (m == kFullRun) {
+          // the common row: every channel of the chunk valid and in one cell
+#pragma unroll
+          for (int k = kChunk - 1; k >= 0; --k) {
+            const float4 v = tile.v[k][j];
+            const float nr_ = fmaf(sr, wr, fmaf(-si, wi, v.x));
+            const float ni_ = fmaf(sr, wi, fmaf(si, wr, v.y));
+            sr = nr_;
+            si = ni_;
+            const float x = g.sf0 * v.z;
+            const float sh = GAUSS ? __expf(-0.5f * x) : round_shape(x);
+            rsum = fmaf(sh, v.w, rsum);
+          }
+          float zs, zc;
+          const float ta = c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0);
+          sincospif(2.f * ta, &zs, &zc);
+          const float zr = zc, zi = -zs;
+          const float cr = fmaf(sr, zr, fmaf(-si, zi, rsum * g.flux));
+          const float ci = fmaf(sr, zi, si * zr);
+          if (g.active) {
+            const int c = tile.cell[0][j];
+            atomicAdd(my + (size_t)c * 64, cr);
+            atomicAdd(my + (size_t)c * 64 + 1, ci);
+          }
+          continue;
+        }
+        // Horner over each run, from its last channel down to its first: S = sum_k R_k w^(k - first)
+#pragma unroll
+        for (int k = kChunk - 1; k >= 0; --k) {
+          if (m & (1u << k)) {
+            const float4 v = tile.v[k][j];
+            const float nr_ = fmaf(sr, wr, fmaf(-si, wi, v.x));
+            const float ni_ = fmaf(sr, wi, fmaf(si, wr, v.y));
+            sr = nr_;
+            si = ni_;
+            const float x = g.sf0 * v.z;
+            const float sh = GAUSS ? __expf(-0.5f * x) : round_shape(x);
+            rsum = fmaf(sh, v.w, rsum);
+            if (m & (1u << (16 + k))) {
+              float zs, zc;
+              const float ta = (c0 + k == 0) ? (T0.hi + T0.lo) : turns_at(T0, dT, c0 + k);
+              sincospif(2.f * ta, &zs, &zc);
+              const float zr = zc, zi = -zs;  // exp(-2 pi i T(first channel))
+              const float cr = fmaf(sr, zr, fmaf(-si, zi, rsum * g.flux));
+              const float ci = fmaf(sr, zi, si * zr);
+              if (g.active) {
+                const int c = tile.cell[k][j];
+                atomicAdd(my + (size_t)c * 64, cr);
+                atomicAdd(my + (size_t)c * 64 + 1, ci);
+              }
+              sr = 0.f;
+              si = 0.f;
+              rsum = 0.f;
+            }
+          }
+        }
+      }
+      __syncwarp();
     }
   }
   __syncthreads();
@@ -309,15 +406,20 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
 int launch_extract_batch(int n_rows, const RowF* rows, const float2* data, const float2* sky, const uint16_t* cell,
                          const GalaxyParams* gals, const int* gidx, int n_groups, int F, int ctas, int gaussian,
                          float2* partial, cudaStream_t st) {
-  const size_t smem = (size_t)F * F * 32 * sizeof(float2);
-  if (smem > kBatchSmemMax) { fprintf(stderr, "rlf: batched extraction facet %d too large\n", F); return 1; }
+  if (F < 1 || (unsigned)F > kBatchMaxFacet) { fprintf(stderr, "rlf: batched extraction facet %d unsupported\n", F); return 1; }
+  const size_t facet = (extract_facet_bytes(F) + 15) & ~(size_t)15;
+  // as many warps (each with its staging tile) as fit beside the facet, at most kBatchWarps
+  int warps = (int)((kBatchSmemMax - facet) / sizeof(ExtractTile));
+  if (warps > kBatchWarps) warps = kBatchWarps;
+  if (warps < 1) { fprintf(stderr, "rlf: batched extraction facet %d too large\n", F); return 1; }
+  const size_t smem = facet + (size_t)warps * sizeof(ExtractTile);
   const void* kern = gaussian ? (const void*)k_extract_batch<1> : (const void*)k_extract_batch<0>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid(ctas, n_groups);
   if (gaussian)
-    k_extract_batch<1><<<grid, kBatchWarps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
+    k_extract_batch<1><<<grid, warps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
   else
-    k_extract_batch<0><<<grid, kBatchWarps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
+    k_extract_batch<0><<<grid, warps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
   return check("k_extract_batch");
 }
 

@@ -6,7 +6,7 @@
 namespace rlf {
 
 constexpr int kBatchWarps = 8;                    // warps per extraction CTA (32 galaxies each)
-constexpr size_t kBatchSmemMax = 200 * 1024;      // shared facet of one CTA: F*F*32 float2
+constexpr size_t kBatchSmemMax = 227 * 1024;      // shared memory of one extraction CTA
 constexpr unsigned kBatchMaxFacet = 28;           // largest facet the batched extraction holds
 constexpr int kRemCh = 16;                        // channels per removal thread
 constexpr int kRemTile = 64;                      // galaxies staged per shared-memory tile

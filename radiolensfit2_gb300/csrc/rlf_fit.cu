@@ -31,6 +31,7 @@ constexpr int kFitThreads = kFitWarps * 32;
 constexpr int kQagCap = 256;       // intervals held by the device QAG
 constexpr int kNewtonMax = 50;     // likelihood.c:290
 constexpr int kSimplexMax = 50;    // galaxy_fitting.c:80
+constexpr int kModelCache = 4;     // facet cells per lane whose model stays in registers
 
 struct FitConst {
   int numr;
@@ -262,10 +263,23 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
   const T cc = T(2 * kPi);
   S s_norm = S(1);
   T inv_s = T(1);
+  // the unnormalised model of the first kModelCache cells of this lane, kept in registers for
+  // the cross-correlation passes (the model does not change during the Newton search)
+  T mc[kModelCache];
   if (!model_in) {
     Acc<T> acc;
     acc.zero();
-    for (int i = lane; i < n; i += 32) {
+#pragma unroll
+    for (int t = 0; t < kModelCache; ++t) {
+      const int i = lane + 32 * t;
+      mc[t] = T(0);
+      if (i < n) {
+        const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+        mc[t] = m;
+        acc.add(m * m / T(sig2[i]));
+      }
+    }
+    for (int i = lane + 32 * kModelCache; i < n; i += 32) {
       T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
       acc.add(m * m / T(sig2[i]));
     }
@@ -274,16 +288,22 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
     inv_s = T(S(1) / s_norm);
   }
   const T t_norm = T(s_norm);
-  auto model_at = [&](int i) -> T {
-    if (model_in) return T(model_in[i]);
-    T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+  auto normalise = [&](T m) -> T {
     if (P::kMixed) return m * inv_s;
     return m / t_norm;  // the reference divides (galaxy_visibilities.c:90)
   };
+  if (!model_in) {
+#pragma unroll
+    for (int t = 0; t < kModelCache; ++t) mc[t] = normalise(mc[t]);
+  }
+  // normalised model of cell i beyond the cached ones
+  auto model_tail = [&](int i) -> T {
+    if (model_in) return T(model_in[i]);
+    return normalise(cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw));
+  };
   Acc<T> val, dx, dy, d2x, d2y, dxy;
   val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
-  for (int i = lane; i < n; i += 32) {
-    T m = model_at(i);
+  auto first_cell = [&](int i, T m) {
     if (model_out) model_out[i] = (double)m;
     T hre = T(dre[i]) * m;
     T him = -T(dim[i]) * m;
@@ -295,7 +315,14 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
     d2x.sub(hre * u * u);
     d2y.sub(hre * v * v);
     dxy.sub(hre * u * v);
+  };
+  // cells in the order i = lane, lane + 32, ... (cached ones first, then the rest)
+#pragma unroll
+  for (int t = 0; t < kModelCache; ++t) {
+    const int i = lane + 32 * t;
+    if (i < n) first_cell(i, model_in ? T(model_in[i]) : mc[t]);
   }
+  for (int i = lane + 32 * kModelCache; i < n; i += 32) first_cell(i, model_tail(i));
   S Sval = val.reduce(), Sdx = dx.reduce(), Sdy = dy.reduce();
   S Sd2x = d2x.reduce(), Sd2y = d2y.reduce(), Sdxy = dxy.reduce();
   S det = Sd2x * Sd2y - Sdxy * Sdxy;
@@ -310,8 +337,7 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
     yo -= incy;
     const T txo = T(xo), tyo = T(yo);
     val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
-    for (int i = lane; i < n; i += 32) {
-      T m = model_at(i);
+    auto newton_cell = [&](int i, T m) {
       T hre = T(dre[i]) * m;
       T him = -T(dim[i]) * m;
       T u = cc * T(gu[i]);
@@ -327,7 +353,13 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
       d2x.sub(rp * u * u);
       d2y.sub(rp * v * v);
       dxy.sub(rp * u * v);
+    };
+#pragma unroll
+    for (int t = 0; t < kModelCache; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) newton_cell(i, model_in ? T(model_in[i]) : mc[t]);
     }
+    for (int i = lane + 32 * kModelCache; i < n; i += 32) newton_cell(i, model_tail(i));
     Sval = val.reduce(); Sdx = dx.reduce(); Sdy = dy.reduce();
     Sd2x = d2x.reduce(); Sd2y = d2y.reduce(); Sdxy = dxy.reduce();
     det = Sd2x * Sd2y - Sdxy * Sdxy;

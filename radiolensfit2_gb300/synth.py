@@ -84,6 +84,10 @@ WORKLOADS = {
                             fmin=5.0, fmax=200.0, g=(0.03, -0.02)),
     "c4_ska_mid_64ch": dict(n_ant=197, ha_hours=4.0, dt_s=30.0, n_ch=64, n_gal=50000,
                             fmin=5.0, fmax=200.0, g=(0.02, 0.01)),
+    # profiling case: C1's channel layout on a smaller array, 15.6M visibilities (250 MB of FP32
+    # data and sky model, larger than the 129 MB L2), 64 galaxies
+    "mid_128ant_16ch": dict(n_ant=128, ha_hours=1.0, dt_s=60.0, n_ch=16, n_gal=64,
+                            fmin=10.0, fmax=200.0, g=(0.03, -0.02)),
 }
 
 ARRAY_SEED, CATALOGUE_SEED, NOISE_SEED = 1, 2, 3
