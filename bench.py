@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--workload", default="c1_ska_mid_16ch")
     ap.add_argument("--galaxies", type=int, default=0)
     ap.add_argument("--batch", type=int, default=1000)
+    ap.add_argument("--rounds", type=int, default=0,
+                    help="extraction + fit rounds per batch (0 = library default)")
     ap.add_argument("--fit-precision", default="f64", choices=["f64", "mixed"],
                     help="arithmetic of the fit (visibility passes are always mixed)")
     ap.add_argument("--no-plain", action="store_true")
@@ -256,38 +258,39 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
 def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak):
     """Roofline of the dominant stage of a step.
 
-    Algorithmic bytes (streaming passes of the batched path): extraction reads data and sky model
-    (2 x 8 B FP32 complex) per visibility and 24 B of uvw per row once per group of up to 32
-    galaxies of one facet size; removal reads and writes data and sky model (32 B) per visibility
-    and the uvw row once per batch.  Algorithmic FP32 work per galaxy-visibility pair: extraction
-    24 FLOP, removal 40 FLOP (FMA = 2).  The fit stage reads only facets (kilobytes) and is
-    reported by FLOP-free time only."""
+    Algorithmic bytes of the streaming passes: a sequential batch extraction pass reads data and
+    sky model (2 x 8 B FP32 complex) per visibility and the 32 B row table entry per row; a removal
+    pass reads and writes data and sky model (32 B) per visibility and reads the row table.
+    Algorithmic FP32 work per galaxy-visibility pair (FMA = 2): extraction 15 FLOP in a first round
+    (Horner step 8, round-model profile 5, spectral sum 2) and 33 FLOP in a correction round (phase
+    recurrence 6, rotation 8, two profiles 10, model difference and residual update 9); removal
+    40 FLOP.  The fit reads only facets (kilobytes) and has no streaming roofline."""
     n_vis, n_rows = float(obs.n_vis), float(obs.n_rows)
     good = int(np.sum(batched["error"] == 0))
     st = res.stats  # passes of the last step (both passes), counted by the library
     dominant = max(stage_ms, key=stage_ms.get)
     t = stage_ms[dominant] * 1e-3
     if dominant == "extract":
-        nbytes = (st["extract_groups"] + st["extract_single"]) * (16.0 * n_vis + 24.0 * n_rows)
-        flops = 24.0 * n_vis * st["fitted"]
+        nbytes = (st["extract_passes"] + st["extract_single"]) * (16.0 * n_vis + 32.0 * n_rows)
+        first = st["extract_gal_first"]
+        flops = n_vis * (15.0 * first + 33.0 * (st["extract_gal"] - first))
     elif dominant == "remove":
-        nbytes = (st["remove_batches"] + st["remove_single"]) * (32.0 * n_vis + 24.0 * n_rows)
+        nbytes = (st["remove_batches"] + st["remove_single"]) * (32.0 * n_vis + 32.0 * n_rows)
         flops = 40.0 * n_vis * good
     else:
         nbytes, flops = None, None
-    kernel = {"remove": "k_remove_batch", "extract": "k_extract_batch", "fit": "k_fit"}[dominant]
+    kernel = {"remove": "k_remove_batch", "extract": "k_extract_seq", "fit": "k_fit"}[dominant]
     r = {"kernel": kernel, "bound": "hbm", "unit": "GB/s",
          "achieved": nbytes / t / 1e9 if nbytes else None, "peak": hbm_peak,
          "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
          "traffic": None, "time_ms_per_step": stage_ms[dominant], "passes": st}
     r["frac"] = r["achieved"] / hbm_peak if r["achieved"] else None
     if flops:
-        # the batched passes are FP32-pipe bound (sincos + FMAs), not HBM bound
+        # the batched passes are FP32-pipe bound (profiles, phase recurrences), not HBM bound
         r["compute"] = {"bound": "fp32", "unit": "TFLOP/s", "achieved": flops / t / 1e12,
                         "peak": fp32_peak / 1e3, "peak_kind": "measured FP32 FMA probe kernel",
                         "frac": flops / t / 1e12 / (fp32_peak / 1e3)}
     return r
-
 
 def main():
     args = parse()
@@ -317,7 +320,7 @@ def main():
 
     def step():
         dev.restore()
-        return dev.process(cat, batch=B, refit=True, fit_precision=fit_prec)
+        return dev.process(cat, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
 
     for _ in range(args.warmup):
         step()

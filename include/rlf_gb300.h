@@ -40,6 +40,10 @@ typedef struct {
                         ellipticities follow the reference's simplex path) or RLF_MIXED (FP32 cell
                         arithmetic: faster, log-likelihood within ~2e-7 relative, but rounding
                         noise can change simplex decisions, moving e by up to ~1e-3) */
+  int rounds;        /* batched mode: extraction + fit rounds per batch (0 = default 3).  Round 1
+                        extracts every galaxy of the batch from the same data; each further round
+                        removes the previous round's fitted models of the earlier galaxies of the
+                        batch from each facet, converging to the one-galaxy-at-a-time result. */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -104,18 +108,26 @@ int rlf_debug_loglike_nodes(void *likelihood_params_facet, double e1, double e2,
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
 
 /* Work counters of the last rlf_obs_process (both passes), for throughput and roofline figures:
- * stats[RLF_STAT_EXTRACT_GROUPS]  batched extraction passes over all visibilities (one per group
- *                                 of up to 32 galaxies of one facet size),
+ * stats[RLF_STAT_EXTRACT_PASSES]  sequential batch extraction passes over all visibilities,
  * stats[RLF_STAT_EXTRACT_SINGLE]  one-galaxy extraction passes,
- * stats[RLF_STAT_REMOVE_BATCHES]  batched removal passes (one per batch),
+ * stats[RLF_STAT_REMOVE_BATCHES]  batched removal passes (one per sub-batch),
  * stats[RLF_STAT_REMOVE_SINGLE]   one-galaxy removal passes,
- * stats[RLF_STAT_FITTED]          galaxies fitted. */
+ * stats[RLF_STAT_FITTED]          galaxy fits (every round counts),
+ * stats[RLF_STAT_EXTRACT_GAL]     galaxies extracted by the batch passes, summed over passes
+ *                                 (x visibilities = galaxy-visibility pairs),
+ * stats[RLF_STAT_CHANGED]         galaxies whose fit still changed in the last round of their
+ *                                 sub-batch (ellipticity by more than 1e-9 or the error flag),
+ * stats[RLF_STAT_EXTRACT_GAL_FIRST] the part of RLF_STAT_EXTRACT_GAL in first rounds (no model
+ *                                 differences removed). */
 enum {
-  RLF_STAT_EXTRACT_GROUPS = 0,
+  RLF_STAT_EXTRACT_PASSES = 0,
   RLF_STAT_EXTRACT_SINGLE = 1,
   RLF_STAT_REMOVE_BATCHES = 2,
   RLF_STAT_REMOVE_SINGLE = 3,
   RLF_STAT_FITTED = 4,
+  RLF_STAT_EXTRACT_GAL = 5,
+  RLF_STAT_CHANGED = 6,
+  RLF_STAT_EXTRACT_GAL_FIRST = 7,
   RLF_NSTATS = 8
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);

@@ -20,6 +20,7 @@
 #include "rlf_batch.cuh"
 #include "rlf_fit.cuh"
 #include <stdio.h>
+#include <algorithm>
 
 namespace rlf {
 
@@ -163,195 +164,296 @@ __device__ __forceinline__ float round_shape(float sfq) {
 }
 
 // ------------------------------------------------------------- extraction
-// grid: (ctas_per_group, n_groups); block: up to kBatchWarps warps; galaxies of group j are
-// gals[gidx[j*32 + lane]] (index < 0 = empty lane).  Shared memory: one facet per CTA,
-// [F*F][32] float2 (lane = galaxy), updated with shared-memory atomics (warps of a CTA collide
-// only when they hit the same cell of the same galaxy at the same time), then one staging tile
-// per warp.
-//
-// Each warp walks its span of rows in tiles of kTileRows rows x kChunk channels.  The tile is
-// staged with coalesced loads (lane -> row, half of the channels) as {data - sky, wn^2 |uv|^2,
-// spec} per visibility plus the row's delay coordinates, and two 16-bit masks per row: valid
-// channels and channels that start a run of one cell.  The 32 lanes (galaxies) then read every
-// staged value as a shared-memory broadcast, so the per-visibility work is the Horner step and
-// the round-model shape; the phase set-up is per row and the anchor + facet update per run.
-// partial: [n_groups][ctas_per_group][F*F][32] float2
-constexpr int kTileRows = 16;
+// Sequential batch extraction: the facets of a batch of galaxies in catalogue order, each one
+// extracted as data_processing.c:61-138 would extract it after fitting and removing every earlier
+// galaxy of the batch.  One thread holds the residual data - sky of one row and 16 channels in
+// registers and walks the batch's galaxies in order; for galaxy j it
+//   * adds the residual, phase-shifted to the galaxy (exp(-2 pi i T_j)), plus the galaxy's own
+//     round model (real after the shift) into the galaxy's facet cell: source_extraction.c:46-68
+//     and the gridding of evaluate_uv_grid.c:143-211;
+//   * subtracts the galaxy's model difference fitted - round of the previous round's fit from the
+//     residual (data_processing.c:109-135 removes the fitted model from the data and the round
+//     model from the sky model), so every later galaxy sees it removed.
+// The first round (no fits yet) is the plain batched extraction; each further round uses the fits
+// of the round before, and the rounds converge to the sequential result (a galaxy's facet depends
+// on earlier galaxies' fits only through their weak, smooth model differences).
+// The phase of each (row, galaxy) is formed once: delay p = u l + v m + w n in double-float, phase
+// turns T(ch) = p * inv_lambda(ch) = T0 + ch * dT, reduced modulo 1.  Within a 16-channel chunk the
+// rotation is a recurrence in w = exp(-2 pi i dT) anchored with an accurate sincospi at the first
+// channel of the chunk (Horner's rule when nothing is removed).
+// Facets of all batch galaxies are accumulated in shared memory (FP32 atomics); every CTA writes
+// its partial facets, reduced in FP64 in CTA order by k_finalize_seq.
 constexpr int kChunk = 16;
-constexpr uint32_t kFullRun = 0x0001FFFFu;  // all kChunk channels valid, one run from channel 0
 
-struct __align__(16) ExtractTile {
-  float4 v[kChunk][kTileRows];       // (re, im) of data - sky, wn^2 (u^2 + v^2), spec
-  RowF row[kTileRows];
-  uint16_t cell[kChunk][kTileRows];
-  uint32_t mask[kTileRows];          // bits 0-15: valid channel; bits 16-31: run starts here
+struct __align__(16) SeqGal {
+  GalF g;
+  int fidx;      // facet size index
+  int off;       // facet offset in the shared buffer (float2 units)
+  int apply;     // subtract fitted - round (good fit in the previous round)
 };
 
-__host__ __device__ constexpr size_t extract_facet_bytes(int F) { return (size_t)F * F * 32 * sizeof(float2); }
+__host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-template <int GAUSS>
-__global__ void __launch_bounds__(kBatchWarps * 32) k_extract_batch(
-    int n_rows, const RowF* __restrict__ rows, const float2* __restrict__ data, const float2* __restrict__ sky,
-    const uint16_t* __restrict__ cell, const GalaxyParams* __restrict__ gals, const int* __restrict__ gidx,
-    int F, float2* __restrict__ partial) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [cell][lane]
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
-  const int nc = F * F;
-  ExtractTile& tile = reinterpret_cast<ExtractTile*>(smem_raw + ((extract_facet_bytes(F) + 15) & ~(size_t)15))[warp];
-  const int group = blockIdx.y;
-  for (int i = threadIdx.x; i < nc * 32; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
-  __syncthreads();
-  const int gi = gidx[group * 32 + lane];
-  GalF g;
-  if (gi >= 0) g = load_gal(gals[gi], nullptr, nullptr);
-  else { g = load_gal(gals[gidx[group * 32]], nullptr, nullptr); g.active = 0; }
-  float* my = reinterpret_cast<float*>(acc + lane);
-  const int nch = c_bnch;
-  // rows of this CTA, split into contiguous spans per warp
-  const long long per_cta = ((long long)n_rows + gridDim.x - 1) / gridDim.x;
-  const long long r_begin = blockIdx.x * per_cta;
-  const long long r_end = min((long long)n_rows, r_begin + per_cta);
-  const long long per_warp = (r_end - r_begin + nwarps - 1) / nwarps;
-  const long long w_begin = r_begin + warp * per_warp;
-  const long long w_end = min(r_end, w_begin + per_warp);
-  const int srow = lane & (kTileRows - 1);   // staging: row of this lane
-  const int shalf = lane >> 4;               // staging: channel half (8 channels)
-  for (long long r0 = w_begin; r0 < w_end; r0 += kTileRows) {
-    const int nr = (int)min((long long)kTileRows, w_end - r0);
-    const long long rs_row = r0 + srow;
-    const bool row_ok = srow < nr;
-    if (shalf == 0 && row_ok) tile.row[srow] = rows[rs_row];
-    const float q = row_ok ? rows[rs_row].q : 0.f;
-    for (int c0 = 0; c0 < nch; c0 += kChunk) {
-      // ---- stage kTileRows rows x kChunk channels
-#pragma unroll
-      for (int t = 0; t < kChunk / 2; ++t) {
-        const int k = shalf * (kChunk / 2) + t;
-        const int ch = c0 + k;
-        uint16_t c = kNoCell;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (row_ok && ch < nch) {
-          const size_t idx = (size_t)ch * n_rows + rs_row;
-          c = cell[idx];
-          const float2 d = data[idx], sk = sky[idx];
-          const BatchChan bc = c_bch[ch];
-          v = make_float4(d.x - sk.x, d.y - sk.y, bc.wn2 * q, bc.spec);
-        }
-        tile.v[k][srow] = v;
-        tile.cell[k][srow] = c;
-      }
-      __syncwarp();
-      if (shalf == 0) {
-        uint32_t valid = 0, start = 0;
-        uint16_t prev = kNoCell;
-#pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-          const uint16_t c = tile.cell[k][srow];
-          if (c != kNoCell) {
-            valid |= 1u << k;
-            if (c != prev) start |= 1u << k;
-          }
-          prev = c;
-        }
-        tile.mask[srow] = valid | (start << 16);
-      }
-      __syncwarp();
-      // ---- every lane (galaxy) walks the staged rows
-      for (int j = 0; j < nr; ++j) {
-        const uint32_t m = tile.mask[j];
-        if (m == 0) continue;
-        const RowF rw = tile.row[j];
-        const f2 p = delay_df(rw, g);
-        const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
-        const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
-        float ws, wc;
-        sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
-        const float wr = wc, wi = -ws;  // w = exp(-2 pi i dT)
-        float sr = 0.f, si = 0.f, rsum = 0.f;
-        if (m == kFullRun) {
-          // the common row: every channel of the chunk valid and in one cell
-#pragma unroll
-          for (int k = kChunk - 1; k >= 0; --k) {
-            const float4 v = tile.v[k][j];
-            const float nr_ = fmaf(sr, wr, fmaf(-si, wi, v.x));
-            const float ni_ = fmaf(sr, wi, fmaf(si, wr, v.y));
-            sr = nr_;
-            si = ni_;
-            const float x = g.sf0 * v.z;
-            const float sh = GAUSS ? __expf(-0.5f * x) : round_shape(x);
-            rsum = fmaf(sh, v.w, rsum);
-          }
-          float zs, zc;
-          const float ta = c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0);
-          sincospif(2.f * ta, &zs, &zc);
-          const float zr = zc, zi = -zs;
-          const float cr = fmaf(sr, zr, fmaf(-si, zi, rsum * g.flux));
-          const float ci = fmaf(sr, zi, si * zr);
-          if (g.active) {
-            const int c = tile.cell[0][j];
-            atomicAdd(my + (size_t)c * 64, cr);
-            atomicAdd(my + (size_t)c * 64 + 1, ci);
-          }
-          continue;
-        }
-        // Horner over each run, from its last channel down to its first: S = sum_k R_k w^(k - first)
-#pragma unroll
-        for (int k = kChunk - 1; k >= 0; --k) {
-          if (m & (1u << k)) {
-            const float4 v = tile.v[k][j];
-            const float nr_ = fmaf(sr, wr, fmaf(-si, wi, v.x));
-            const float ni_ = fmaf(sr, wi, fmaf(si, wr, v.y));
-            sr = nr_;
-            si = ni_;
-            const float x = g.sf0 * v.z;
-            const float sh = GAUSS ? __expf(-0.5f * x) : round_shape(x);
-            rsum = fmaf(sh, v.w, rsum);
-            if (m & (1u << (16 + k))) {
-              float zs, zc;
-              const float ta = (c0 + k == 0) ? (T0.hi + T0.lo) : turns_at(T0, dT, c0 + k);
-              sincospif(2.f * ta, &zs, &zc);
-              const float zr = zc, zi = -zs;  // exp(-2 pi i T(first channel))
-              const float cr = fmaf(sr, zr, fmaf(-si, zi, rsum * g.flux));
-              const float ci = fmaf(sr, zi, si * zr);
-              if (g.active) {
-                const int c = tile.cell[k][j];
-                atomicAdd(my + (size_t)c * 64, cr);
-                atomicAdd(my + (size_t)c * 64 + 1, ci);
-              }
-              sr = 0.f;
-              si = 0.f;
-              rsum = 0.f;
-            }
-          }
-        }
-      }
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  float2* out = partial + ((size_t)group * gridDim.x + blockIdx.x) * (size_t)nc * 32;
-  for (int i = threadIdx.x; i < nc * 32; i += blockDim.x) out[i] = acc[i];
+size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes) {
+  return align16((size_t)total_cells * sizeof(float2)) + align16((size_t)n_gal * sizeof(SeqGal)) +
+         (size_t)n_sizes * kSeqThreads * sizeof(uint32_t);
 }
 
-// partials of one group -> per-galaxy facet sums (FP64, fixed order), then the facet
-// finalisation of evaluate_uv_grid.c:196-209 / 113-133.  grid: one block per galaxy slot.
-__global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ partial, const int* __restrict__ gidx,
-                                 const double* __restrict__ ss, const double* __restrict__ sw, double len,
-                                 FacetOut out) {
-  const int group = blockIdx.y, lane = blockIdx.x;  // block = (lane, group)
-  const int slot = gidx[group * 32 + lane];        // galaxy index = facet slot
-  if (slot < 0) return;
+__global__ void k_cell_desc(int n_rows, int nch, const uint16_t* __restrict__ cell, uint32_t* __restrict__ desc) {
+  const int nchunk = (nch + kChunk - 1) / kChunk;
+  const long long total = (long long)n_rows * nchunk;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(t % n_rows);
+    const int c0 = (int)(t / n_rows) * kChunk;
+    const uint16_t c = cell[(size_t)c0 * n_rows + r];
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      const int ch = c0 + k;
+      if (ch >= nch || c == kNoCell || cell[(size_t)ch * n_rows + r] != c) mask |= 1u << k;
+    }
+    desc[t] = (uint32_t)c | (mask << 16);
+  }
+}
+
+int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, cudaStream_t st) {
+  const long long total = (long long)n_rows * ((n_ch + kChunk - 1) / kChunk);
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 8192);
+  k_cell_desc<<<blocks, 256, 0, st>>>(n_rows, n_ch, cell, desc);
+  return check("k_cell_desc");
+}
+
+// Work items (row, chunk) of a batch split into "simple" ones, one run of 16 valid channels for
+// every facet size of the batch (front of items, count in *n_simple), and the others (back), so
+// that the extraction runs each kind without divergence between the lanes of a warp.
+__global__ void k_classify_items(long long total, SeqBatch b, int* __restrict__ items, int* __restrict__ n_simple,
+                                 int* __restrict__ n_complex) {
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  // whole warps walk 32 consecutive items per step (the ballots below need every lane)
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < total; w += nwarps) {
+    const long long t = w * 32 + lane;
+    const bool live = t < total;
+    bool simple = live;
+    if (live)
+      for (int f = 0; f < b.n_sizes; ++f) simple = simple && (b.desc[f][t] >> 16) == 0;
+    const unsigned ms = __ballot_sync(0xffffffffu, simple);
+    const unsigned mc = __ballot_sync(0xffffffffu, live && !simple);
+    int s0 = 0, c0 = 0;
+    if (lane == 0) {
+      if (ms) s0 = atomicAdd(n_simple, __popc(ms));
+      if (mc) c0 = atomicAdd(n_complex, __popc(mc));
+    }
+    s0 = __shfl_sync(0xffffffffu, s0, 0);
+    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (simple) items[s0 + __popc(ms & below)] = (int)t;
+    else if (live) items[total - 1 - (c0 + __popc(mc & below))] = (int)t;
+  }
+}
+
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* counters, cudaStream_t st) {
+  const cudaError_t e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), st);
+  if (e != cudaSuccess) { fprintf(stderr, "rlf: classify: %s\n", cudaGetErrorString(e)); return (int)e; }
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
+  k_classify_items<<<blocks, 256, 0, st>>>(total, b, items, counters, counters + 1);
+  return check("k_classify_items");
+}
+
+__device__ __forceinline__ float profile(float x, int gauss) {
+  return gauss ? __expf(-0.5f * x) : round_shape(x);
+}
+
+// one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order
+template <int GAUSS, bool SIMPLE>
+__device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF* __restrict__ rows,
+                                         const float2* __restrict__ data, const float2* __restrict__ sky,
+                                         const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
+  const int tid = threadIdx.x;
+  const int r = t % n_rows;
+  const int c0 = (t / n_rows) * kChunk;
+  const int nk = min(kChunk, nch - c0);
+  const RowF rw = rows[r];
+  float pr[kChunk], pi[kChunk];
+#pragma unroll
+  for (int k = 0; k < kChunk; ++k) {
+    pr[k] = pi[k] = 0.f;
+    if (SIMPLE || k < nk) {
+      const size_t idx = (size_t)(c0 + k) * n_rows + r;
+      const float2 d = data[idx], s = sky[idx];
+      pr[k] = d.x - s.x;
+      pi[k] = d.y - s.y;
+    }
+  }
+  for (int f = 0; f < b.n_sizes; ++f) dcache[f * kSeqThreads + tid] = b.desc[f][t];
+  const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
+  // wn^2 (u^2 + v^2) of channel c0 + k
+#define XB(k) (c_bch[c0 + (k)].wn2 * rw.q)
+  for (int j = 0; j < b.n_gal; ++j) {
+    const SeqGal s = sg[j];
+    const GalF& g = s.g;
+    const f2 p = delay_df(rw, g);
+    const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
+    const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
+    float ws, wc, zs, zc;
+    sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
+    const float ta = c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0);
+    sincospif(2.f * ta, &zs, &zc);
+    const float wr = wc, wi = -ws;    // w = exp(-2 pi i dT)
+    const float zr0 = zc, zi0 = -zs;  // exp(-2 pi i T(c0))
+    const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
+    float2* fac = acc + s.off;
+    // fitted model: |k'|^2 = A u^2 + B uv + C v^2 (sheared), as a factor on wn^2 (u^2 + v^2)
+    const float k1q = g.A * uu + g.B * rw.uv + g.Cc * vv;
+    const float f1 = rw.q > 0.f ? g.sf1 * k1q / rw.q : 0.f;
+    if (SIMPLE) {
+      // one run: all 16 channels valid and in the cell d & 0xffff
+      float cr, ci;
+      if (!s.apply) {
+        float sr = 0.f, si = 0.f, rs = 0.f;
+#pragma unroll
+        for (int k = kChunk - 1; k >= 0; --k) {
+          const float nr_ = fmaf(sr, wr, fmaf(-si, wi, pr[k]));
+          const float ni_ = fmaf(sr, wi, fmaf(si, wr, pi[k]));
+          sr = nr_;
+          si = ni_;
+          rs = fmaf(profile(g.sf0 * XB(k), GAUSS), c_bch[c0 + k].spec, rs);
+        }
+        cr = fmaf(sr, zr0, fmaf(-si, zi0, rs * g.flux));
+        ci = fmaf(sr, zi0, si * zr0);
+      } else {
+        float ar = 0.f, ai = 0.f, rs = 0.f, zr = zr0, zi = zi0;
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+          ar = fmaf(pr[k], zr, fmaf(-pi[k], zi, ar));
+          ai = fmaf(pr[k], zi, fmaf(pi[k], zr, ai));
+          const float spec = c_bch[c0 + k].spec;
+          const float xbk = XB(k);
+          const float s0 = profile(g.sf0 * xbk, GAUSS);
+          const float s1 = profile(f1 * xbk, GAUSS);
+          rs = fmaf(s0, spec, rs);
+          const float a = g.flux * spec * (s1 - s0);
+          // residual -= a * exp(+2 pi i T)
+          pr[k] = fmaf(-a, zr, pr[k]);
+          pi[k] = fmaf(a, zi, pi[k]);
+          const float nzr = fmaf(zr, wr, -zi * wi);
+          const float nzi = fmaf(zr, wi, zi * wr);
+          zr = nzr;
+          zi = nzi;
+        }
+        cr = fmaf(rs, g.flux, ar);
+        ci = ai;
+      }
+      const int c = (int)(d & 0xffffu);
+      atomicAdd(&fac[c].x, cr);
+      atomicAdd(&fac[c].y, ci);
+    } else {
+      // flagged channels, several cells or a short chunk: channel by channel
+      const uint16_t* cl = b.cells[s.fidx];
+      const uint16_t cell0 = (uint16_t)(d & 0xffffu);
+      const uint32_t mask = d >> 16;
+      float zr = zr0, zi = zi0;
+#pragma unroll
+      for (int k = 0; k < kChunk; ++k) {
+        if (k < nk) {
+          const float spec = c_bch[c0 + k].spec;
+          const float xbk = XB(k);
+          const float s0 = profile(g.sf0 * xbk, GAUSS);
+          const uint16_t c = (mask & (1u << k)) ? cl[(size_t)(c0 + k) * n_rows + r] : cell0;
+          if (c != kNoCell) {
+            const float cr = fmaf(pr[k], zr, fmaf(-pi[k], zi, s0 * spec * g.flux));
+            const float ci = fmaf(pr[k], zi, pi[k] * zr);
+            atomicAdd(&fac[c].x, cr);
+            atomicAdd(&fac[c].y, ci);
+          }
+          if (s.apply) {
+            const float a = g.flux * spec * (profile(f1 * xbk, GAUSS) - s0);
+            pr[k] = fmaf(-a, zr, pr[k]);
+            pi[k] = fmaf(a, zi, pi[k]);
+          }
+          const float nzr = fmaf(zr, wr, -zi * wi);
+          const float nzi = fmaf(zr, wi, zi * wr);
+          zr = nzr;
+          zi = nzi;
+        }
+      }
+    }
+  }
+#undef XB
+}
+
+template <int GAUSS>
+__global__ void __launch_bounds__(kSeqThreads, 2) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
+                                                                const float2* __restrict__ data,
+                                                                const float2* __restrict__ sky, SeqBatch b,
+                                                                float2* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* acc = reinterpret_cast<float2*>(smem_raw);
+  SeqGal* sg = reinterpret_cast<SeqGal*>(smem_raw + align16((size_t)b.total_cells * sizeof(float2)));
+  uint32_t* dcache = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sg) +
+                                                 align16((size_t)b.n_gal * sizeof(SeqGal)));
+  const int tid = threadIdx.x;
+  for (int i = tid; i < b.total_cells; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+  for (int i = tid; i < b.n_gal; i += blockDim.x) {
+    SeqGal s;
+    const bool has_fit = b.fit != nullptr;
+    s.g = load_gal(b.gals[i], has_fit ? &b.fit[i].e1 : nullptr, has_fit ? &b.fit[i].error : nullptr);
+    s.fidx = b.fidx[i];
+    s.off = b.foff[i];
+    s.apply = has_fit && b.fit[i].error == 0;
+    sg[i] = s;
+  }
+  __syncthreads();
+  const int nch = c_bnch;
+  const long long total = (long long)n_rows * ((nch + kChunk - 1) / kChunk);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long first = blockIdx.x * (long long)blockDim.x + tid;
+  const long long ns = *b.n_simple;
+  for (long long q = first; q < ns; q += stride)
+    seq_item<GAUSS, true>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+  for (long long q = ns + first; q < total; q += stride)
+    seq_item<GAUSS, false>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+  __syncthreads();
+  float2* out = partial + (size_t)blockIdx.x * b.total_cells;
+  for (int i = tid; i < b.total_cells; i += blockDim.x) out[i] = acc[i];
+}
+
+int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
+                       int gaussian, int ctas, float2* partial, cudaStream_t st) {
+  if (b.n_gal < 1 || b.n_gal > kSeqMaxGal || b.n_sizes < 1 || b.n_sizes > kSeqMaxSizes) {
+    fprintf(stderr, "rlf: sequential extraction batch of %d galaxies / %d facet sizes unsupported\n", b.n_gal,
+            b.n_sizes);
+    return 1;
+  }
+  const size_t smem = seq_smem_bytes(b.n_gal, b.total_cells, b.n_sizes);
+  if (smem > 227 * 1024) { fprintf(stderr, "rlf: sequential extraction batch too large (%zu B)\n", smem); return 1; }
+  const void* kern = gaussian ? (const void*)k_extract_seq<1> : (const void*)k_extract_seq<0>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (gaussian) k_extract_seq<1><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+  else k_extract_seq<0><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+  return check("k_extract_seq");
+}
+
+// one block per galaxy of the batch: FP64 sums of the CTA partials, then the facet finalisation of
+// evaluate_uv_grid.c:196-209 / 113-133 with compaction to the non-empty cells in row-major order
+__global__ void k_finalize_seq(SeqBatch b, int ctas, const float2* __restrict__ partial,
+                               const double* const* __restrict__ ss_of, const double* const* __restrict__ sw_of,
+                               double len, FacetOut out) {
+  const int slot = blockIdx.x;
+  if (slot >= b.n_gal) return;
+  const int F = b.facet[slot], off = b.foff[slot];
   const int nc = F * F;
   const double inc = 2 * len / F;
+  const double* ss = ss_of[slot];
+  const double* sw = sw_of[slot];
   __shared__ int warp_tot[32];
   __shared__ int base;
   if (threadIdx.x == 0) base = 0;
   __syncthreads();
-  const int off = out.offset[slot];
-  for (int c0 = 0; c0 < nc; c0 += blockDim.x) {
-    const int c = c0 + threadIdx.x;
+  const int dst = out.offset[slot];
+  for (int cbase = 0; cbase < nc; cbase += blockDim.x) {
+    const int c = cbase + threadIdx.x;
     int flagc = 0;
     double vre = 0, vim = 0, sg = 0;
     if (c < nc) {
@@ -359,7 +461,7 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
       if (w != 0.0) {
         double sre = 0.0, sim = 0.0;
         for (int p = 0; p < ctas; ++p) {
-          const float2 v = partial[(((size_t)group * ctas + p) * nc + c) * 32 + lane];
+          const float2 v = partial[(size_t)p * b.total_cells + off + c];
           sre += (double)v.x;
           sim += (double)v.y;
         }
@@ -378,10 +480,10 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
     int before = base;
     for (int w = 0; w < wp; ++w) before += warp_tot[w];
     if (flagc) {
-      const int pos = off + before + inwarp;
-      const int i = c % F, j = c / F;
+      const int pos = dst + before + inwarp;
+      const int i = c % F, jj = c / F;
       // evaluate_uv_grid.c:125-126 without a fused multiply-add
-      const double gu = __dsub_rn(__dmul_rn(i + 0.5, inc), len), gv = __dsub_rn(__dmul_rn(j + 0.5, inc), len);
+      const double gu = __dsub_rn(__dmul_rn(i + 0.5, inc), len), gv = __dsub_rn(__dmul_rn(jj + 0.5, inc), len);
       if (out.as_float) {
         ((float*)out.gu)[pos] = (float)gu; ((float*)out.gv)[pos] = (float)gv;
         ((float*)out.dre)[pos] = (float)vre; ((float*)out.dim)[pos] = (float)vim;
@@ -403,31 +505,10 @@ __global__ void k_finalize_batch(int ctas, int F, const float2* __restrict__ par
   if (threadIdx.x == 0) out.ncoords[slot] = base;
 }
 
-int launch_extract_batch(int n_rows, const RowF* rows, const float2* data, const float2* sky, const uint16_t* cell,
-                         const GalaxyParams* gals, const int* gidx, int n_groups, int F, int ctas, int gaussian,
-                         float2* partial, cudaStream_t st) {
-  if (F < 1 || (unsigned)F > kBatchMaxFacet) { fprintf(stderr, "rlf: batched extraction facet %d unsupported\n", F); return 1; }
-  const size_t facet = (extract_facet_bytes(F) + 15) & ~(size_t)15;
-  // as many warps (each with its staging tile) as fit beside the facet, at most kBatchWarps
-  int warps = (int)((kBatchSmemMax - facet) / sizeof(ExtractTile));
-  if (warps > kBatchWarps) warps = kBatchWarps;
-  if (warps < 1) { fprintf(stderr, "rlf: batched extraction facet %d too large\n", F); return 1; }
-  const size_t smem = facet + (size_t)warps * sizeof(ExtractTile);
-  const void* kern = gaussian ? (const void*)k_extract_batch<1> : (const void*)k_extract_batch<0>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid(ctas, n_groups);
-  if (gaussian)
-    k_extract_batch<1><<<grid, warps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
-  else
-    k_extract_batch<0><<<grid, warps * 32, smem, st>>>(n_rows, rows, data, sky, cell, gals, gidx, F, partial);
-  return check("k_extract_batch");
-}
-
-int launch_finalize_batch(int n_groups, int ctas, int F, const float2* partial, const int* gidx, const double* ss,
-                          const double* sw, double len, FacetOut out, cudaStream_t st) {
-  dim3 grid(32, n_groups);
-  k_finalize_batch<<<grid, 256, 0, st>>>(ctas, F, partial, gidx, ss, sw, len, out);
-  return check("k_finalize_batch");
+int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, const double* const* ss,
+                        const double* const* sw, double len, FacetOut out, cudaStream_t st) {
+  k_finalize_seq<<<b.n_gal, 256, 0, st>>>(b, ctas, partial, ss, sw, len, out);
+  return check("k_finalize_seq");
 }
 
 // ---------------------------------------------------------------- removal

@@ -5,8 +5,6 @@
 
 namespace rlf {
 
-constexpr int kBatchWarps = 8;                    // warps per extraction CTA (32 galaxies each)
-constexpr size_t kBatchSmemMax = 227 * 1024;      // shared memory of one extraction CTA
 constexpr unsigned kBatchMaxFacet = 28;           // largest facet the batched extraction holds
 constexpr int kRemCh = 16;                        // channels per removal thread
 constexpr int kRemTile = 64;                      // galaxies staged per shared-memory tile
@@ -22,14 +20,45 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
                        cudaStream_t st);
 int launch_row_table(int n_rows, const double* uu, const double* vv, const double* ww, RowF* rows,
                      cudaStream_t st);
-// visibilities are channel-major [ch][row]; gidx[group*32 + lane] = galaxy/slot index or -1
-int launch_extract_batch(int n_rows, const RowF* rows, const float2* data, const float2* sky,
-                         const uint16_t* cell, const GalaxyParams* gals, const int* gidx,
-                         int n_groups, int F, int ctas, int gaussian, float2* partial,
-                         cudaStream_t st);
-int launch_finalize_batch(int n_groups, int ctas, int F, const float2* partial, const int* gidx,
-                          const double* ss, const double* sw, double len, FacetOut out,
-                          cudaStream_t st);
+// ---- sequential batch extraction (exact in-batch removal order)
+constexpr int kSeqThreads = 256;
+constexpr int kSeqMaxSizes = 16;                  // distinct facet sizes in one batch
+constexpr int kSeqMaxGal = 512;                   // galaxies in one batch
+constexpr size_t kSeqFacetBudget = 96 * 1024;     // shared facet accumulators of one batch, bytes
+
+// Run descriptor of one 16-channel chunk of one row for one facet size: the cell of the chunk's
+// first channel in bits 0-15, bit 16+k set when channel k of the chunk is flagged, beyond the last
+// channel or in another cell (so 0 in the high half = one run over all 16 channels).
+// desc: [chunk][row]; cell: [ch][row] (launch_cell_index).
+int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, cudaStream_t st);
+
+struct SeqBatch {
+  int n_gal;
+  const GalaxyParams* gals;   // [n_gal] in catalogue order
+  const FitOut* fit;          // [n_gal] fits of the previous round, whose model differences
+                              // (fitted - round) are removed from every later galaxy's facet; or
+                              // nullptr in the first round
+  const int* fidx;            // [n_gal] index of the galaxy's facet size in desc / cells
+  const int* foff;            // [n_gal] offset of the galaxy's facet in the batch's cell buffer
+  const int* facet;           // [n_gal] facet size
+  int total_cells;            // sum of facet^2 over the batch
+  int n_sizes;
+  const uint32_t* desc[kSeqMaxSizes];
+  const uint16_t* cells[kSeqMaxSizes];
+  const int* items;           // work items (row, 16-channel chunk) = chunk * n_rows + row: the
+  const int* n_simple;        // *n_simple single-run ones first, then the others
+};
+size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes);
+// split the batch's work items into single-run ones (front) and the others (back) for
+// launch_extract_seq; items: [n_rows * chunks], counters: [2] (simple, other)
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* counters, cudaStream_t st);
+// partial: [ctas][total_cells] float2
+int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
+                       int gaussian, int ctas, float2* partial, cudaStream_t st);
+// partial sums of every CTA -> facet of each galaxy (FP64 sums in CTA order), evaluate_uv_grid.c
+// finalisation and compaction into out (slot = galaxy index in the batch)
+int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, const double* const* ss,
+                        const double* const* sw, double len, FacetOut out, cudaStream_t st);
 int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
                         const GalaxyParams* gals, const FitOut* fit, int n_gal, int gaussian,
                         cudaStream_t st);

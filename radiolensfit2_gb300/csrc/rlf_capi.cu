@@ -11,6 +11,7 @@
 #include <signal.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <map>
 #include <vector>
 
@@ -107,7 +108,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -135,6 +136,7 @@ static int lib_stream(cudaStream_t* st) {
 struct FacetCache {
   DevBuf<uint16_t> cell;
   DevBuf<double> ss, sw;
+  DevBuf<uint32_t> desc;   // run descriptors of the sequential batch extraction (built on first use)
 };
 
 struct Timing {
@@ -160,6 +162,8 @@ struct rlf_observation {
   rlf::DevBuf<double> partial;
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
   rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
+  rlf::DevBuf<int> items;           // work items of the sequential batch extraction
+  rlf::DevBuf<int> item_count;      // [2] simple / other work items
   double max_delay_m = 0;
   int n_part = 0;
   double ms[4] = {0, 0, 0, 0};
@@ -257,10 +261,48 @@ static std::vector<GalaxyParams> make_gals(int n, const double* flux, const doub
 }
 
 // ------------------------------------------------------------------ pipeline
-// One pass of data_processing.c:61-138 over `order` (catalogue indices), `batch` galaxies at a
-// time: extraction + facet finalisation per galaxy, one persistent fit launch per batch, removal
-// per galaxy (skipped on the device for bad fits).  Everything is queued on one stream; the host
-// waits once at the end.  With batch = 1 the order of operations is the reference's.
+// CUDA-event intervals labelled extract / fit / remove, summed per label
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> label;  // label of the interval that ends at ev[i]
+  int mark(int lab, cudaStream_t st) {
+    cudaEvent_t e;
+    RLF_CUDA(cudaEventCreate(&e));
+    ev.push_back(e);
+    label.push_back(lab);
+    RLF_CUDA(cudaEventRecord(e, st));
+    return 0;
+  }
+  void sum(double* ms3) const {
+    for (size_t i = 1; i < ev.size(); ++i) {
+      float x = 0;
+      cudaEventElapsedTime(&x, ev[i - 1], ev[i]);
+      if (label[i] >= 0 && label[i] < 3) ms3[label[i]] += x;
+    }
+  }
+  ~PhaseTimer() { for (auto e : ev) cudaEventDestroy(e); }
+};
+enum { kPhaseExtract = 0, kPhaseFit = 1, kPhaseRemove = 2 };
+
+// galaxies whose fit differs between two rounds (ellipticity by more than tol, or the error flag)
+__global__ void k_count_changed(int n, const FitOut* a, const FitOut* b, double tol, unsigned long long* count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool changed = a[i].error != b[i].error || fabs(a[i].e1 - b[i].e1) > tol || fabs(a[i].e2 - b[i].e2) > tol;
+  if (changed) atomicAdd(count, 1ull);
+}
+
+// One pass of data_processing.c:61-138 over `order` (catalogue indices).
+//
+// batch = 1 (or F64 visibilities, or unevenly spaced channels): each galaxy is extracted, fitted
+// and removed before the next one, the reference's order.
+// batch > 1 with FP32 visibilities: the galaxies are taken in sub-batches of consecutive galaxies
+// (up to `batch`, and as many as the shared-memory facets of the sequential extraction hold).  Each
+// sub-batch runs `rounds` times sequential extraction (k_extract_seq: every facet with the previous
+// round's fitted models of the earlier galaxies of the sub-batch removed) + finalisation + one
+// persistent fit launch, then one removal pass with the final fits.  Galaxies whose facet is
+// larger than the batched kernels hold are processed one at a time at their place in the order.
+// Everything is queued on one stream; the host waits once at the end.
 static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, const std::vector<int>& order,
                     int numr, const double* ro, const rlf_options& opt, std::vector<FitOut>& out,
                     cudaStream_t st, double* ms3, double* facets_out = nullptr, int* ncoords_out = nullptr,
@@ -272,6 +314,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   const Precision prec = (ob->precision == RLF_F64) ? kF64 : kMixed;   // visibility passes
   const Precision fprec = (opt.fit_precision == RLF_MIXED) ? kMixed : kF64;  // the fit
   const int B = opt.batch > 0 ? opt.batch : 1;
+  const int rounds = facets_out ? 1 : (opt.rounds > 0 ? opt.rounds : 3);
   const Observation o = ob->view();
   unsigned fmax = 0;
   for (int i = 0; i < n; ++i) fmax = std::max<unsigned>(fmax, (unsigned)gals[order[i]].facet);
@@ -298,35 +341,83 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     ssp[i] = cache[i]->ss.p;
     swp[i] = cache[i]->sw.p;
   }
-  const int nb = std::min(B, n);
-  std::vector<int> slot_off(nb);
-  for (int k = 0; k < nb; ++k) slot_off[k] = k * max_cells;
+  // batched mode: FP32 visibilities, batch > 1, evenly spaced channels
+  bool batched = prec == kMixed && B > 1;
+  if (batched) {
+    const int bc = batch_set_channels(ob->n_ch, ob->wavenumbers.data(), ob->spec.data(), ob->max_delay_m, st);
+    if (bc < 0) batched = false;
+    else if (bc > 0) return bc;
+  }
+  // units of work in order: sub-batches [u0, u1) of the sequential extraction, or single galaxies
+  struct Unit { int b0, bn; bool seq; };
+  std::vector<Unit> units;
+  // per-galaxy index of the facet size and facet offset inside its sub-batch
+  std::vector<int> fidx(n, 0), foff(n, 0);
+  std::vector<std::vector<int>> unit_sizes;  // distinct facet sizes of each sequential unit
+  {
+    int i = 0;
+    while (i < n) {
+      if (!batched || (unsigned)facets[i] > kBatchMaxFacet) {
+        units.push_back({i, 1, false});
+        unit_sizes.push_back({});
+        ++i;
+        continue;
+      }
+      std::vector<int> sizes;
+      int cells = 0, j = i;
+      while (j < n && j - i < std::min(B, kSeqMaxGal) && (unsigned)facets[j] <= kBatchMaxFacet) {
+        const int F = facets[j];
+        const bool new_size = std::find(sizes.begin(), sizes.end(), F) == sizes.end();
+        if ((size_t)(cells + F * F) * sizeof(float2) > kSeqFacetBudget) break;
+        if (new_size && (int)sizes.size() == kSeqMaxSizes) break;
+        if (new_size) sizes.push_back(F);
+        fidx[j] = (int)(std::find(sizes.begin(), sizes.end(), F) - sizes.begin());
+        foff[j] = cells;
+        cells += F * F;
+        ++j;
+      }
+      units.push_back({i, j - i, true});
+      unit_sizes.push_back(sizes);
+      i = j;
+    }
+  }
+  // slots of the facet cell buffer: every galaxy of a unit needs its own
+  int max_unit = 1;
+  for (const Unit& u : units) max_unit = std::max(max_unit, u.bn);
+  std::vector<int> slot_off(max_unit);
+  for (int k = 0; k < max_unit; ++k) slot_off[k] = k * max_cells;
   DevBuf<GalaxyParams> dg;
   DevBuf<double> dprior, dstart;
-  DevBuf<int> dfac, doff, dnc, dqueue;
+  DevBuf<int> doff, dnc, dqueue, dfidx, dfoff, dfac;
   DevBuf<const double*> dss, dsw;
-  DevBuf<FitOut> dout;
+  DevBuf<FitOut> dout, dprev;
+  DevBuf<unsigned long long> dchanged;
   RLF_OK(dg.upload(hg.data(), n, st));
   RLF_OK(dprior.upload(rprior.data(), rprior.size(), st));
-  RLF_OK(dfac.upload(facets.data(), n, st));
   RLF_OK(dss.upload(ssp.data(), n, st));
   RLF_OK(dsw.upload(swp.data(), n, st));
-  RLF_OK(doff.upload(slot_off.data(), nb, st));
+  RLF_OK(doff.upload(slot_off.data(), max_unit, st));
+  RLF_OK(dfidx.upload(fidx.data(), n, st));
+  RLF_OK(dfoff.upload(foff.data(), n, st));
+  RLF_OK(dfac.upload(facets.data(), n, st));
   if (opt.start) {
     std::vector<double> sv((size_t)3 * n);
     for (int i = 0; i < n; ++i)
       for (int k = 0; k < 3; ++k) sv[3 * i + k] = opt.start[3 * order[i] + k];
     RLF_OK(dstart.upload(sv.data(), sv.size(), st));
   }
-  const int nbatches = (n + B - 1) / B;
   RLF_OK(dout.ensure(n));
   RLF_CUDA(cudaMemsetAsync(dout.p, 0, n * sizeof(FitOut), st));
   RLF_OK(dnc.ensure(n));
-  RLF_OK(dqueue.ensure(nbatches));
-  RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, nbatches * sizeof(int), st));
+  RLF_OK(dqueue.ensure(1));
+  if (batched && rounds > 1) {
+    RLF_OK(dprev.ensure(std::min(n, max_unit)));
+    RLF_OK(dchanged.ensure(1));
+    RLF_CUDA(cudaMemsetAsync(dchanged.p, 0, sizeof(unsigned long long), st));
+  }
   const size_t esz = fprec == kF64 ? sizeof(double) : sizeof(float);
   DevBuf<unsigned char> cells;
-  const size_t plane = (size_t)nb * max_cells * esz;
+  const size_t plane = (size_t)max_unit * max_cells * esz;
   RLF_OK(cells.ensure(5 * plane));
   void* gu = cells.p;
   void* gv = cells.p + plane;
@@ -334,87 +425,109 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   void* dim = cells.p + 3 * plane;
   void* sg = cells.p + 4 * plane;
   RLF_OK(ob->partial.ensure((size_t)ob->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
-  std::vector<cudaEvent_t> ev((size_t)nbatches * 3 + 1);
-  for (auto& e : ev) RLF_CUDA(cudaEventCreate(&e));
   const int grid_fit = fit_max_grid(fprec);
-  // batched extraction/removal: mixed precision, batch > 1, evenly spaced channels
-  bool batched = prec == kMixed && B > 1;
-  if (batched) {
-    const int bc = batch_set_channels(ob->n_ch, ob->wavenumbers.data(), ob->spec.data(), ob->max_delay_m, st);
-    if (bc < 0) batched = false;
-    else if (bc > 0) return bc;
-  }
+  int sms = 0, dev = 0;
+  RLF_CUDA(cudaGetDevice(&dev));
+  RLF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int seq_ctas = 2 * sms;
   if (batched && !ob->rows.p) {
     RLF_OK(ob->rows.ensure(ob->n_rows));
     RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
   }
-  const int ctas_per_group = std::max(1, std::min(1024, (ob->n_rows + 4095) / 4096));
-  DevBuf<int> dgidx;
-  RLF_CUDA(cudaEventRecord(ev[0], st));
-  for (int bi = 0; bi < nbatches; ++bi) {
-    const int b0 = bi * B;
-    const int bn = std::min(B, n - b0);
+  PhaseTimer pt;
+  RLF_OK(pt.mark(-1, st));
+  for (size_t ui = 0; ui < units.size(); ++ui) {
+    const Unit& u = units[ui];
+    const int b0 = u.b0, bn = u.bn;
     FacetOut fo;
     fo.offset = doff.p;
     fo.ncoords = dnc.p + b0;
     fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
     fo.as_float = fprec == kMixed;
-    std::vector<int> single;  // galaxies extracted one at a time
-    if (batched) {
-      // group the batch by facet size, 32 galaxies per warp-group
-      std::map<int, std::vector<int>> byF;
-      for (int k = 0; k < bn; ++k) {
-        const int F = facets[b0 + k];
-        if ((unsigned)F <= kBatchMaxFacet) byF[F].push_back(k);
-        else single.push_back(k);
-      }
-      std::vector<int> hgidx;
-      std::vector<std::pair<int, std::pair<int, int>>> launches;  // F -> (first group, n_groups)
-      for (auto& kv : byF) {
-        const int ng = ((int)kv.second.size() + 31) / 32;
-        launches.push_back({kv.first, {(int)hgidx.size() / 32, ng}});
-        for (int j = 0; j < ng * 32; ++j) hgidx.push_back(j < (int)kv.second.size() ? kv.second[j] : -1);
-      }
-      if (!hgidx.empty()) {
-        RLF_OK(dgidx.upload(hgidx.data(), hgidx.size(), st));
-        size_t need = 0;
-        for (auto& L : launches) need = std::max(need, (size_t)L.second.second * ctas_per_group * L.first * L.first * 32);
-        RLF_OK(ob->bpartial.ensure(need));
-        for (auto& L : launches) {
-          const int F = L.first, g0 = L.second.first, ng = L.second.second;
-          FacetCache* fcF = nullptr;
-          RLF_OK(obs_facet(ob, (unsigned)F, &fcF, st));
-          ob->stats[RLF_STAT_EXTRACT_GROUPS] += ng;
-          RLF_OK(launch_extract_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, fcF->cell.p, dg.p + b0,
-                                      dgidx.p + (size_t)g0 * 32, ng, F, ctas_per_group, opt.gaussian, ob->bpartial.p,
-                                      st));
-          RLF_OK(launch_finalize_batch(ng, ctas_per_group, F, ob->bpartial.p, dgidx.p + (size_t)g0 * 32, fcF->ss.p,
-                                       fcF->sw.p, ob->len, fo, st));
+    FacetBatch fb;
+    fb.n_gal = bn;
+    fb.max_cells = max_cells;
+    fb.offset = doff.p;
+    fb.count = dnc.p + b0;
+    fb.gu = gu; fb.gv = gv; fb.dre = dre; fb.dim = dim; fb.sig2 = sg;
+    fb.rprior = dprior.p + (size_t)b0 * kMaxNodes;
+    fb.start = opt.start ? dstart.p + (size_t)3 * b0 : nullptr;
+    fb.active = nullptr;
+    fb.out = dout.p + b0;
+    fb.queue = dqueue.p;
+    fb.trace = nullptr;
+    fb.trace_cap = 0;
+    SeqBatch sb{};
+    if (u.seq) {
+      sb.n_gal = bn;
+      sb.gals = dg.p + b0;
+      sb.fidx = dfidx.p + b0;
+      sb.foff = dfoff.p + b0;
+      sb.facet = dfac.p + b0;
+      sb.total_cells = 0;
+      for (int k = b0; k < b0 + bn; ++k) sb.total_cells += facets[k] * facets[k];
+      sb.n_sizes = (int)unit_sizes[ui].size();
+      for (int f = 0; f < sb.n_sizes; ++f) {
+        FacetCache* fcF = nullptr;
+        RLF_OK(obs_facet(ob, (unsigned)unit_sizes[ui][f], &fcF, st));
+        if (!fcF->desc.p) {
+          RLF_OK(fcF->desc.ensure((size_t)ob->n_rows * ((ob->n_ch + 15) / 16)));
+          RLF_OK(launch_cell_desc(ob->n_rows, ob->n_ch, fcF->cell.p, fcF->desc.p, st));
         }
+        sb.desc[f] = fcF->desc.p;
+        sb.cells[f] = fcF->cell.p;
       }
-    } else {
-      for (int k = 0; k < bn; ++k) single.push_back(k);
+      RLF_OK(ob->bpartial.ensure((size_t)seq_ctas * sb.total_cells));
+      const long long n_items = (long long)ob->n_rows * ((ob->n_ch + 15) / 16);
+      if (n_items > 0x7fffffffLL) { fprintf(stderr, "rlf: %lld row-chunks exceed the batched extraction\n", n_items); return 1; }
+      RLF_OK(ob->items.ensure((size_t)n_items));
+      RLF_OK(ob->item_count.ensure(2));
+      sb.items = ob->items.p;
+      sb.n_simple = ob->item_count.p;
+      RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->item_count.p, st));
     }
-    ob->stats[RLF_STAT_EXTRACT_SINGLE] += (long long)single.size();
-    for (int k : single) {
-      const int i = b0 + k;
-      const unsigned F = (unsigned)facets[i];
-      if (prec == kF64)
-        RLF_OK(launch_extract_f64(o, ob->data64.p, ob->sky64.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
-                                  ob->partial.p, ob->n_part, st));
-      else
-        RLF_OK(launch_extract_mixed(o, ob->data32.p, ob->sky32.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
+    const int nr = u.seq ? rounds : 1;
+    for (int rd = 0; rd < nr; ++rd) {
+      // ---- extraction
+      if (u.seq) {
+        sb.fit = rd == 0 ? nullptr : dout.p + b0;
+        ob->stats[RLF_STAT_EXTRACT_PASSES] += 1;
+        ob->stats[RLF_STAT_EXTRACT_GAL] += bn;
+        if (rd == 0) ob->stats[RLF_STAT_EXTRACT_GAL_FIRST] += bn;
+        RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sb, opt.gaussian, seq_ctas,
+                                  ob->bpartial.p, st));
+        RLF_OK(launch_finalize_seq(sb, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, ob->len, fo, st));
+      } else {
+        const int i = b0;
+        const unsigned F = (unsigned)facets[i];
+        ob->stats[RLF_STAT_EXTRACT_SINGLE] += 1;
+        if (prec == kF64)
+          RLF_OK(launch_extract_f64(o, ob->data64.p, ob->sky64.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
                                     ob->partial.p, ob->n_part, st));
-      FacetOut f1 = fo;
-      f1.offset = doff.p + k;
-      f1.ncoords = dnc.p + i;
-      double* sums = ob->partial.p + (size_t)ob->n_part * 2 * F * F;
-      RLF_OK(launch_reduce_partials(ob->partial.p, ob->n_part, 2 * F * F, sums, st));
-      RLF_OK(launch_facet_finalize(1, dfac.p + i, sums, 1, 0, dss.p + i, dsw.p + i, ob->len, f1, st));
+        else
+          RLF_OK(launch_extract_mixed(o, ob->data32.p, ob->sky32.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
+                                      ob->partial.p, ob->n_part, st));
+        double* sums = ob->partial.p + (size_t)ob->n_part * 2 * F * F;
+        RLF_OK(launch_reduce_partials(ob->partial.p, ob->n_part, 2 * F * F, sums, st));
+        RLF_OK(launch_facet_finalize(1, dfac.p + i, sums, 1, 0, dss.p + i, dsw.p + i, ob->len, fo, st));
+      }
+      RLF_OK(pt.mark(kPhaseExtract, st));
+      if (facets_out) break;
+      // ---- fit
+      if (u.seq && rd == nr - 1 && nr > 1)
+        RLF_CUDA(cudaMemcpyAsync(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
+      RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
+      ob->stats[RLF_STAT_FITTED] += bn;
+      RLF_OK(fit_launch(fb, fprec, std::min(grid_fit, bn), st));
+      if (u.seq && rd == nr - 1 && nr > 1) {
+        k_count_changed<<<(bn + 127) / 128, 128, 0, st>>>(bn, dprev.p, dout.p + b0, 1e-9, dchanged.p);
+        count_launch();
+        RLF_CUDA(cudaGetLastError());
+      }
+      RLF_OK(pt.mark(kPhaseFit, st));
     }
-    RLF_CUDA(cudaEventRecord(ev[3 * bi + 1], st));
     if (facets_out) {
-      // extraction only: hand the packed facets of this batch back as doubles
+      // extraction only: hand the packed facets of this unit back as doubles
       std::vector<int> nc(bn);
       RLF_CUDA(cudaMemcpyAsync(nc.data(), dnc.p + b0, bn * sizeof(int), cudaMemcpyDeviceToHost, st));
       std::vector<unsigned char> h(5 * plane);
@@ -430,56 +543,31 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
             facets_out[((size_t)(b0 + k) * 5 + a) * facets_stride + c] = v;
           }
       }
-      RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
-      RLF_CUDA(cudaEventRecord(ev[3 * bi + 3], st));
       continue;
     }
-    FacetBatch fb;
-    fb.n_gal = bn;
-    fb.max_cells = max_cells;
-    fb.offset = doff.p;
-    fb.count = dnc.p + b0;
-    fb.gu = gu; fb.gv = gv; fb.dre = dre; fb.dim = dim; fb.sig2 = sg;
-    fb.rprior = dprior.p + (size_t)b0 * kMaxNodes;
-    fb.start = opt.start ? dstart.p + (size_t)3 * b0 : nullptr;
-    fb.active = nullptr;
-    fb.out = dout.p + b0;
-    fb.queue = dqueue.p + bi;
-    fb.trace = nullptr;
-    fb.trace_cap = 0;
-    RLF_OK(fit_launch(fb, fprec, std::min(grid_fit, bn), st));
-    RLF_CUDA(cudaEventRecord(ev[3 * bi + 2], st));
-    ob->stats[RLF_STAT_FITTED] += bn;
-    if (batched) {
+    // ---- removal with the final fits
+    if (u.seq) {
       ob->stats[RLF_STAT_REMOVE_BATCHES] += 1;
       RLF_OK(launch_remove_batch(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, dg.p + b0, dout.p + b0, bn,
                                  opt.gaussian, st));
     } else {
-      ob->stats[RLF_STAT_REMOVE_SINGLE] += bn;
-      for (int k = 0; k < bn; ++k) {
-        const int i = b0 + k;
-        const double* e12 = &dout.p[i].e1;
-        const int* err = &dout.p[i].error;
-        if (prec == kF64)
-          RLF_OK(launch_remove_f64(o, ob->data64.p, ob->sky64.p, dg.p + i, e12, err, opt.gaussian, st));
-        else
-          RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
-      }
+      ob->stats[RLF_STAT_REMOVE_SINGLE] += 1;
+      const int i = b0;
+      const double* e12 = &dout.p[i].e1;
+      const int* err = &dout.p[i].error;
+      if (prec == kF64)
+        RLF_OK(launch_remove_f64(o, ob->data64.p, ob->sky64.p, dg.p + i, e12, err, opt.gaussian, st));
+      else
+        RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
     }
-    RLF_CUDA(cudaEventRecord(ev[3 * bi + 3], st));
+    RLF_OK(pt.mark(kPhaseRemove, st));
   }
-  RLF_OK(dout.download(out.data(), n, st));
+  if (!facets_out) RLF_OK(dout.download(out.data(), n, st));
+  unsigned long long changed = 0;
+  if (dchanged.p) RLF_CUDA(cudaMemcpyAsync(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
-  double t[3] = {0, 0, 0};
-  for (int bi = 0; bi < nbatches; ++bi) {
-    for (int k = 0; k < 3; ++k) {
-      float x = 0;
-      cudaEventElapsedTime(&x, ev[3 * bi + k], ev[3 * bi + k + 1]);
-      t[k] += x;
-    }
-  }
-  for (auto& e : ev) cudaEventDestroy(e);
-  if (ms3) for (int k = 0; k < 3; ++k) ms3[k] += t[k];
+  ob->stats[RLF_STAT_CHANGED] += (long long)changed;
+  if (ms3) pt.sum(ms3);
   return 0;
 }
 

@@ -108,7 +108,7 @@ class DeviceObservation:
         self._check(self.lib.rlf_obs_restore(self.h), "rlf_obs_restore")
 
     def process(self, cat: Catalogue, *, batch: int = 1, refit: bool = True, gaussian: int = 0,
-                start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64) -> ProcessResult:
+                start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64, rounds: int = 0) -> ProcessResult:
         ro, pro = _d(K.ro_grid())
         arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
         opt = _lib.Options()
@@ -118,6 +118,7 @@ class DeviceObservation:
         opt.refit = 1 if refit else 0
         opt.verbose = verbose
         opt.fit_precision = int(fit_precision)
+        opt.rounds = int(rounds)
         st = None
         if start is not None:
             st = np.ascontiguousarray(start, dtype=np.float64).reshape(-1)
@@ -131,8 +132,8 @@ class DeviceObservation:
         self.lib.rlf_obs_last_timing(self.h, ms)
         sv = (C.c_longlong * 8)()
         self.lib.rlf_obs_last_stats(self.h, sv)
-        stats = dict(zip(("extract_groups", "extract_single", "remove_batches", "remove_single", "fitted"),
-                         (int(x) for x in sv[:5])))
+        stats = dict(zip(("extract_passes", "extract_single", "remove_batches", "remove_single", "fitted",
+                          "extract_gal", "changed", "extract_gal_first"), (int(x) for x in sv[:8])))
         return ProcessResult(res, nbad.value, tuple(ms), stats)
 
     def extract(self, cat: Catalogue, *, batch: int = 1):

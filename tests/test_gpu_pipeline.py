@@ -72,12 +72,15 @@ def test_pipeline_modes(orc, case, sky):
     L_ref = np.array([r[5] for r in ref])
     err_ref = np.array([r[6] for r in ref])
     out = {}
-    modes = (("f64", _lib.RLF_F64, _lib.RLF_F64, 1), ("mixed", _lib.RLF_MIXED, _lib.RLF_F64, 1),
-             ("mixed-fit", _lib.RLF_MIXED, _lib.RLF_MIXED, 1))
-    for name, prec, fprec, batch in modes:
+    modes = (("f64", _lib.RLF_F64, _lib.RLF_F64, 1, 0), ("mixed", _lib.RLF_MIXED, _lib.RLF_F64, 1, 0),
+             ("mixed-fit", _lib.RLF_MIXED, _lib.RLF_MIXED, 1, 0), ("batched", _lib.RLF_MIXED, _lib.RLF_F64, 16, 3),
+             ("batched-1round", _lib.RLF_MIXED, _lib.RLF_F64, 16, 1))
+    changed = {}
+    for name, prec, fprec, batch, rounds in modes:
         dev = _dev(case, sky, prec)
-        pr = dev.process(case.cat, batch=batch, refit=False, fit_precision=fprec)
+        pr = dev.process(case.cat, batch=batch, refit=False, fit_precision=fprec, rounds=rounds)
         out[name] = pr.results
+        changed[name] = pr.stats["changed"]
         dev.close()
     f = out["f64"]
     assert np.array_equal(f["error"], err_ref)
@@ -89,14 +92,14 @@ def test_pipeline_modes(orc, case, sky):
     assert np.max(np.abs(f["e2"][good] - e_ref[good, 1])) < 1e-7
     assert np.allclose(f["maxL"][good], L_ref[good], rtol=1e-9)
     stats = {}
-    for name in ("mixed", "mixed-fit"):
+    for name in ("mixed", "mixed-fit", "batched", "batched-1round"):
         r = out[name]
         ok = good & (r["error"] == 0)
         de = np.maximum(np.abs(r["e1"][ok] - e_ref[ok, 0]), np.abs(r["e2"][ok] - e_ref[ok, 1]))
         dL = np.abs(r["maxL"][ok] - L_ref[ok]) / np.abs(L_ref[ok])
         stats[name] = (de, dL, int(np.sum(r["error"] != err_ref)))
         print(f"{name}: |de| max {de.max():.2e} median {np.median(de):.2e}; |dL/L| max {dL.max():.2e}; "
-              f"errors {int(r['error'].sum())} vs {int(err_ref.sum())}")
+              f"errors {int(r['error'].sum())} vs {int(err_ref.sum())}; changed in last round {changed[name]}")
     de, dL, nerr = stats["mixed"]
     assert nerr == 0
     assert de.max() < 1e-4 and dL.max() < 1e-6
