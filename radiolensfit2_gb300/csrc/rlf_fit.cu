@@ -26,12 +26,23 @@
 
 namespace rlf {
 
-constexpr int kFitWarps = 24;
+#ifndef RLF_FIT_WARPS
+#define RLF_FIT_WARPS 24
+#endif
+// warps of a fit CTA (one galaxy); the scalelength nodes are spread over them, and small CTAs run
+// several galaxies per SM
+constexpr int kFitWarps = RLF_FIT_WARPS;
 constexpr int kFitThreads = kFitWarps * 32;
+constexpr int kFitMinBlocks = kFitWarps <= 7 ? 3 : (kFitWarps <= 12 ? 2 : 1);
 constexpr int kQagCap = 256;       // intervals held by the device QAG
 constexpr int kNewtonMax = 50;     // likelihood.c:290
 constexpr int kSimplexMax = 50;    // galaxy_fitting.c:80
 constexpr int kModelCache = 4;     // facet cells per lane whose model stays in registers
+constexpr int kNodePart = 8;       // partials per cross-correlation sum left by a node's warp
+constexpr int kNodeCache = 64;     // facet cells per node whose model stays in shared memory
+constexpr int kEiTerms = 512;      // reciprocal table of the per-lane Ei series
+
+__constant__ double c_invk[kEiTerms];  // 1 / k
 
 struct FitConst {
   int numr;
@@ -105,7 +116,7 @@ __device__ __forceinline__ double s_exp(double x) { return exp(x); }
 __device__ __forceinline__ float s_exp(float x) { return expf(x); }
 __device__ __forceinline__ double s_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float s_abs(float x) { return fabsf(x); }
-__device__ __forceinline__ double s_pow15(double x) { return pow(x, 1.5); }
+__device__ __forceinline__ double s_pow15(double x) { return x * sqrt(x); }
 __device__ __forceinline__ float s_pow15(float x) { return x * sqrtf(x); }
 __device__ __forceinline__ void s_sincos(double a, double* s, double* c) { sincos(a, s, c); }
 __device__ __forceinline__ void s_sincos(float a, float* s, float* c) { sincosf(a, s, c); }
@@ -381,6 +392,17 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
 // ------------------------------------------------------------- shared state
 template <class S>
 struct FitShared {
+  // phased node evaluation (eval_nodes): per-node partial sums, state and model cache
+  double part[7][kMaxNodes][kNodePart];  // 0: model norm; 1..6: val, dx, dy, d2x, d2y, dxy
+  double mcache[kMaxNodes][kNodeCache];   // model of the first kNodeCache cells of each node
+  double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
+  double nnorm[kMaxNodes];                // the node's model normalisation (F64: norm, mixed: 1/norm)
+  int nactive[kMaxNodes];                 // node has a pass pending
+  int nany;
+  // natural spline rows and the factorisation of its matrix for the abscissae fac_x[0..fac_n)
+  S soff[kMaxNodes], sdiag[kMaxNodes], sg[kMaxNodes], sz[kMaxNodes], salpha[kMaxNodes], sgamma[kMaxNodes];
+  S fac_x[kMaxNodes];
+  int fac_n;
   S Lr[kMaxNodes];
   S rprior[kMaxNodes];
   S xs[kMaxNodes], ys[kMaxNodes], cs[kMaxNodes];
@@ -551,50 +573,75 @@ __device__ __noinline__ int qag_warp(FitShared<S>& sh, int n, bool cubic, S a, S
 template <class S>
 __device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
   const int lane = threadIdx.x & 31;
-  S ymax = S(-10.0);
-  int ymaxpos = 0;
-  for (int ii = 0; ii < n; ii++)
-    if (sh.ys[ii] > ymax) { ymax = sh.ys[ii]; ymaxpos = ii; }
-  S xmin, xmax;
-  xmin = xmax = sh.xs[ymaxpos];
-  if (ymaxpos < n - 1) xmax = sh.xs[ymaxpos + 1];
-  if (ymaxpos > 0) xmin = sh.xs[ymaxpos - 1];
-  for (int ii = 0; ii < n; ii++) {
-    if (sh.xs[ii] < xmin) xmin = sh.xs[ii];
-    if (sh.xs[ii] > xmax) xmax = sh.xs[ii];
+  const bool in = lane < n;
+  const S y_l = in ? sh.ys[lane] : S(0);
+  const S x_l = in ? sh.xs[lane] : S(0);
+  // ymax: the first maximum above -10 (strict comparison from ymax = -10, marginalise_r.c:90-96)
+  S ymax = (in && y_l > S(-10.0)) ? y_l : S(-10.0);
+  int ypos = (in && y_l > S(-10.0)) ? lane : 0x7fffffff;
+  // xmin, xmax: the node range (it contains the maximum's neighbours, marginalise_r.c:97-106)
+  S xmin = in ? x_l : S(1e300), xmax = in ? x_l : S(-1e300);
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    const S oy = __shfl_xor_sync(0xffffffffu, ymax, m);
+    const int op = __shfl_xor_sync(0xffffffffu, ypos, m);
+    if (oy > ymax || (oy == ymax && op < ypos)) { ymax = oy; ypos = op; }
+    xmin = fmin(xmin, __shfl_xor_sync(0xffffffffu, xmin, m));
+    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, m));
   }
+  if (in) { sh.ys[lane] = y_l - ymax; sh.cs[lane] = S(0); }
+  // natural cubic spline: c_0 = c_{n-1} = 0, interior from the symmetric tridiagonal system
+  // solved by LDL^T (as gsl_interp_cspline).  The lanes form the rows; the factorisation
+  // (alpha, gamma) depends only on the abscissae and is kept while they do not change.
+  const int m = n - 2;
   __syncwarp();
-  if (lane == 0) {
-    for (int ii = 0; ii < n; ii++) sh.ys[ii] -= ymax;
-    // natural cubic spline: c_0 = c_{n-1} = 0, interior from the symmetric tridiagonal
-    // system solved by LDL^T (as gsl_interp_cspline)
-    for (int ii = 0; ii < n; ii++) sh.cs[ii] = S(0);
-    const int m = n - 2;
-    S alpha[kMaxNodes], gamma[kMaxNodes], z[kMaxNodes], diag[kMaxNodes], off[kMaxNodes], g[kMaxNodes];
-    for (int i = 0; i < m; i++) {
-      const S h_i = sh.xs[i + 1] - sh.xs[i], h_ip1 = sh.xs[i + 2] - sh.xs[i + 1];
-      const S dy_i = sh.ys[i + 1] - sh.ys[i], dy_ip1 = sh.ys[i + 2] - sh.ys[i + 1];
-      const S g_i = (h_i != S(0)) ? S(1) / h_i : S(0);
-      const S g_ip1 = (h_ip1 != S(0)) ? S(1) / h_ip1 : S(0);
-      off[i] = h_ip1;
-      diag[i] = S(2) * (h_ip1 + h_i);
-      g[i] = S(3) * (dy_ip1 * g_ip1 - dy_i * g_i);
-    }
-    if (m == 1) {
-      sh.cs[1] = g[0] / diag[0];
-    } else if (m > 1) {
-      alpha[0] = diag[0];
-      gamma[0] = off[0] / alpha[0];
-      for (int i = 1; i < m - 1; i++) {
-        alpha[i] = diag[i] - off[i - 1] * gamma[i - 1];
-        gamma[i] = off[i] / alpha[i];
+  if (lane < m) {
+    const int i = lane;
+    const S h_i = sh.xs[i + 1] - sh.xs[i], h_ip1 = sh.xs[i + 2] - sh.xs[i + 1];
+    const S dy_i = sh.ys[i + 1] - sh.ys[i], dy_ip1 = sh.ys[i + 2] - sh.ys[i + 1];
+    const S g_i = (h_i != S(0)) ? S(1) / h_i : S(0);
+    const S g_ip1 = (h_ip1 != S(0)) ? S(1) / h_ip1 : S(0);
+    sh.soff[i] = h_ip1;
+    sh.sdiag[i] = S(2) * (h_ip1 + h_i);
+    sh.sg[i] = S(3) * (dy_ip1 * g_ip1 - dy_i * g_i);
+  }
+  const bool same = __all_sync(0xffffffffu, !in || sh.fac_x[lane] == x_l) && sh.fac_n == n;
+  __syncwarp();
+  if (m == 1) {
+    if (lane == 0) sh.cs[1] = sh.sg[0] / sh.sdiag[0];
+  } else if (m > 1) {
+    if (!same) {
+      if (lane == 0) {
+        sh.salpha[0] = sh.sdiag[0];
+        sh.sgamma[0] = sh.soff[0] / sh.salpha[0];
+        for (int i = 1; i < m - 1; i++) {
+          sh.salpha[i] = sh.sdiag[i] - sh.soff[i - 1] * sh.sgamma[i - 1];
+          sh.sgamma[i] = sh.soff[i] / sh.salpha[i];
+        }
+        sh.salpha[m - 1] = sh.sdiag[m - 1] - sh.soff[m - 2] * sh.sgamma[m - 2];
+        sh.fac_n = n;
       }
-      alpha[m - 1] = diag[m - 1] - off[m - 2] * gamma[m - 2];
-      z[0] = g[0];
-      for (int i = 1; i < m; i++) z[i] = g[i] - gamma[i - 1] * z[i - 1];
-      for (int i = 0; i < m; i++) z[i] = z[i] / alpha[i];
-      sh.cs[m] = z[m - 1];
-      for (int k = m - 1; k-- > 0;) sh.cs[k + 1] = z[k] - gamma[k] * sh.cs[k + 2];
+      if (in) sh.fac_x[lane] = x_l;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      S z = sh.sg[0];
+      sh.sz[0] = z;
+      for (int i = 1; i < m; i++) {
+        z = sh.sg[i] - sh.sgamma[i - 1] * z;
+        sh.sz[i] = z;
+      }
+    }
+    __syncwarp();
+    if (lane < m) sh.sz[lane] = sh.sz[lane] / sh.salpha[lane];
+    __syncwarp();
+    if (lane == 0) {
+      S c = sh.sz[m - 1];
+      sh.cs[m] = c;
+      for (int k = m - 1; k-- > 0;) {
+        c = sh.sz[k] - sh.sgamma[k] * c;
+        sh.cs[k + 1] = c;
+      }
     }
   }
   __syncwarp();
@@ -604,6 +651,314 @@ __device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
   if (status) status = qag_warp<S>(sh, n, false, xmin, xmax, &sump);
   if (status) return S(kBad);
   return s_log(sump) + ymax;
+}
+
+// ------------------------------------------------------------ phased nodes
+// Ei(x1) and Ei(x2), x > 0, evaluated by one lane (each lane its own x): for each argument the
+// power series gamma + ln x + sum_k x^k / (k k!) when x <= 40, else the asymptotic series
+// e^x/x sum_k k!/x^k stopped at its smallest term; the reciprocals 1/k come from a table.  The
+// two recurrences run in one loop (independent chains, so their latencies overlap); each keeps
+// its own arithmetic and stopping test.
+__device__ __forceinline__ void ei_pair_lane(double x1, double x2, double* e1, double* e2) {
+  const bool ser1 = x1 <= 40.0, ser2 = x2 <= 40.0;
+  const double ix1 = ser1 ? 0.0 : 1.0 / x1, ix2 = ser2 ? 0.0 : 1.0 / x2;
+  double term1 = 1.0, sum1 = ser1 ? 0.0 : 1.0, term2 = 1.0, sum2 = ser2 ? 0.0 : 1.0;
+  bool run1 = true, run2 = true;
+  for (int k = 1; k < kEiTerms && (run1 || run2); ++k) {
+    const double ik = c_invk[k];
+    if (run1) {
+      if (ser1) {
+        term1 = term1 * x1 * ik;
+        const double t = term1 * ik;
+        sum1 += t;
+        if (t < 1e-18 * sum1) run1 = false;
+      } else {
+        const double next = term1 * (double)k * ix1;
+        if (next >= term1 || next < 1e-18 * sum1) run1 = false;
+        else { term1 = next; sum1 += term1; }
+      }
+    }
+    if (run2) {
+      if (ser2) {
+        term2 = term2 * x2 * ik;
+        const double t = term2 * ik;
+        sum2 += t;
+        if (t < 1e-18 * sum2) run2 = false;
+      } else {
+        const double next = term2 * (double)k * ix2;
+        if (next >= term2 || next < 1e-18 * sum2) run2 = false;
+        else { term2 = next; sum2 += term2; }
+      }
+    }
+  }
+  *e1 = ser1 ? kEulerGamma + log(x1) + sum1 : exp(x1) * ix1 * sum1;
+  *e2 = ser2 ? kEulerGamma + log(x2) + sum2 : exp(x2) * ix2 * sum2;
+}
+
+// likelihood.c:376-421 for one lane's own x
+__device__ double pos_marg_lane(double x) {
+  const double Delta = 0.5 * 5.991;
+  if (x <= Delta) return kBad;
+  if (x > 100.) return x - log(Delta) - exp(-Delta);
+  if ((x - Delta) < 0.0001) x = Delta + 0.0001;
+  double yc, ys;
+  ei_pair_lane(x, x - Delta, &yc, &ys);
+  return log((yc - ys) / log(x / (x - Delta)));
+}
+
+// ---- double-float (unevaluated sum of two floats) arithmetic for sin/cos on the FP32 pipes
+__device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
+  f2 p = two_prod(a.hi, b.hi);
+  p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+  return quick_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ f2 df_add(f2 a, f2 b) {
+  f2 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+// P * y + c
+__device__ __forceinline__ f2 df_horner(f2 P, f2 y, float c_hi, float c_lo) {
+  return df_add(df_mul(P, y), f2{c_hi, c_lo});
+}
+
+// sin and cos of a double |a| <= pi/4 from their Taylor series (coefficients 1/n!, split into
+// float pairs), the low-order terms in double-float and the terms below ~2e-9 of the result in
+// float:  sin a = a * sum_k (-1)^k y^k / (2k+1)!,  cos a = sum_k (-1)^k y^k / (2k)!,  y = a^2.
+// Relative error ~1e-14 (double-float carries 48 bits).  About 150 FP32 operations replace the
+// ~40 FP64 ones of sincos(), which at this GPU's FP64 rate cost as much as ~3000 FP32 ones.
+__device__ __forceinline__ void dsincos_small(double a, double* sa, double* ca) {
+  const f2 x = df_from_double(a);
+  const f2 y = df_mul(x, x);
+  const float yf = y.hi;
+  // sin: tail k = 5..9 in float, k = 0..4 in double-float
+  float t = -8.220635078476521e-18f;                                        // -1/19!
+  t = fmaf(t, yf, 2.8114573589663704e-15f);                                 // 1/17!
+  t = fmaf(t, yf, -7.647163609812713e-13f);                                 // -1/15!
+  t = fmaf(t, yf, 1.6059044372074283e-10f);                                 // 1/13!
+  t = fmaf(t, yf, -2.5052107943679403e-08f);                                // -1/11!
+  f2 P{t, 0.f};
+  P = df_horner(P, y, 2.7557318844628753e-06f, 3.793571224297229e-14f);   // 1/9!
+  P = df_horner(P, y, -0.00019841270113829523f, 2.725596874933456e-12f);  // -1/7!
+  P = df_horner(P, y, 0.008333333767950535f, -4.34617203337595e-10f);     // 1/5!
+  P = df_horner(P, y, -0.1666666716337204f, 4.967053879312289e-09f);     // -1/3!
+  P = df_horner(P, y, 1.f, 0.f);
+  const f2 sv = df_mul(x, P);
+  // cos: tail k = 6..10 in float, k = 0..5 in double-float
+  float u = 4.110317590937049e-19f;                                        // 1/20!
+  u = fmaf(u, yf, -1.5619206814541513e-16f);                                // -1/18!
+  u = fmaf(u, yf, 4.7794772561329454e-14f);                                 // 1/16!
+  u = fmaf(u, yf, -1.147074536050896e-11f);                                 // -1/14!
+  u = fmaf(u, yf, 2.0876755879584152e-09f);                                 // 1/12!
+  f2 Q{u, 0.f};
+  Q = df_horner(Q, y, -2.755731998149713e-07f, 7.575112209051195e-15f);   // -1/10!
+  Q = df_horner(Q, y, 2.4801587642286904e-05f, -3.40699609366682e-13f);   // 1/8!
+  Q = df_horner(Q, y, -0.0013888889225199819f, 3.3631094437103215e-11f);  // -1/6!
+  Q = df_horner(Q, y, 0.0416666679084301f, -1.2417634698280722e-09f);     // 1/4!
+  Q = df_horner(Q, y, -0.5f, 0.f);                                         // -1/2!
+  Q = df_horner(Q, y, 1.f, 0.f);
+  *sa = (double)sv.hi + (double)sv.lo;
+  *ca = (double)Q.hi + (double)Q.lo;
+}
+__device__ __forceinline__ void pass_sincos(double a, double* sa, double* ca) {
+  if (fabs(a) <= 0.78539816339744831) dsincos_small(a, sa, ca);
+  else sincos(a, sa, ca);
+}
+__device__ __forceinline__ void pass_sincos(float a, float* sa, float* ca) { sincosf(a, sa, ca); }
+
+// lanes 0..kNodePart-1 of a warp hold the sums of lanes {l, l+8, l+16, l+24}
+__device__ __forceinline__ double part_sum(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 16);
+  v += __shfl_xor_sync(0xffffffffu, v, 8);
+  return v;
+}
+template <class A>
+__device__ __forceinline__ double acc_part(const A& a);
+template <>
+__device__ __forceinline__ double acc_part(const Acc<double>& a) { return part_sum(a.s); }
+template <>
+__device__ __forceinline__ double acc_part(const Acc<float>& a) {
+  float hi = a.s, lo = -a.c;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int m = 16; m >= 8; m >>= 1) {
+    const float ohi = __shfl_xor_sync(0xffffffffu, hi, m), olo = __shfl_xor_sync(0xffffffffu, lo, m);
+    const bool first = (lane & m) == 0;
+    const float ahi = first ? hi : ohi, alo = first ? lo : olo, bhi = first ? ohi : hi, blo = first ? olo : lo;
+    const f2 t = two_sum(ahi, bhi);
+    const f2 r = quick_two_sum(t.hi, t.lo + (alo + blo));
+    hi = r.hi;
+    lo = r.lo;
+  }
+  return (double)hi + (double)lo;
+}
+__device__ __forceinline__ double node_sum(const double* p) {
+  double s = p[0];
+#pragma unroll
+  for (int k = 1; k < kNodePart; ++k) s += p[k];
+  return s;
+}
+
+// The likelihood at every scalelength node (likelihood.c:117-187 with the cross-correlation and
+// Newton search of :194-358 and the position marginal of :376-421), into sh.Lr[1..numr-1].
+// The per-cell passes run on the node warps (lanes = cells; warp w takes nodes w+1, w+1+nw, ...)
+// and leave kNodePart partials of each sum in shared memory.  Warp 0 then carries every node at
+// once (lane = node): the sums, determinant and Newton step of each node and its position
+// marginal.  An FP64 instruction costs the same whatever number of lanes it uses, so the
+// lane-uniform scalar work of 28 nodes costs one warp's instruction stream instead of 28.  The
+// nodes step through their Newton iterations in lock-step rounds, each stopping by the
+// reference's own test.
+template <class P>
+__device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell* gu, const typename P::Cell* gv,
+                           const typename P::Cell* dre, const typename P::Cell* dim, const typename P::Cell* sig2,
+                           int n, double e1, double e2) {
+  using T = typename P::Cell;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  const int numR = c_fit.numr;
+  const int gaussian = c_fit.gaussian;
+  const T a1 = T(1.0 + e1), a2 = T(e2), a3 = T(1.0 - e1);
+  const double detA = 1.0 - e1 * e1 - e2 * e2;
+  const T cc = T(2 * kPi);
+  // galaxy_visibilities.c:63-65 then the 4 pi^2 wave factor of :69
+  auto sfw_of = [&](int node) -> T {
+    const double sc = c_fit.ro[node] * (kPi / 648000.0);
+    return T(((sc * sc) / (detA * detA)) * (4 * kPi * kPi));
+  };
+  // ---- A: model and its norm
+  for (int node = warp + 1; node < numR; node += nw) {
+    const T sfw = sfw_of(node);
+    Acc<T> acc;
+    acc.zero();
+    for (int i = lane; i < n; i += 32) {
+      const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+      if (i < kNodeCache) sh.mcache[node][i] = (double)m;
+      acc.add(m * m / T(sig2[i]));
+    }
+    const double p = acc_part(acc);
+    if (lane < kNodePart) sh.part[0][node][lane] = p;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int node = lane;
+    if (node >= 1 && node < numR) {
+      const double s_norm = sqrt(node_sum(sh.part[0][node]));
+      sh.nnorm[node] = P::kMixed ? 1.0 / s_norm : s_norm;
+    }
+  }
+  __syncthreads();
+  // normalised model of cell i of a node (the reference divides, galaxy_visibilities.c:90)
+  auto model = [&](int node, int i, T sfw, T nn) -> T {
+    const T m = i < kNodeCache ? T(sh.mcache[node][i]) : cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+    return P::kMixed ? m * nn : m / nn;
+  };
+  // ---- B: cross-correlation at zero shift
+  for (int node = warp + 1; node < numR; node += nw) {
+    const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
+    Acc<T> val, dx, dy, d2x, d2y, dxy;
+    val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
+    for (int i = lane; i < n; i += 32) {
+      const T m = model(node, i, sfw, nn);
+      const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
+      const T u = cc * T(gu[i]), v = cc * T(gv[i]);
+      val.add(hre);
+      dx.sub(him * u);
+      dy.sub(him * v);
+      d2x.sub(hre * u * u);
+      d2y.sub(hre * v * v);
+      dxy.sub(hre * u * v);
+    }
+    const double p1 = acc_part(val), p2 = acc_part(dx), p3 = acc_part(dy);
+    const double p4 = acc_part(d2x), p5 = acc_part(d2y), p6 = acc_part(dxy);
+    if (lane < kNodePart) {
+      sh.part[1][node][lane] = p1; sh.part[2][node][lane] = p2; sh.part[3][node][lane] = p3;
+      sh.part[4][node][lane] = p4; sh.part[5][node][lane] = p5; sh.part[6][node][lane] = p6;
+    }
+  }
+  __syncthreads();
+  // ---- Newton rounds; warp 0 holds each node's state in its lane
+  double Sval = 0, Sdx = 0, Sdy = 0, Sd2x = 0, Sd2y = 0, Sdxy = 0, det = 0;
+  double xo = 0, yo = 0, norm = 1, normv = 0;
+  int iter = 0;
+  const bool mine = warp == 0 && lane >= 1 && lane < numR;
+  const double tol = 1.e-7;
+  while (true) {
+    if (warp == 0) {
+      bool act = false;
+      if (mine) {
+        const int node = lane;
+        if (iter == 0 || sh.nactive[node]) {
+          Sval = node_sum(sh.part[1][node]); Sdx = node_sum(sh.part[2][node]); Sdy = node_sum(sh.part[3][node]);
+          Sd2x = node_sum(sh.part[4][node]); Sd2y = node_sum(sh.part[5][node]); Sdxy = node_sum(sh.part[6][node]);
+          det = Sd2x * Sd2y - Sdxy * Sdxy;
+          if (iter > 0) norm = normv;
+          if (det > 0 && norm > tol && iter < kNewtonMax) {
+            iter++;
+            const double incx = (Sdx * Sd2y - Sdy * Sdxy) / det;
+            const double incy = (Sdy * Sd2x - Sdx * Sdxy) / det;
+            xo -= incx;
+            yo -= incy;
+            normv = sqrt(incx * incx + incy * incy);
+            sh.nx[node] = xo;
+            sh.ny[node] = yo;
+            act = true;
+          }
+        }
+        sh.nactive[node] = act;
+      }
+      const unsigned any = __ballot_sync(0xffffffffu, act);
+      if (lane == 0) sh.nany = any != 0;
+    }
+    __syncthreads();
+    if (!sh.nany) break;
+    for (int node = warp + 1; node < numR; node += nw) {
+      if (!sh.nactive[node]) continue;
+      const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
+      const T txo = T(sh.nx[node]), tyo = T(sh.ny[node]);
+      Acc<T> val, dx, dy, d2x, d2y, dxy;
+      val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
+      for (int i = lane; i < n; i += 32) {
+        const T m = model(node, i, sfw, nn);
+        const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
+        const T u = cc * T(gu[i]), v = cc * T(gv[i]);
+        const T a = txo * u + tyo * v;
+        T sa, ca;
+        pass_sincos(a, &sa, &ca);
+        const T rp = (hre * ca - him * sa);
+        const T ip = (hre * sa + him * ca);
+        val.add(rp);
+        dx.sub(ip * u);
+        dy.sub(ip * v);
+        d2x.sub(rp * u * u);
+        d2y.sub(rp * v * v);
+        dxy.sub(rp * u * v);
+      }
+      const double p1 = acc_part(val), p2 = acc_part(dx), p3 = acc_part(dy);
+      const double p4 = acc_part(d2x), p5 = acc_part(d2y), p6 = acc_part(dxy);
+      if (lane < kNodePart) {
+        sh.part[1][node][lane] = p1; sh.part[2][node][lane] = p2; sh.part[3][node][lane] = p3;
+        sh.part[4][node][lane] = p4; sh.part[5][node][lane] = p5; sh.part[6][node][lane] = p6;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- position marginal and determinant term of every node
+  if (mine) {
+    double L = kBad;
+    if (det > 0) {
+      L = pos_marg_lane((Sval * Sval) * 0.5);
+      if (isnan(L)) L = kBad;
+      else if (L != kBad) L = L - 0.5 * log(det);
+    }
+    sh.Lr[lane] = typename P::S(L);
+  }
+  if (warp == 0) {
+    int it = mine ? iter : 0;
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) it += __shfl_xor_sync(0xffffffffu, it, m);
+    if (lane == 0) sh.newton += it;
+  }
+  __syncthreads();
 }
 
 // CTA-collective loglikelihood(e1, e2) (likelihood.c:106-149).
@@ -616,17 +971,8 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typena
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   const int numR = c_fit.numr;
-  for (int node = warp + 1; node < numR; node += nw) {
-    int it = 0;
-    const S r = S(c_fit.ro[node]);
-    S L = node_loglike<P>(gu, gv, dre, dim, sig2, n, e1, e2, r, c_fit.gaussian, &it, nullptr, nullptr,
-                          nullptr, nullptr);
-    if (lane == 0) {
-      sh.Lr[node] = L;
-      atomicAdd(&sh.newton, it);
-    }
-  }
-  __syncthreads();
+  (void)nw;
+  eval_nodes<P>(sh, gu, gv, dre, dim, sig2, n, (double)e1, (double)e2);
   if (warp == 0) {
     // set_posterior_values (marginalise_r.c:29-64)
     if (lane == 0) {
@@ -978,7 +1324,7 @@ __device__ __forceinline__ size_t cells_smem_bytes(int max_cells) {
 }
 
 template <class P>
-__global__ void __launch_bounds__(kFitThreads, 1) k_fit(FacetBatch b) {
+__global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b) {
   using Cell = typename P::Cell;
   using S = typename P::S;
   __shared__ FitShared<S> sh;
@@ -1009,7 +1355,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_fit(FacetBatch b) {
       gu[i] = Gu[i]; gv[i] = Gv[i]; dre[i] = Dr[i]; dim[i] = Di[i]; sig2[i] = Sg[i];
     }
     for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[(size_t)g * kMaxNodes + i]);
-    if (tid == 0) { sh.newton = 0; sh.status = 0; }
+    if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
@@ -1037,7 +1383,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_loglike_once(FacetBatch b, d
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
-  if (tid == 0) { sh.newton = 0; sh.status = 0; }
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   __syncthreads();
   int err = 0;
   S L = eval_loglike<P>(sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
@@ -1056,7 +1402,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, 
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
-  if (tid == 0) { sh.newton = 0; sh.status = 0; }
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   __syncthreads();
   FitCtx<P> c{&sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
               reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
@@ -1088,7 +1434,7 @@ __global__ void k_xcorr(int n, const double* gu, const double* gv, const double*
 __global__ void k_marginalise_once(int n, const double* x, double* y, double* out1) {
   __shared__ FitShared<double> sh;
   const int lane = threadIdx.x;
-  if (lane == 0) { sh.status = 0; for (int i = 0; i < n; ++i) { sh.xs[i] = x[i]; sh.ys[i] = y[i]; } }
+  if (lane == 0) { sh.status = 0; sh.fac_n = -1; for (int i = 0; i < n; ++i) { sh.xs[i] = x[i]; sh.ys[i] = y[i]; } }
   __syncwarp();
   double L = marginalise_posterior_warp<double>(sh, n);
   __syncwarp();
@@ -1134,7 +1480,11 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
   for (int i = 0; i < kMaxNodes; ++i) {
     h.ro[i] = (i < cfg.numr) ? cfg.ro[i] : 0.0;
   }
+  static double invk[kEiTerms];
+  for (int k = 0; k < kEiTerms; ++k) invk[k] = k ? 1.0 / k : 0.0;
   cudaError_t e = cudaMemcpyToSymbolAsync(c_fit, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invk, invk, sizeof(invk), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // h is released on return
   if (e != cudaSuccess) { fprintf(stderr, "rlf: fit config: %s\n", cudaGetErrorString(e)); return (int)e; }
   return 0;
 }
