@@ -261,6 +261,32 @@ int launch_classify_items(long long total, const SeqBatch& b, int* items, int* c
   return check("k_classify_items");
 }
 
+// sin(2 pi t) and cos(2 pi t) for a phase in turns: quadrant q = rint(4t), remainder
+// r = t - q/4 in [-1/8, 1/8] (an angle within pi/4), Taylor series of sin and cos in r with the
+// coefficients (2 pi)^n / n! rounded to float (terms below 2e-9 dropped); ~1.3 ulp.
+__device__ __forceinline__ void sincos_turn(float t, float* s, float* c) {
+  const float q = rintf(4.f * t);
+  const float r = fmaf(q, -0.25f, t);
+  const float r2 = r * r;
+  float sp = 42.058692932128906f;
+  sp = fmaf(sp, r2, -76.70585632324219f);
+  sp = fmaf(sp, r2, 81.6052474975586f);
+  sp = fmaf(sp, r2, -41.34170150756836f);
+  sp = fmaf(sp, r2, 6.2831854820251465f);
+  sp *= r;
+  float cp = 7.903536319732666f;
+  cp = fmaf(cp, r2, -26.42625617980957f);
+  cp = fmaf(cp, r2, 60.2446403503418f);
+  cp = fmaf(cp, r2, -85.45681762695312f);
+  cp = fmaf(cp, r2, 64.93939208984375f);
+  cp = fmaf(cp, r2, -19.739208221435547f);
+  cp = fmaf(cp, r2, 1.f);
+  const int qi = (int)q & 3;
+  const float s1 = (qi & 1) ? cp : sp, c1 = (qi & 1) ? -sp : cp;
+  *s = (qi & 2) ? -s1 : s1;
+  *c = (qi & 2) ? -c1 : c1;
+}
+
 __device__ __forceinline__ float profile(float x, int gauss) {
   return gauss ? __expf(-0.5f * x) : round_shape(x);
 }
@@ -288,6 +314,7 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
   }
   for (int f = 0; f < b.n_sizes; ++f) dcache[f * kSeqThreads + tid] = b.desc[f][t];
   const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
+  const float invq = rw.q > 0.f ? 1.f / rw.q : 0.f;
   // wn^2 (u^2 + v^2) of channel c0 + k
 #define XB(k) (c_bch[c0 + (k)].wn2 * rw.q)
   for (int j = 0; j < b.n_gal; ++j) {
@@ -297,16 +324,15 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
     const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
     const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
     float ws, wc, zs, zc;
-    sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
+    sincos_turn(dT.hi + dT.lo, &ws, &wc);
     const float ta = c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0);
-    sincospif(2.f * ta, &zs, &zc);
+    sincos_turn(ta, &zs, &zc);
     const float wr = wc, wi = -ws;    // w = exp(-2 pi i dT)
     const float zr0 = zc, zi0 = -zs;  // exp(-2 pi i T(c0))
     const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
     float2* fac = acc + s.off;
     // fitted model: |k'|^2 = A u^2 + B uv + C v^2 (sheared), as a factor on wn^2 (u^2 + v^2)
-    const float k1q = g.A * uu + g.B * rw.uv + g.Cc * vv;
-    const float f1 = rw.q > 0.f ? g.sf1 * k1q / rw.q : 0.f;
+    const float f1 = s.apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
     if (SIMPLE) {
       // one run: all 16 channels valid and in the cell d & 0xffff
       float cr, ci;
@@ -384,7 +410,7 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
 }
 
 template <int GAUSS>
-__global__ void __launch_bounds__(kSeqThreads, 2) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
+__global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
                                                                 const float2* __restrict__ sky, SeqBatch b,
                                                                 float2* __restrict__ partial) {

@@ -21,10 +21,20 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
 int launch_row_table(int n_rows, const double* uu, const double* vv, const double* ww, RowF* rows,
                      cudaStream_t st);
 // ---- sequential batch extraction (exact in-batch removal order)
-constexpr int kSeqThreads = 256;
+#ifndef RLF_SEQ_THREADS
+#define RLF_SEQ_THREADS 384
+#endif
+#ifndef RLF_SEQ_CTAS_PER_SM
+#define RLF_SEQ_CTAS_PER_SM 2
+#endif
+#ifndef RLF_SEQ_FACET_KB
+#define RLF_SEQ_FACET_KB 96
+#endif
+constexpr int kSeqThreads = RLF_SEQ_THREADS;      // threads of a sequential extraction CTA
+constexpr int kSeqCtasPerSm = RLF_SEQ_CTAS_PER_SM;  // CTAs per SM (register budget of the kernel)
 constexpr int kSeqMaxSizes = 16;                  // distinct facet sizes in one batch
 constexpr int kSeqMaxGal = 512;                   // galaxies in one batch
-constexpr size_t kSeqFacetBudget = 96 * 1024;     // shared facet accumulators of one batch, bytes
+constexpr size_t kSeqFacetBudget = (size_t)RLF_SEQ_FACET_KB * 1024;  // shared facet accumulators of one batch
 
 // Run descriptor of one 16-channel chunk of one row for one facet size: the cell of the chunk's
 // first channel in bits 0-15, bit 16+k set when channel k of the chunk is flagged, beyond the last

@@ -429,7 +429,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   int sms = 0, dev = 0;
   RLF_CUDA(cudaGetDevice(&dev));
   RLF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int seq_ctas = 2 * sms;
+  const int seq_ctas = kSeqCtasPerSm * sms;
   if (batched && !ob->rows.p) {
     RLF_OK(ob->rows.ensure(ob->n_rows));
     RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
