@@ -13,13 +13,17 @@ class Case:
     """A small observation with its catalogue, data, variances and flags (host arrays)."""
 
     def __init__(self, n_ant=24, ha_hours=2.0, dt_s=600.0, n_ch=4, n_gal=8, fmin=50.0, fmax=200.0,
-                 noise=600.0, g=(0.03, -0.02), seed=2, flag_frac=0.0, scale_mult=1.0):
+                 noise=600.0, g=(0.03, -0.02), seed=2, flag_frac=0.0, scale_mult=1.0, gaussian=False,
+                 scale_override=None):
         self.obs = synth.make_observation(n_ant=n_ant, ha_hours=ha_hours, dt_s=dt_s, n_ch=n_ch)
         self.cat = synth.make_catalogue(n_gal, fmin, fmax, g=g, seed=seed)
         self.cat.scale = np.clip(self.cat.scale * scale_mult, 0.05, K.RMAX)
+        for gi, sc in (scale_override or {}).items():
+            self.cat.scale[gi] = sc
+        self.gaussian = int(bool(gaussian))
         self.noise = noise
-        self.data = synth.simulate_visibilities_np(self.obs, self.cat, noise_sigma=noise,
-                                                   seed=seed + 1).astype(np.complex128)
+        self.data = synth.simulate_visibilities_np(self.obs, self.cat, noise_sigma=noise, seed=seed + 1,
+                                                   gaussian=bool(gaussian)).astype(np.complex128)
         self.sigma2 = np.full(self.obs.n_vis, np.float32(noise * noise), dtype=np.float32)
         rng = np.random.default_rng(seed + 7)
         self.flag = (rng.random(self.obs.n_vis) < flag_frac).astype(np.uint8)
@@ -37,7 +41,7 @@ def oracle_sky_model(orc, case):
     gal = np.zeros(o.n_vis, np.complex128)
     orc.orc_sky_model(O.dp(o.wavenumbers), O.dp(o.spec), o.n_ch, c.n, O.dp(c.flux), O.dp(c.scale),
                       O.dp(c.l), O.dp(c.m), o.n_rows, O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), O.cp(gal),
-                      O.cp(sky), 0)
+                      O.cp(sky), case.gaussian)
     return sky
 
 
@@ -59,7 +63,7 @@ def oracle_data_processing(orc, case, data, sky, re_fitting=False, bad_list=None
                             o.n_rows, o.n_ch, O.dp(o.spec), O.dp(o.wavenumbers), case.numr,
                             O.dp(case.ro), O.dp(c.l), O.dp(c.m), O.dp(c.flux), O.dp(c.scale),
                             O.dp(sumw), O.cp(gal), O.cp(sky), O.cp(data), O.fp(case.sigma2),
-                            O.bp(case.flag), O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), 0, out,
+                            O.bp(case.flag), O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), case.gaussian, out,
                             C.byref(bad))
     res = [(r.e1, r.e2, r.var_e1, r.var_e2, r.oneDimvar, r.maxL, r.error, r.nevals, r.max_e1, r.max_e2)
            for r in out]
@@ -78,7 +82,7 @@ def oracle_facet(orc, case, gi, data, sky):
     orc.orc_source_extraction(o.n_ch, O.dp(o.spec), O.dp(o.wavenumbers), F, O.cp(fvis), O.dp(fs2),
                               O.dp(sumw), c.l[gi], c.m[gi], c.flux[gi], c.scale[gi], 0.0, 0.0,
                               O.cp(sky), O.cp(data), O.cp(gal), O.fp(case.sigma2), O.bp(case.flag),
-                              o.n_rows, O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), case.len, 0)
+                              o.n_rows, O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), case.len, case.gaussian)
     gu = np.zeros(nc)
     gv = np.zeros(nc)
     n = orc.orc_facet_coords(O.dp(gu), O.dp(gv), case.len, F, O.dp(sumw))
