@@ -1,22 +1,17 @@
-// Batched mixed-precision extraction and removal: many galaxies per pass over the visibilities.
+// Batched FP32 visibility passes: many galaxies per pass over the visibilities.
 //
-// A single-galaxy pass over the data is HBM-bound (one read of data and sky model per galaxy);
-// processing a batch of B galaxies per pass reads the data once per 32 galaxies and turns the
-// pass into FP32/SFU work, B times less HBM traffic per galaxy.
+// A one-galaxy pass over the data is HBM-bound (one read of data and sky model per galaxy);
+// taking a batch of galaxies per pass reads the data once per batch and turns the pass into
+// FP32/SFU work.  Every kernel forms, per (row, galaxy), the delay p = u l + v m + w n in
+// double-float arithmetic from an FP32 row table, the phase turns T(ch) = p * inv_lambda(ch) =
+// T0 + ch * dT (channels evenly spaced) reduced modulo 1, and rotates through the channels of a
+// 16-channel chunk by a recurrence in exp(-+2 pi i dT).
 //
-// Extraction (source_extraction.c:46-68 + evaluate_uv_grid.c:143-211, batch form): a warp owns
-// 32 galaxies with the same facet size; all lanes walk the same rows, so every row load is a
-// broadcast and every facet update hits consecutive shared-memory words (lane = galaxy).  For a
-// row and galaxy the delay p = u l + v m + w n is formed in double-float arithmetic, the phase
-// turns T(ch) = p * inv_lambda(ch) = T0 + ch * dT (channels evenly spaced) are range-reduced, and
-// the rotated residual sum over a run of channels in one cell is evaluated by Horner's rule in
-// w = exp(-2 pi i dT), re-anchored with an accurate sincospi every 16 channels.  The galaxy's own
-// round model, real after the shift, is added per visibility.  Warps accumulate FP32 facets in
-// shared memory; CTAs write partial facets that are reduced in FP64, in a fixed order.
-//
-// Removal (data_processing.c:109-135, batch form): one thread per (row, 16-channel chunk) loops
-// over the batch's galaxies held in shared memory and subtracts sum(round) from the sky model
-// and sum(fitted) from the data with one read-modify-write of each.
+//   k_extract_seq      source extraction of a sub-batch in the reference's removal order
+//                      (source_extraction.c:46-68, evaluate_uv_grid.c:143-211, data_processing.c:61-138)
+//   k_finalize_seq     per-galaxy facet sums and finalisation
+//   k_remove_batch     removal of a sub-batch's fitted and round models (data_processing.c:109-135)
+//   k_model_sum_batch  sums of round or sheared models: sky model and simulator
 #include "rlf_batch.cuh"
 #include "rlf_fit.cuh"
 #include <stdio.h>
@@ -628,6 +623,97 @@ int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
   if (gaussian) k_remove_batch<1><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
   else k_remove_batch<0><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
   return check("k_remove_batch");
+}
+
+// ------------------------------------------------------------- model sums
+// vis += sum over galaxies of their model visibilities: the round models for the sky model
+// (data_simulation.c:131-165, sky_model) or the sheared models for the simulator
+// (data_simulation.c:41-127 with galaxy_visibilities.c:154-190).  Thread per (row, 16-channel
+// chunk), galaxies staged in shared memory; per (row, galaxy) the double-float delay and two
+// sin/cos of the phase, per channel a phase recurrence and the profile.
+template <int GAUSS, int SHEARED>
+__global__ void __launch_bounds__(256) k_model_sum_batch(int n_rows, const RowF* __restrict__ rows, float2* vis,
+                                                         const GalaxyParams* __restrict__ gals, int n_gal) {
+  __shared__ GalF sg[kRemTile];
+  const int nch = c_bnch;
+  const int nchunk = (nch + kRemCh - 1) / kRemCh;
+  const long long total = (long long)n_rows * nchunk;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // all threads of the block iterate the same number of times so that the tiles can be shared
+  const long long iters = (total + stride - 1) / stride;
+  for (long long it = 0; it < iters; ++it) {
+    const long long t = it * stride + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = t < total;
+    const int r = live ? (int)(t % n_rows) : 0;
+    const int ch0 = live ? (int)(t / n_rows) * kRemCh : 0;
+    const RowF rw = rows[r];
+    const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
+    float ar[kRemCh], ai[kRemCh];
+#pragma unroll
+    for (int k = 0; k < kRemCh; ++k) { ar[k] = ai[k] = 0.f; }
+    for (int g0 = 0; g0 < n_gal; g0 += kRemTile) {
+      const int gn = min(kRemTile, n_gal - g0);
+      __syncthreads();
+      for (int i = threadIdx.x; i < gn; i += blockDim.x) sg[i] = load_gal(gals[g0 + i], nullptr, nullptr);
+      __syncthreads();
+      if (!live) continue;
+      for (int i = 0; i < gn; ++i) {
+        const GalF g = sg[i];
+        const f2 p = delay_df(rw, g);
+        const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
+        const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
+        float zr, zi, ws, wc;
+        sincos_turn(turns_at(T0, dT, ch0), &zi, &zr);  // exp(+2 pi i T): the model phase
+        sincos_turn(dT.hi + dT.lo, &ws, &wc);
+        const float q = SHEARED ? g.A * uu + g.B * rw.uv + g.Cc * vv : rw.q;
+        const float sf = SHEARED ? g.sf1 : g.sf0;
+#pragma unroll
+        for (int k = 0; k < kRemCh; ++k) {
+          const int ch = ch0 + k;
+          if (ch < nch) {
+            const BatchChan bc = c_bch[ch];
+            const float x = sf * bc.wn2 * q;
+            const float a = (GAUSS ? __expf(-0.5f * x) : round_shape(x)) * bc.spec * g.flux;
+            ar[k] = fmaf(a, zr, ar[k]);
+            ai[k] = fmaf(a, zi, ai[k]);
+            const float nzr = fmaf(zr, wc, -zi * ws);
+            const float nzi = fmaf(zr, ws, zi * wc);
+            zr = nzr;
+            zi = nzi;
+          }
+        }
+      }
+    }
+    if (!live) continue;
+#pragma unroll
+    for (int k = 0; k < kRemCh; ++k) {
+      const int ch = ch0 + k;
+      if (ch < nch) {
+        const size_t idx = (size_t)ch * n_rows + r;
+        float2 v = vis[idx];
+        v.x += ar[k];
+        v.y += ai[k];
+        vis[idx] = v;
+      }
+    }
+  }
+}
+
+int launch_model_sum_batch(int n_rows, const RowF* rows, float2* vis, const GalaxyParams* gals, int n_gal,
+                           int sheared, int gaussian, cudaStream_t st) {
+  if (n_gal <= 0) return 0;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 4;
+  if (gaussian) {
+    if (sheared) k_model_sum_batch<1, 1><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
+    else k_model_sum_batch<1, 0><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
+  } else {
+    if (sheared) k_model_sum_batch<0, 1><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
+    else k_model_sum_batch<0, 0><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
+  }
+  return check("k_model_sum_batch");
 }
 
 }  // namespace rlf

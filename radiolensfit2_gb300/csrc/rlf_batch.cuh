@@ -69,6 +69,10 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
 // finalisation and compaction into out (slot = galaxy index in the batch)
 int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, const double* const* ss,
                         const double* const* sw, double len, FacetOut out, cudaStream_t st);
+// vis += the round models (sheared = 0: the sky model) or the sheared models (sheared = 1: the
+// simulator) of n_gal galaxies, FP32 visibilities, evenly spaced channels (batch_set_channels)
+int launch_model_sum_batch(int n_rows, const RowF* rows, float2* vis, const GalaxyParams* gals, int n_gal,
+                           int sheared, int gaussian, cudaStream_t st);
 int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
                         const GalaxyParams* gals, const FitOut* fit, int n_gal, int gaussian,
                         cudaStream_t st);

@@ -838,6 +838,42 @@ int rlf_obs_get_vis(rlf_observation* obs, double* data_c128, double* sky_c128) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace rlf {
+// data (use_e = 1, sheared models) or sky model (use_e = 0, round models) += the models of n_gal
+// galaxies; FP32 observations with evenly spaced channels take the batched kernel, the others
+// the per-visibility kernels
+static int add_models(rlf_observation* obs, const GalaxyParams* dg, int n_gal, int use_e, int gaussian,
+                      cudaStream_t st) {
+  const Observation o = obs->view();
+  const int chunk = 256;  // galaxies per launch keeps each launch short
+  int bc = -1;
+  if (obs->precision != RLF_F64) {
+    bc = batch_set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), obs->max_delay_m, st);
+    if (bc > 0) return bc;
+    if (bc == 0 && !obs->rows.p) {
+      RLF_OK(obs->rows.ensure(obs->n_rows));
+      RLF_OK(launch_row_table(obs->n_rows, obs->uu.p, obs->vv.p, obs->ww.p, obs->rows.p, st));
+    }
+  }
+  for (int g0 = 0; g0 < n_gal; g0 += chunk) {
+    const int gn = std::min(chunk, n_gal - g0);
+    if (obs->precision == RLF_F64) {
+      RLF_OK(launch_sky_model_f64(o, use_e ? obs->data64.p : obs->sky64.p, dg + g0, gn, use_e, gaussian, st));
+    } else if (bc == 0) {
+      RLF_OK(launch_model_sum_batch(obs->n_rows, obs->rows.p, use_e ? obs->data32.p : obs->sky32.p, dg + g0, gn,
+                                    use_e, gaussian, st));
+    } else {
+      RLF_OK(launch_sky_model_mixed(o, use_e ? obs->data32.p : obs->sky32.p, dg + g0, gn, use_e, gaussian, st));
+    }
+  }
+  return 0;
+}
+}  // namespace rlf
+
+extern "C" {
+
 int rlf_obs_simulate(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* e1,
                      const double* e2, const double* l, const double* m, double noise_sigma, uint64_t seed,
                      int gaussian) {
@@ -847,13 +883,7 @@ int rlf_obs_simulate(rlf_observation* obs, int n_gal, const double* flux, const 
   std::vector<GalaxyParams> g = make_gals(n_gal, flux, scale, e1, e2, l, m, obs->len, 0);
   DevBuf<GalaxyParams> dg;
   RLF_OK(dg.upload(g.data(), g.size(), st));
-  const Observation o = obs->view();
-  const int chunk = 256;  // galaxies per launch keeps each launch short
-  for (int g0 = 0; g0 < n_gal; g0 += chunk) {
-    const int gn = std::min(chunk, n_gal - g0);
-    if (obs->precision == RLF_F64) RLF_OK(launch_sky_model_f64(o, obs->data64.p, dg.p + g0, gn, 1, gaussian, st));
-    else RLF_OK(launch_sky_model_mixed(o, obs->data32.p, dg.p + g0, gn, 1, gaussian, st));
-  }
+  RLF_OK(add_models(obs, dg.p, n_gal, 1, gaussian, st));
   if (noise_sigma > 0) {
     if (obs->precision == RLF_F64) k_add_noise<double2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data64.p, noise_sigma, seed);
     else k_add_noise<float2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data32.p, noise_sigma, seed);
@@ -871,13 +901,7 @@ int rlf_obs_sky_model(rlf_observation* obs, int n_gal, const double* flux, const
   std::vector<GalaxyParams> g = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, 0);
   DevBuf<GalaxyParams> dg;
   RLF_OK(dg.upload(g.data(), g.size(), st));
-  const Observation o = obs->view();
-  const int chunk = 256;
-  for (int g0 = 0; g0 < n_gal; g0 += chunk) {
-    const int gn = std::min(chunk, n_gal - g0);
-    if (obs->precision == RLF_F64) RLF_OK(launch_sky_model_f64(o, obs->sky64.p, dg.p + g0, gn, 0, gaussian, st));
-    else RLF_OK(launch_sky_model_mixed(o, obs->sky32.p, dg.p + g0, gn, 0, gaussian, st));
-  }
+  RLF_OK(add_models(obs, dg.p, n_gal, 0, gaussian, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   return 0;
 }

@@ -91,3 +91,35 @@ def test_batched_two_passes(orc):
     # data and sky model after both passes: FP32 storage, relative to their scale
     assert np.max(np.abs(d - d2)) < 1e-5 * np.max(np.abs(d2))
     assert np.max(np.abs(s - s2)) < 1e-5 * np.max(np.abs(sky))
+
+
+@pytest.mark.parametrize("gaussian", [0, 1])
+def test_sky_model_and_simulator(orc, gaussian):
+    """rlf_obs_sky_model (round models, data_simulation.c:131-165) and the noise-free
+    rlf_obs_simulate (sheared models) against the oracle's per-galaxy, per-channel model
+    visibilities (galaxy_visibilities.c:154-190)."""
+    case = Case(n_ant=48, ha_hours=2.0, dt_s=600.0, n_ch=8, n_gal=12, fmin=30.0, fmax=200.0, noise=0.0,
+                gaussian=bool(gaussian))
+    o, c = case.obs, case.cat
+    sky_ref = oracle_sky_model(orc, case)
+    data_ref = np.zeros(o.n_vis, np.complex128)
+    one = np.zeros(o.n_rows, np.complex128)
+    for gi in range(c.n):
+        for ch in range(o.n_ch):
+            orc.orc_data_galaxy_vis(o.spec[ch], o.wavenumbers[ch], c.e1[gi], c.e2[gi], c.scale[gi], c.flux[gi],
+                                    c.l[gi], c.m[gi], o.n_rows, O.dp(o.uu), O.dp(o.vv), O.dp(o.ww), O.cp(one),
+                                    gaussian)
+            data_ref[ch * o.n_rows:(ch + 1) * o.n_rows] += one
+    # F64 observations follow the reference arithmetic; FP32 ones carry the phase argument as
+    # double-float and round every visibility to FP32
+    for prec, tol in ((_lib.RLF_F64, 1e-12), (_lib.RLF_MIXED, 2e-6)):
+        dev = DeviceObservation(o, precision=prec, sigma2=case.sigma2, flag=case.flag)
+        dev.set_vis(np.zeros(o.n_vis, np.complex128), np.zeros(o.n_vis, np.complex128))
+        dev.sky_model(c, gaussian=gaussian)
+        dev.simulate(c, 0.0, gaussian=gaussian)
+        d, s = dev.get_vis()
+        dev.close()
+        es = np.max(np.abs(s - sky_ref)) / np.max(np.abs(sky_ref))
+        ed = np.max(np.abs(d - data_ref)) / np.max(np.abs(data_ref))
+        print(f"precision {prec} gaussian {gaussian}: sky model {es:.2e}, simulated data {ed:.2e}")
+        assert es < tol and ed < tol
