@@ -27,19 +27,21 @@
 namespace rlf {
 
 #ifndef RLF_FIT_WARPS
-#define RLF_FIT_WARPS 24
+#define RLF_FIT_WARPS 8
 #endif
 // warps of a fit CTA (one galaxy); the scalelength nodes are spread over them, and small CTAs run
-// several galaxies per SM
+// several galaxies per SM, so that one galaxy's serial phases overlap another's cell passes
 constexpr int kFitWarps = RLF_FIT_WARPS;
 constexpr int kFitThreads = kFitWarps * 32;
-constexpr int kFitMinBlocks = kFitWarps <= 7 ? 3 : (kFitWarps <= 12 ? 2 : 1);
+constexpr int kFitMinBlocks = kFitWarps <= 8 ? 3 : (kFitWarps <= 12 ? 2 : 1);
 constexpr int kQagCap = 256;       // intervals held by the device QAG
 constexpr int kNewtonMax = 50;     // likelihood.c:290
 constexpr int kSimplexMax = 50;    // galaxy_fitting.c:80
 constexpr int kModelCache = 4;     // facet cells per lane whose model stays in registers
-constexpr int kNodePart = 8;       // partials per cross-correlation sum left by a node's warp
+constexpr int kNodePart = 8;       // partials per cross-correlation sum left by a node's lanes
 constexpr int kNodeCache = 64;     // facet cells per node whose model stays in shared memory
+constexpr int kNodeStride = kNodeCache + 8;  // padded row of the per-node caches (bank spread)
+constexpr int kNodesPerWarp = 32 / kNodePart;  // nodes whose cell passes share a warp
 constexpr int kEiTerms = 512;      // reciprocal table of the per-lane Ei series
 
 __constant__ double c_invk[kEiTerms];  // 1 / k
@@ -390,15 +392,24 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
 }
 
 // ------------------------------------------------------------- shared state
+// Per-node caches of the phased node evaluation (eval_nodes), in dynamic shared memory: the first
+// kNodeCache cells of every node.  Phase A leaves the unnormalised model in hre; phase B replaces
+// it by the real part of data x normalised model and fills him (the model does not change during
+// the Newton search, so the Newton passes read both back and evaluate no model).
+struct NodeCache {
+  double hre[kMaxNodes][kNodeStride];
+  double him[kMaxNodes][kNodeStride];
+  double cu[kNodeCache], cv[kNodeCache];  // 2 pi u and 2 pi v of the cells
+};
+
 template <class S>
 struct FitShared {
-  // phased node evaluation (eval_nodes): per-node partial sums, state and model cache
+  // phased node evaluation (eval_nodes): per-node partial sums and state
   double part[7][kMaxNodes][kNodePart];  // 0: model norm; 1..6: val, dx, dy, d2x, d2y, dxy
-  double mcache[kMaxNodes][kNodeCache];   // model of the first kNodeCache cells of each node
   double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
   double nnorm[kMaxNodes];                // the node's model normalisation (F64: norm, mixed: 1/norm)
-  int nactive[kMaxNodes];                 // node has a pass pending
-  int nany;
+  int alist[kMaxNodes];                   // nodes with a Newton pass pending
+  int nact;
   // natural spline rows and the factorisation of its matrix for the abscissae fac_x[0..fac_n)
   S soff[kMaxNodes], sdiag[kMaxNodes], sg[kMaxNodes], sz[kMaxNodes], salpha[kMaxNodes], sgamma[kMaxNodes];
   S fac_x[kMaxNodes];
@@ -766,32 +777,13 @@ __device__ __forceinline__ void pass_sincos(double a, double* sa, double* ca) {
 }
 __device__ __forceinline__ void pass_sincos(float a, float* sa, float* ca) { sincosf(a, sa, ca); }
 
-// lanes 0..kNodePart-1 of a warp hold the sums of lanes {l, l+8, l+16, l+24}
-__device__ __forceinline__ double part_sum(double v) {
-  v += __shfl_xor_sync(0xffffffffu, v, 16);
-  v += __shfl_xor_sync(0xffffffffu, v, 8);
-  return v;
-}
+// one lane's partial of a cross-correlation sum, as double
 template <class A>
-__device__ __forceinline__ double acc_part(const A& a);
+__device__ __forceinline__ double acc_value(const A& a);
 template <>
-__device__ __forceinline__ double acc_part(const Acc<double>& a) { return part_sum(a.s); }
+__device__ __forceinline__ double acc_value(const Acc<double>& a) { return a.s; }
 template <>
-__device__ __forceinline__ double acc_part(const Acc<float>& a) {
-  float hi = a.s, lo = -a.c;
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int m = 16; m >= 8; m >>= 1) {
-    const float ohi = __shfl_xor_sync(0xffffffffu, hi, m), olo = __shfl_xor_sync(0xffffffffu, lo, m);
-    const bool first = (lane & m) == 0;
-    const float ahi = first ? hi : ohi, alo = first ? lo : olo, bhi = first ? ohi : hi, blo = first ? olo : lo;
-    const f2 t = two_sum(ahi, bhi);
-    const f2 r = quick_two_sum(t.hi, t.lo + (alo + blo));
-    hi = r.hi;
-    lo = r.lo;
-  }
-  return (double)hi + (double)lo;
-}
+__device__ __forceinline__ double acc_value(const Acc<float>& a) { return (double)a.s - (double)a.c; }
 __device__ __forceinline__ double node_sum(const double* p) {
   double s = p[0];
 #pragma unroll
@@ -801,17 +793,20 @@ __device__ __forceinline__ double node_sum(const double* p) {
 
 // The likelihood at every scalelength node (likelihood.c:117-187 with the cross-correlation and
 // Newton search of :194-358 and the position marginal of :376-421), into sh.Lr[1..numr-1].
-// The per-cell passes run on the node warps (lanes = cells; warp w takes nodes w+1, w+1+nw, ...)
-// and leave kNodePart partials of each sum in shared memory.  Warp 0 then carries every node at
-// once (lane = node): the sums, determinant and Newton step of each node and its position
-// marginal.  An FP64 instruction costs the same whatever number of lanes it uses, so the
-// lane-uniform scalar work of 28 nodes costs one warp's instruction stream instead of 28.  The
-// nodes step through their Newton iterations in lock-step rounds, each stopping by the
-// reference's own test.
+//
+// Cell passes: a node's cells run on a segment of kNodePart lanes (four nodes per warp; lane
+// 8j + c takes cells c, c + 8, ... of the warp's j-th node) and every lane leaves its own partial
+// of each sum in shared memory.  Most facets hold a few dozen cells, so a whole warp per node
+// would leave most lanes idle, and an FP64 instruction costs this GPU's SM the same whatever
+// number of its lanes are active.  Warp 0 then carries every node at once (lane = node): the
+// sums, determinant and Newton step of each node and its position marginal.  The nodes step
+// through their Newton iterations in lock-step rounds, each stopping by the reference's own test;
+// a round's cell pass takes only the nodes still iterating, packed into consecutive segments.
 template <class P>
-__device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell* gu, const typename P::Cell* gv,
-                           const typename P::Cell* dre, const typename P::Cell* dim, const typename P::Cell* sig2,
-                           int n, double e1, double e2) {
+__device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const typename P::Cell* gu,
+                           const typename P::Cell* gv, const typename P::Cell* dre,
+                           const typename P::Cell* dim, const typename P::Cell* sig2, int n, double e1,
+                           double e2) {
   using T = typename P::Cell;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
@@ -820,23 +815,37 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell*
   const T a1 = T(1.0 + e1), a2 = T(e2), a3 = T(1.0 - e1);
   const double detA = 1.0 - e1 * e1 - e2 * e2;
   const T cc = T(2 * kPi);
+  const int seg = lane >> 3, c0 = lane & (kNodePart - 1);
+  const int ncache = n < kNodeCache ? n : kNodeCache;
   // galaxy_visibilities.c:63-65 then the 4 pi^2 wave factor of :69
   auto sfw_of = [&](int node) -> T {
     const double sc = c_fit.ro[node] * (kPi / 648000.0);
     return T(((sc * sc) / (detA * detA)) * (4 * kPi * kPi));
   };
+  // normalised model of an uncached cell (the reference divides, galaxy_visibilities.c:90)
+  auto model = [&](int i, T sfw, T nn) -> T {
+    const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+    return P::kMixed ? m * nn : m / nn;
+  };
+  const int groups = (numR - 1 + kNodesPerWarp - 1) / kNodesPerWarp;
   // ---- A: model and its norm
-  for (int node = warp + 1; node < numR; node += nw) {
-    const T sfw = sfw_of(node);
-    Acc<T> acc;
-    acc.zero();
-    for (int i = lane; i < n; i += 32) {
-      const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-      if (i < kNodeCache) sh.mcache[node][i] = (double)m;
-      acc.add(m * m / T(sig2[i]));
+  for (int i = threadIdx.x; i < ncache; i += blockDim.x) {
+    nc.cu[i] = (double)(cc * T(gu[i]));
+    nc.cv[i] = (double)(cc * T(gv[i]));
+  }
+  for (int g = warp; g < groups; g += nw) {
+    const int node = 1 + g * kNodesPerWarp + seg;
+    if (node < numR) {
+      const T sfw = sfw_of(node);
+      Acc<T> acc;
+      acc.zero();
+      for (int i = c0; i < n; i += kNodePart) {
+        const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+        if (i < kNodeCache) nc.hre[node][i] = (double)m;
+        acc.add(m * m / T(sig2[i]));
+      }
+      sh.part[0][node][c0] = acc_value(acc);
     }
-    const double p = acc_part(acc);
-    if (lane < kNodePart) sh.part[0][node][lane] = p;
   }
   __syncthreads();
   if (warp == 0) {
@@ -847,32 +856,37 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell*
     }
   }
   __syncthreads();
-  // normalised model of cell i of a node (the reference divides, galaxy_visibilities.c:90)
-  auto model = [&](int node, int i, T sfw, T nn) -> T {
-    const T m = i < kNodeCache ? T(sh.mcache[node][i]) : cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-    return P::kMixed ? m * nn : m / nn;
-  };
-  // ---- B: cross-correlation at zero shift
-  for (int node = warp + 1; node < numR; node += nw) {
-    const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
-    Acc<T> val, dx, dy, d2x, d2y, dxy;
-    val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
-    for (int i = lane; i < n; i += 32) {
-      const T m = model(node, i, sfw, nn);
-      const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
-      const T u = cc * T(gu[i]), v = cc * T(gv[i]);
-      val.add(hre);
-      dx.sub(him * u);
-      dy.sub(him * v);
-      d2x.sub(hre * u * u);
-      d2y.sub(hre * v * v);
-      dxy.sub(hre * u * v);
-    }
-    const double p1 = acc_part(val), p2 = acc_part(dx), p3 = acc_part(dy);
-    const double p4 = acc_part(d2x), p5 = acc_part(d2y), p6 = acc_part(dxy);
-    if (lane < kNodePart) {
-      sh.part[1][node][lane] = p1; sh.part[2][node][lane] = p2; sh.part[3][node][lane] = p3;
-      sh.part[4][node][lane] = p4; sh.part[5][node][lane] = p5; sh.part[6][node][lane] = p6;
+  // ---- B: cross-correlation at zero shift; caches data x model
+  for (int g = warp; g < groups; g += nw) {
+    const int node = 1 + g * kNodesPerWarp + seg;
+    if (node < numR) {
+      const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
+      Acc<T> val, dx, dy, d2x, d2y, dxy;
+      val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
+      for (int i = c0; i < n; i += kNodePart) {
+        T m;
+        if (i < kNodeCache) {
+          const T mu = T(nc.hre[node][i]);
+          m = P::kMixed ? mu * nn : mu / nn;
+        } else {
+          m = model(i, sfw, nn);
+        }
+        const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
+        if (i < kNodeCache) {
+          nc.hre[node][i] = (double)hre;
+          nc.him[node][i] = (double)him;
+        }
+        const T u = cc * T(gu[i]), v = cc * T(gv[i]);
+        val.add(hre);
+        dx.sub(him * u);
+        dy.sub(him * v);
+        d2x.sub(hre * u * u);
+        d2y.sub(hre * v * v);
+        dxy.sub(hre * u * v);
+      }
+      sh.part[1][node][c0] = acc_value(val); sh.part[2][node][c0] = acc_value(dx);
+      sh.part[3][node][c0] = acc_value(dy); sh.part[4][node][c0] = acc_value(d2x);
+      sh.part[5][node][c0] = acc_value(d2y); sh.part[6][node][c0] = acc_value(dxy);
     }
   }
   __syncthreads();
@@ -880,47 +894,48 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell*
   double Sval = 0, Sdx = 0, Sdy = 0, Sd2x = 0, Sd2y = 0, Sdxy = 0, det = 0;
   double xo = 0, yo = 0, norm = 1, normv = 0;
   int iter = 0;
+  bool pending = true;  // this lane's node had a pass in the last round
   const bool mine = warp == 0 && lane >= 1 && lane < numR;
   const double tol = 1.e-7;
   while (true) {
     if (warp == 0) {
       bool act = false;
-      if (mine) {
+      if (mine && pending) {
         const int node = lane;
-        if (iter == 0 || sh.nactive[node]) {
-          Sval = node_sum(sh.part[1][node]); Sdx = node_sum(sh.part[2][node]); Sdy = node_sum(sh.part[3][node]);
-          Sd2x = node_sum(sh.part[4][node]); Sd2y = node_sum(sh.part[5][node]); Sdxy = node_sum(sh.part[6][node]);
-          det = Sd2x * Sd2y - Sdxy * Sdxy;
-          if (iter > 0) norm = normv;
-          if (det > 0 && norm > tol && iter < kNewtonMax) {
-            iter++;
-            const double incx = (Sdx * Sd2y - Sdy * Sdxy) / det;
-            const double incy = (Sdy * Sd2x - Sdx * Sdxy) / det;
-            xo -= incx;
-            yo -= incy;
-            normv = sqrt(incx * incx + incy * incy);
-            sh.nx[node] = xo;
-            sh.ny[node] = yo;
-            act = true;
-          }
+        Sval = node_sum(sh.part[1][node]); Sdx = node_sum(sh.part[2][node]); Sdy = node_sum(sh.part[3][node]);
+        Sd2x = node_sum(sh.part[4][node]); Sd2y = node_sum(sh.part[5][node]); Sdxy = node_sum(sh.part[6][node]);
+        det = Sd2x * Sd2y - Sdxy * Sdxy;
+        if (iter > 0) norm = normv;
+        if (det > 0 && norm > tol && iter < kNewtonMax) {
+          iter++;
+          const double incx = (Sdx * Sd2y - Sdy * Sdxy) / det;
+          const double incy = (Sdy * Sd2x - Sdx * Sdxy) / det;
+          xo -= incx;
+          yo -= incy;
+          normv = sqrt(incx * incx + incy * incy);
+          sh.nx[node] = xo;
+          sh.ny[node] = yo;
+          act = true;
         }
-        sh.nactive[node] = act;
       }
-      const unsigned any = __ballot_sync(0xffffffffu, act);
-      if (lane == 0) sh.nany = any != 0;
+      pending = act;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act) sh.alist[__popc(am & ((1u << lane) - 1u))] = lane;
+      if (lane == 0) sh.nact = __popc(am);
     }
     __syncthreads();
-    if (!sh.nany) break;
-    for (int node = warp + 1; node < numR; node += nw) {
-      if (!sh.nactive[node]) continue;
+    const int nact = sh.nact;
+    if (!nact) break;
+    const int agroups = (nact + kNodesPerWarp - 1) / kNodesPerWarp;
+    for (int g = warp; g < agroups; g += nw) {
+      const int k = g * kNodesPerWarp + seg;
+      if (k >= nact) continue;
+      const int node = sh.alist[k];
       const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
       const T txo = T(sh.nx[node]), tyo = T(sh.ny[node]);
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
-      for (int i = lane; i < n; i += 32) {
-        const T m = model(node, i, sfw, nn);
-        const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
-        const T u = cc * T(gu[i]), v = cc * T(gv[i]);
+      auto cell = [&](T hre, T him, T u, T v) {
         const T a = txo * u + tyo * v;
         T sa, ca;
         pass_sincos(a, &sa, &ca);
@@ -932,13 +947,16 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell*
         d2x.sub(rp * u * u);
         d2y.sub(rp * v * v);
         dxy.sub(rp * u * v);
+      };
+      int i = c0;
+      for (; i < ncache; i += kNodePart) cell(T(nc.hre[node][i]), T(nc.him[node][i]), T(nc.cu[i]), T(nc.cv[i]));
+      for (; i < n; i += kNodePart) {
+        const T m = model(i, sfw, nn);
+        cell(T(dre[i]) * m, -T(dim[i]) * m, cc * T(gu[i]), cc * T(gv[i]));
       }
-      const double p1 = acc_part(val), p2 = acc_part(dx), p3 = acc_part(dy);
-      const double p4 = acc_part(d2x), p5 = acc_part(d2y), p6 = acc_part(dxy);
-      if (lane < kNodePart) {
-        sh.part[1][node][lane] = p1; sh.part[2][node][lane] = p2; sh.part[3][node][lane] = p3;
-        sh.part[4][node][lane] = p4; sh.part[5][node][lane] = p5; sh.part[6][node][lane] = p6;
-      }
+      sh.part[1][node][c0] = acc_value(val); sh.part[2][node][c0] = acc_value(dx);
+      sh.part[3][node][c0] = acc_value(dy); sh.part[4][node][c0] = acc_value(d2x);
+      sh.part[5][node][c0] = acc_value(d2y); sh.part[6][node][c0] = acc_value(dxy);
     }
     __syncthreads();
   }
@@ -963,7 +981,7 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, const typename P::Cell*
 
 // CTA-collective loglikelihood(e1, e2) (likelihood.c:106-149).
 template <class P>
-__device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typename P::Cell* gu,
+__device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, NodeCache& nc, const typename P::Cell* gu,
                                       const typename P::Cell* gv, const typename P::Cell* dre,
                                       const typename P::Cell* dim, const typename P::Cell* sig2,
                                       int n, typename P::S e1, typename P::S e2, int* error) {
@@ -972,7 +990,7 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typena
   const int nw = blockDim.x >> 5;
   const int numR = c_fit.numr;
   (void)nw;
-  eval_nodes<P>(sh, gu, gv, dre, dim, sig2, n, (double)e1, (double)e2);
+  eval_nodes<P>(sh, nc, gu, gv, dre, dim, sig2, n, (double)e1, (double)e2);
   if (warp == 0) {
     // set_posterior_values (marginalise_r.c:29-64)
     if (lane == 0) {
@@ -1015,6 +1033,7 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, const typena
 template <class P>
 struct FitCtx {
   FitShared<typename P::S>* sh;
+  NodeCache* nc;
   const typename P::Cell *gu, *gv, *dre, *dim, *sig2;
   int n;
   int nevals;
@@ -1026,7 +1045,7 @@ template <class P>
 __device__ __noinline__ typename P::S loglike(FitCtx<P>& c, typename P::S e1, typename P::S e2,
                                               int* error) {
   c.nevals++;
-  const typename P::S L = eval_loglike<P>(*c.sh, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, e1, e2, error);
+  const typename P::S L = eval_loglike<P>(*c.sh, *c.nc, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, e1, e2, error);
   if (c.trace && threadIdx.x == 0 && c.nevals <= c.trace_cap) {
     double* t = c.trace + 4 * (size_t)(c.nevals - 1);
     t[0] = (double)e1; t[1] = (double)e2; t[2] = (double)L; t[3] = (double)*error;
@@ -1329,7 +1348,8 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
   using S = typename P::S;
   __shared__ FitShared<S> sh;
   extern __shared__ __align__(16) unsigned char dyn[];
-  Cell* gu = reinterpret_cast<Cell*>(dyn);
+  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
+  Cell* gu = reinterpret_cast<Cell*>(dyn + sizeof(NodeCache));
   Cell* gv = gu + b.max_cells;
   Cell* dre = gv + b.max_cells;
   Cell* dim = dre + b.max_cells;
@@ -1359,7 +1379,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
-    FitCtx<P> c{&sh, gu, gv, dre, dim, sig2, n, 0,
+    FitCtx<P> c{&sh, &nc, gu, gv, dre, dim, sig2, n, 0,
                 b.trace ? b.trace + (size_t)g * b.trace_cap * 4 : nullptr, b.trace_cap};
     FitOut o = fit_galaxy<P>(c, se1, se2, step, c_fit.np_max);
     __syncthreads();
@@ -1380,13 +1400,15 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_loglike_once(FacetBatch b, d
   using Cell = typename P::Cell;
   using S = typename P::S;
   __shared__ FitShared<S> sh;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
   if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   __syncthreads();
   int err = 0;
-  S L = eval_loglike<P>(sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
+  S L = eval_loglike<P>(sh, nc, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
                         reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
                         reinterpret_cast<const Cell*>(b.sig2), n, S(e1), S(e2), &err);
   if (tid == 0) { out2[0] = (double)L; out2[1] = (double)err; }
@@ -1399,12 +1421,14 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, 
   using Cell = typename P::Cell;
   using S = typename P::S;
   __shared__ FitShared<S> sh;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
   if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   __syncthreads();
-  FitCtx<P> c{&sh, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
+  FitCtx<P> c{&sh, &nc, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
               reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
               reinterpret_cast<const Cell*>(b.sig2), n, 0, b.trace, b.trace_cap};
   S m1 = S(e1), m2 = S(e2), v1, v2, od;
@@ -1491,13 +1515,21 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
 
 template <class P>
 static int fit_launch_t(const FacetBatch& b, int grid, cudaStream_t st) {
-  size_t dyn = (size_t)5 * (b.max_cells > 0 ? b.max_cells : 1) * sizeof(typename P::Cell);
+  const size_t dyn = sizeof(NodeCache) + (size_t)5 * (b.max_cells > 0 ? b.max_cells : 1) * sizeof(typename P::Cell);
+  constexpr size_t kDynMax = 190 * 1024;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_fit<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_fit<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynMax);
     attr_set = true;
   }
-  if (dyn > 160 * 1024) { fprintf(stderr, "rlf: facet too large for the fit kernel\n"); return 1; }
+  if (dyn > kDynMax) { fprintf(stderr, "rlf: facet too large for the fit kernel\n"); return 1; }
+  // persistent CTAs: as many as fit on the GPU with this batch's facet staging
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit<P>, kFitThreads, dyn);
+  if (per < 1) per = 1;
+  if (grid > sms * per) grid = sms * per;
   k_fit<P><<<grid, kFitThreads, dyn, st>>>(b);
   return check("k_fit");
 }
@@ -1510,14 +1542,11 @@ int fit_launch(const FacetBatch& b, Precision p, int grid, cudaStream_t st) {
 }
 
 int fit_max_grid(Precision p) {
+  (void)p;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int per = 1;
-  if (p == kF64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit<PolicyF64>, kFitThreads, 5 * 1156 * 8);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fit<PolicyMixed>, kFitThreads, 5 * 1156 * 4);
-  if (per < 1) per = 1;
-  return sms * per;
+  return sms * kFitMinBlocks;  // fit_launch lowers it to the occupancy of the launch's staging
 }
 
 int launch_loglikelihood_r(double e1, double e2, double scale, int n, const double* variance,
@@ -1531,22 +1560,31 @@ int launch_cross_correlation(int n, const double* gu, const double* gv, const do
   k_xcorr<<<1, 32, 0, st>>>(n, gu, gv, dre, dim, visMod, out3);
   return check("k_xcorr");
 }
+// the single-evaluation kernels take the per-node caches in dynamic shared memory, above the
+// default 48 KB together with their static state
+template <class K>
+static void allow_node_cache(K kernel) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(NodeCache));
+}
 int launch_loglikelihood(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
                          cudaStream_t st) {
-  k_loglike_once<PolicyF64><<<1, kFitThreads, 0, st>>>(b, e1, e2, out2, node_L);
+  allow_node_cache(k_loglike_once<PolicyF64>);
+  k_loglike_once<PolicyF64><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, out2, node_L);
   return check("k_loglike_once");
 }
 int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
                               Precision prec, cudaStream_t st) {
   if (prec == kMixed) {
-    k_loglike_once<PolicyMixed><<<1, kFitThreads, 0, st>>>(b, e1, e2, out2, node_L);
+    allow_node_cache(k_loglike_once<PolicyMixed>);
+    k_loglike_once<PolicyMixed><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, out2, node_L);
     return check("k_loglike_once<mixed>");
   }
   return launch_loglikelihood(b, e1, e2, out2, node_L, st);
 }
 int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
                                double* out5, cudaStream_t st) {
-  k_sampling_once<PolicyF64><<<1, kFitThreads, 0, st>>>(b, e1, e2, maxL, np_max, out5);
+  allow_node_cache(k_sampling_once<PolicyF64>);
+  k_sampling_once<PolicyF64><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, maxL, np_max, out5);
   return check("k_sampling_once");
 }
 int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st) {
