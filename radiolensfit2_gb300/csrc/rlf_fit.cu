@@ -42,9 +42,14 @@ constexpr int kNodePart = 8;       // partials per cross-correlation sum left by
 constexpr int kNodeCache = 64;     // facet cells per node whose model stays in shared memory
 constexpr int kNodeStride = kNodeCache + 8;  // padded row of the per-node caches (bank spread)
 constexpr int kNodesPerWarp = 32 / kNodePart;  // nodes whose cell passes share a warp
-constexpr int kEiTerms = 512;      // reciprocal table of the per-lane Ei series
+constexpr int kEiTab = 101;        // Ei(k) and e^k for k = 0..100 (the position marginal's range)
+constexpr int kEiTerms = 48;       // terms of the per-lane Ei expansions (at most ~26 are used)
+constexpr int kInvTab = 128;       // 1/k for k < kInvTab
 
-__constant__ double c_invk[kEiTerms];  // 1 / k
+__constant__ double c_invk[kInvTab];       // 1 / k
+__constant__ double c_invfact[kEiTerms];   // 1 / k!
+__constant__ double c_ei_tab[kEiTab];      // Ei(k), computed on the host in extended precision
+__constant__ double c_exp_tab[kEiTab];     // e^k
 
 struct FitConst {
   int numr;
@@ -250,6 +255,20 @@ __device__ __forceinline__ S cell_shape(int gaussian, S a1, S a2, S a3, S u, S v
   return S(1) / (den * s_sqrt(den));
 }
 
+// The same model for the fit's cell passes: (1 + q)^(-3/2) as rsqrt(1 + q)^3, one FP64 square-root
+// approximation and two products instead of a square root and a division (a few ulp apart).
+__device__ __forceinline__ double s_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float s_rsqrt(float x) { return rsqrtf(x); }
+template <class S>
+__device__ __forceinline__ S cell_shape_fit(int gaussian, S a1, S a2, S a3, S u, S v, S sfw) {
+  S k1 = a1 * u + a2 * v;
+  S k2 = a2 * u + a3 * v;
+  S q = sfw * (k1 * k1 + k2 * k2);
+  if (gaussian) return s_exp(S(-0.5) * q);
+  const S r = s_rsqrt(S(1) + q);
+  return r * r * r;
+}
+
 // Warp-level likelihood at one scalelength node, likelihood.c:156-187 with the model of
 // galaxy_visibilities.c:59-91 and the cross-correlation of likelihood.c:194-358.
 // Cell arithmetic runs in P::Cell (the per-cell model, products and phase rotations); the six
@@ -400,6 +419,7 @@ struct NodeCache {
   double hre[kMaxNodes][kNodeStride];
   double him[kMaxNodes][kNodeStride];
   double cu[kNodeCache], cv[kNodeCache];  // 2 pi u and 2 pi v of the cells
+  double isg[kNodeCache];                 // 1 / variance of the cells
 };
 
 template <class S>
@@ -407,7 +427,7 @@ struct FitShared {
   // phased node evaluation (eval_nodes): per-node partial sums and state
   double part[7][kMaxNodes][kNodePart];  // 0: model norm; 1..6: val, dx, dy, d2x, d2y, dxy
   double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
-  double nnorm[kMaxNodes];                // the node's model normalisation (F64: norm, mixed: 1/norm)
+  double nnorm[kMaxNodes];                // 1 / the node's model normalisation
   int alist[kMaxNodes];                   // nodes with a Newton pass pending
   int nact;
   // natural spline rows and the factorisation of its matrix for the abscissae fac_x[0..fac_n)
@@ -423,7 +443,6 @@ struct FitShared {
   int g;
   int newton;
   int status;
-  int numvals;
 };
 
 // ------------------------------------------------- scalelength marginalisation
@@ -665,45 +684,46 @@ __device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
 }
 
 // ------------------------------------------------------------ phased nodes
-// Ei(x1) and Ei(x2), x > 0, evaluated by one lane (each lane its own x): for each argument the
-// power series gamma + ln x + sum_k x^k / (k k!) when x <= 40, else the asymptotic series
-// e^x/x sum_k k!/x^k stopped at its smallest term; the reciprocals 1/k come from a table.  The
-// two recurrences run in one loop (independent chains, so their latencies overlap); each keeps
-// its own arithmetic and stopping test.
+// Ei(x1) and Ei(x2), 0 < x <= 100, evaluated by one lane (each lane its own x).
+//   x <= 2.5: the power series  gamma + ln x + sum_k x^k / (k k!)  (at most 26 terms);
+//   x > 2.5: the Taylor expansion about the nearest integer x0 of
+//       Ei(x) = Ei(x0) + e^x0 int_0^s e^t / (x0 + t) dt,   s = x - x0,  |s| <= 1/2,
+//     with e^t / (x0 + t) = sum_n c_n t^n,  c_0 = 1/x0,  c_n = (1/n! - c_(n-1)) / x0  (from
+//     (x0 + t) sum c_n t^n = e^t), so  Ei(x) = Ei(x0) + e^x0 sum_n c_n s^(n+1) / (n+1);  the terms
+//     shrink at least as (1/6)^n.  Ei(x0) and e^x0 come from a table made on the host in extended
+//     precision.
+// Each expansion stops at its first term below 1e-18 of its sum; relative error ~1e-15 against an
+// arbitrary-precision Ei over (0, 100], where the series alone needs up to ~100 terms.  The two
+// recurrences run in one loop (independent chains, so their latencies overlap).
 __device__ __forceinline__ void ei_pair_lane(double x1, double x2, double* e1, double* e2) {
-  const bool ser1 = x1 <= 40.0, ser2 = x2 <= 40.0;
-  const double ix1 = ser1 ? 0.0 : 1.0 / x1, ix2 = ser2 ? 0.0 : 1.0 / x2;
-  double term1 = 1.0, sum1 = ser1 ? 0.0 : 1.0, term2 = 1.0, sum2 = ser2 ? 0.0 : 1.0;
+  const bool ser1 = x1 <= 2.5, ser2 = x2 <= 2.5;
+  const int k1 = ser1 ? 0 : (int)(x1 + 0.5), k2 = ser2 ? 0 : (int)(x2 + 0.5);
+  const double s1 = ser1 ? x1 : x1 - k1, s2 = ser2 ? x2 : x2 - k2;
+  const double i1 = c_invk[k1], i2 = c_invk[k2];
+  // series: c = s^k / k!, term c / k;  Taylor: c = c_k, p = s^(k+1), term c p / (k+1)
+  double c1 = ser1 ? 1.0 : i1, c2 = ser2 ? 1.0 : i2;
+  double p1 = s1, p2 = s2;
+  double a1 = ser1 ? 0.0 : i1 * s1, a2 = ser2 ? 0.0 : i2 * s2;
   bool run1 = true, run2 = true;
-  for (int k = 1; k < kEiTerms && (run1 || run2); ++k) {
-    const double ik = c_invk[k];
+  for (int k = 1; k < kEiTerms - 1 && (run1 || run2); ++k) {
+    const double ik = c_invk[k], ik1 = c_invk[k + 1], ifk = c_invfact[k];
     if (run1) {
-      if (ser1) {
-        term1 = term1 * x1 * ik;
-        const double t = term1 * ik;
-        sum1 += t;
-        if (t < 1e-18 * sum1) run1 = false;
-      } else {
-        const double next = term1 * (double)k * ix1;
-        if (next >= term1 || next < 1e-18 * sum1) run1 = false;
-        else { term1 = next; sum1 += term1; }
-      }
+      double t;
+      if (ser1) { c1 = c1 * s1 * ik; t = c1 * ik; }
+      else { c1 = (ifk - c1) * i1; p1 = p1 * s1; t = c1 * p1 * ik1; }
+      a1 += t;
+      if (fabs(t) < 1e-18 * fabs(a1)) run1 = false;
     }
     if (run2) {
-      if (ser2) {
-        term2 = term2 * x2 * ik;
-        const double t = term2 * ik;
-        sum2 += t;
-        if (t < 1e-18 * sum2) run2 = false;
-      } else {
-        const double next = term2 * (double)k * ix2;
-        if (next >= term2 || next < 1e-18 * sum2) run2 = false;
-        else { term2 = next; sum2 += term2; }
-      }
+      double t;
+      if (ser2) { c2 = c2 * s2 * ik; t = c2 * ik; }
+      else { c2 = (ifk - c2) * i2; p2 = p2 * s2; t = c2 * p2 * ik1; }
+      a2 += t;
+      if (fabs(t) < 1e-18 * fabs(a2)) run2 = false;
     }
   }
-  *e1 = ser1 ? kEulerGamma + log(x1) + sum1 : exp(x1) * ix1 * sum1;
-  *e2 = ser2 ? kEulerGamma + log(x2) + sum2 : exp(x2) * ix2 * sum2;
+  *e1 = ser1 ? kEulerGamma + log(x1) + a1 : c_ei_tab[k1] + c_exp_tab[k1] * a1;
+  *e2 = ser2 ? kEulerGamma + log(x2) + a2 : c_ei_tab[k2] + c_exp_tab[k2] * a2;
 }
 
 // likelihood.c:376-421 for one lane's own x
@@ -822,26 +842,33 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
     const double sc = c_fit.ro[node] * (kPi / 648000.0);
     return T(((sc * sc) / (detA * detA)) * (4 * kPi * kPi));
   };
-  // normalised model of an uncached cell (the reference divides, galaxy_visibilities.c:90)
-  auto model = [&](int i, T sfw, T nn) -> T {
-    const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-    return P::kMixed ? m * nn : m / nn;
+  // normalised model of an uncached cell (galaxy_visibilities.c:90 divides by the norm; the fit
+  // multiplies by its reciprocal)
+  auto model = [&](int i, T sfw, T inn) -> T {
+    return cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw) * inn;
   };
   const int groups = (numR - 1 + kNodesPerWarp - 1) / kNodesPerWarp;
   // ---- A: model and its norm
   for (int i = threadIdx.x; i < ncache; i += blockDim.x) {
     nc.cu[i] = (double)(cc * T(gu[i]));
     nc.cv[i] = (double)(cc * T(gv[i]));
+    nc.isg[i] = (double)(T(1) / T(sig2[i]));
   }
+  __syncthreads();
   for (int g = warp; g < groups; g += nw) {
     const int node = 1 + g * kNodesPerWarp + seg;
     if (node < numR) {
       const T sfw = sfw_of(node);
       Acc<T> acc;
       acc.zero();
-      for (int i = c0; i < n; i += kNodePart) {
-        const T m = cell_shape<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-        if (i < kNodeCache) nc.hre[node][i] = (double)m;
+      int i = c0;
+      for (; i < ncache; i += kNodePart) {
+        const T m = cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
+        nc.hre[node][i] = (double)m;
+        acc.add(m * m * T(nc.isg[i]));
+      }
+      for (; i < n; i += kNodePart) {
+        const T m = cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
         acc.add(m * m / T(sig2[i]));
       }
       sh.part[0][node][c0] = acc_value(acc);
@@ -852,7 +879,7 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
     const int node = lane;
     if (node >= 1 && node < numR) {
       const double s_norm = sqrt(node_sum(sh.part[0][node]));
-      sh.nnorm[node] = P::kMixed ? 1.0 / s_norm : s_norm;
+      sh.nnorm[node] = 1.0 / s_norm;
     }
   }
   __syncthreads();
@@ -864,13 +891,7 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
       for (int i = c0; i < n; i += kNodePart) {
-        T m;
-        if (i < kNodeCache) {
-          const T mu = T(nc.hre[node][i]);
-          m = P::kMixed ? mu * nn : mu / nn;
-        } else {
-          m = model(i, sfw, nn);
-        }
+        const T m = i < kNodeCache ? T(nc.hre[node][i]) * nn : model(i, sfw, nn);
         const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
         if (i < kNodeCache) {
           nc.hre[node][i] = (double)hre;
@@ -992,24 +1013,16 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, NodeCache& n
   (void)nw;
   eval_nodes<P>(sh, nc, gu, gv, dre, dim, sig2, n, (double)e1, (double)e2);
   if (warp == 0) {
-    // set_posterior_values (marginalise_r.c:29-64)
-    if (lane == 0) {
-      int num = 0, nRo = 1;
-      while (nRo < numR && (sh.Lr[nRo] <= S(kBad))) nRo++;
-      if (nRo < numR) {
-        for (nRo = 1; nRo < numR; nRo++) {
-          S lv = sh.Lr[nRo];
-          if (lv > S(kBad)) {
-            sh.xs[num] = S(c_fit.ro[nRo]);
-            sh.ys[num] = lv + sh.rprior[nRo];
-            num++;
-          }
-        }
-      }
-      sh.numvals = num;
+    // set_posterior_values (marginalise_r.c:29-64): the nodes with a likelihood, in node order
+    const bool ok = lane >= 1 && lane < numR && sh.Lr[lane] > S(kBad);
+    const unsigned okm = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      const int pos = __popc(okm & ((1u << lane) - 1u));
+      sh.xs[pos] = S(c_fit.ro[lane]);
+      sh.ys[pos] = sh.Lr[lane] + sh.rprior[lane];
     }
+    const int num = __popc(okm);
     __syncwarp();
-    const int num = sh.numvals;
     S L_e;
     int err = 0;
     if (num > 4) {
@@ -1504,10 +1517,33 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
   for (int i = 0; i < kMaxNodes; ++i) {
     h.ro[i] = (i < cfg.numr) ? cfg.ro[i] : 0.0;
   }
-  static double invk[kEiTerms];
-  for (int k = 0; k < kEiTerms; ++k) invk[k] = k ? 1.0 / k : 0.0;
+  static double invk[kInvTab], invfact[kEiTerms], eitab[kEiTab], exptab[kEiTab];
+  for (int k = 0; k < kInvTab; ++k) invk[k] = k ? 1.0 / k : 0.0;
+  long double f = 1.0L;
+  for (int k = 0; k < kEiTerms; ++k) {
+    if (k) f *= k;
+    invfact[k] = (double)(1.0L / f);
+  }
+  // Ei(k) = gamma + ln k + sum_j k^j / (j j!) and e^k in extended precision (all terms positive)
+  eitab[0] = 0.0;
+  exptab[0] = 1.0;
+  for (int k = 1; k < kEiTab; ++k) {
+    const long double x = k;
+    long double term = 1.0L, sum = 0.0L;
+    for (int j = 1; j < 2000; ++j) {
+      term *= x / j;
+      const long double t = term / j;
+      sum += t;
+      if (t < 1e-30L * sum) break;
+    }
+    eitab[k] = (double)(0.577215664901532860606512090082402431L + logl(x) + sum);
+    exptab[k] = (double)expl(x);
+  }
   cudaError_t e = cudaMemcpyToSymbolAsync(c_fit, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invk, invk, sizeof(invk), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invfact, invfact, sizeof(invfact), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_ei_tab, eitab, sizeof(eitab), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_exp_tab, exptab, sizeof(exptab), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // h is released on return
   if (e != cudaSuccess) { fprintf(stderr, "rlf: fit config: %s\n", cudaGetErrorString(e)); return (int)e; }
   return 0;
