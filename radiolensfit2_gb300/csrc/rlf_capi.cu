@@ -410,6 +410,18 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   RLF_CUDA(cudaMemsetAsync(dout.p, 0, n * sizeof(FitOut), st));
   RLF_OK(dnc.ensure(n));
   RLF_OK(dqueue.ensure(1));
+  // sampling board of the fit launches (rows indexed by the galaxy's place in its unit)
+  DevBuf<SampleSlot> bslot;
+  DevBuf<double> bL;
+  DevBuf<int> berr, bflag, bnewton, bdone;
+  if (!facets_out) {
+    RLF_OK(bslot.ensure(max_unit));
+    RLF_OK(bL.ensure((size_t)max_unit * 2 * kBoardCap));
+    RLF_OK(berr.ensure((size_t)max_unit * 2 * kBoardCap));
+    RLF_OK(bflag.ensure((size_t)max_unit * 2 * kBoardCap));
+    RLF_OK(bnewton.ensure(max_unit));
+    RLF_OK(bdone.ensure(1));
+  }
   if (batched && rounds > 1) {
     RLF_OK(dprev.ensure(std::min(n, max_unit)));
     RLF_OK(dchanged.ensure(1));
@@ -444,7 +456,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fo.ncoords = dnc.p + b0;
     fo.gu = gu; fo.gv = gv; fo.dre = dre; fo.dim = dim; fo.sig2 = sg;
     fo.as_float = fprec == kMixed;
-    FacetBatch fb;
+    FacetBatch fb{};
     fb.n_gal = bn;
     fb.max_cells = max_cells;
     fb.offset = doff.p;
@@ -457,6 +469,14 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     fb.queue = dqueue.p;
     fb.trace = nullptr;
     fb.trace_cap = 0;
+    if (bslot.p) {
+      fb.board.slot = bslot.p;
+      fb.board.L = bL.p;
+      fb.board.err = berr.p;
+      fb.board.flag = bflag.p;
+      fb.board.newton = bnewton.p;
+      fb.board.done_gal = bdone.p;
+    }
     SeqBatch sb{};
     if (u.seq) {
       sb.n_gal = bn;
@@ -517,8 +537,15 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       if (u.seq && rd == nr - 1 && nr > 1)
         RLF_CUDA(cudaMemcpyAsync(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
       RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
+      if (fb.board.slot) {
+        RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bn * sizeof(SampleSlot), st));
+        RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)bn * 2 * kBoardCap * sizeof(int), st));
+        RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)bn * sizeof(int), st));
+        RLF_CUDA(cudaMemsetAsync(bdone.p, 0, sizeof(int), st));
+      }
       ob->stats[RLF_STAT_FITTED] += bn;
-      RLF_OK(fit_launch(fb, fprec, std::min(grid_fit, bn), st));
+      // with the board, CTAs beyond the galaxy count start as helpers of the sampling grids
+      RLF_OK(fit_launch(fb, fprec, fb.board.slot ? grid_fit : std::min(grid_fit, bn), st));
       if (u.seq && rd == nr - 1 && nr > 1) {
         k_count_changed<<<(bn + 127) / 128, 128, 0, st>>>(bn, dprev.p, dout.p + b0, 1e-9, dchanged.p);
         count_launch();
@@ -738,6 +765,7 @@ struct OneFacet {
     fb.queue = nullptr;
     fb.trace = nullptr;
     fb.trace_cap = 0;
+    fb.board = SampleBoard{};
     return 0;
   }
 };

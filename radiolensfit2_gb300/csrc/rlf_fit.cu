@@ -415,10 +415,16 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
 // kNodeCache cells of every node.  Phase A leaves the unnormalised model in hre; phase B replaces
 // it by the real part of data x normalised model and fills him (the model does not change during
 // the Newton search, so the Newton passes read both back and evaluate no model).
+// The FP64 policy keeps the Newton inputs as double-float pairs (f2), the mixed policy as double.
+union CacheSlot {
+  double d;
+  f2 f;
+};
 struct NodeCache {
-  double hre[kMaxNodes][kNodeStride];
-  double him[kMaxNodes][kNodeStride];
+  CacheSlot hre[kMaxNodes][kNodeStride];
+  CacheSlot him[kMaxNodes][kNodeStride];
   double cu[kNodeCache], cv[kNodeCache];  // 2 pi u and 2 pi v of the cells
+  f2 cu2[kNodeCache], cv2[kNodeCache];    // the same as double-float pairs
   double isg[kNodeCache];                 // 1 / variance of the cells
 };
 
@@ -442,6 +448,9 @@ struct FitShared {
   int bcast_err;
   int g;
   int newton;
+  // sampling board: a claimed grid point and its chunk (owner and helper CTAs)
+  SampleSlot claim_prm;
+  int claim_g, claim_seq, claim_idx, claim_state;
   int status;
 };
 
@@ -748,6 +757,9 @@ __device__ __forceinline__ f2 df_add(f2 a, f2 b) {
   s.lo += a.lo + b.lo;
   return quick_two_sum(s.hi, s.lo);
 }
+__device__ __forceinline__ f2 df_neg(f2 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ f2 df_sub(f2 a, f2 b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ double df_to_double(f2 a) { return (double)a.hi + (double)a.lo; }
 // P * y + c
 __device__ __forceinline__ f2 df_horner(f2 P, f2 y, float c_hi, float c_lo) {
   return df_add(df_mul(P, y), f2{c_hi, c_lo});
@@ -758,8 +770,7 @@ __device__ __forceinline__ f2 df_horner(f2 P, f2 y, float c_hi, float c_lo) {
 // float:  sin a = a * sum_k (-1)^k y^k / (2k+1)!,  cos a = sum_k (-1)^k y^k / (2k)!,  y = a^2.
 // Relative error ~1e-14 (double-float carries 48 bits).  About 150 FP32 operations replace the
 // ~40 FP64 ones of sincos(), which at this GPU's FP64 rate cost as much as ~3000 FP32 ones.
-__device__ __forceinline__ void dsincos_small(double a, double* sa, double* ca) {
-  const f2 x = df_from_double(a);
+__device__ __forceinline__ void df_sincos_small(f2 x, f2* sa, f2* ca) {
   const f2 y = df_mul(x, x);
   const float yf = y.hi;
   // sin: tail k = 5..9 in float, k = 0..4 in double-float
@@ -788,8 +799,14 @@ __device__ __forceinline__ void dsincos_small(double a, double* sa, double* ca) 
   Q = df_horner(Q, y, 0.0416666679084301f, -1.2417634698280722e-09f);     // 1/4!
   Q = df_horner(Q, y, -0.5f, 0.f);                                         // -1/2!
   Q = df_horner(Q, y, 1.f, 0.f);
-  *sa = (double)sv.hi + (double)sv.lo;
-  *ca = (double)Q.hi + (double)Q.lo;
+  *sa = sv;
+  *ca = Q;
+}
+__device__ __forceinline__ void dsincos_small(double a, double* sa, double* ca) {
+  f2 s, c;
+  df_sincos_small(df_from_double(a), &s, &c);
+  *sa = df_to_double(s);
+  *ca = df_to_double(c);
 }
 __device__ __forceinline__ void pass_sincos(double a, double* sa, double* ca) {
   if (fabs(a) <= 0.78539816339744831) dsincos_small(a, sa, ca);
@@ -852,6 +869,8 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
   for (int i = threadIdx.x; i < ncache; i += blockDim.x) {
     nc.cu[i] = (double)(cc * T(gu[i]));
     nc.cv[i] = (double)(cc * T(gv[i]));
+    nc.cu2[i] = df_from_double(nc.cu[i]);
+    nc.cv2[i] = df_from_double(nc.cv[i]);
     nc.isg[i] = (double)(T(1) / T(sig2[i]));
   }
   __syncthreads();
@@ -864,7 +883,7 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       int i = c0;
       for (; i < ncache; i += kNodePart) {
         const T m = cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-        nc.hre[node][i] = (double)m;
+        nc.hre[node][i].d = (double)m;
         acc.add(m * m * T(nc.isg[i]));
       }
       for (; i < n; i += kNodePart) {
@@ -891,11 +910,16 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
       for (int i = c0; i < n; i += kNodePart) {
-        const T m = i < kNodeCache ? T(nc.hre[node][i]) * nn : model(i, sfw, nn);
+        const T m = i < kNodeCache ? T(nc.hre[node][i].d) * nn : model(i, sfw, nn);
         const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
         if (i < kNodeCache) {
-          nc.hre[node][i] = (double)hre;
-          nc.him[node][i] = (double)him;
+          if constexpr (P::kMixed) {
+            nc.hre[node][i].d = (double)hre;
+            nc.him[node][i].d = (double)him;
+          } else {
+            nc.hre[node][i].f = df_from_double(hre);
+            nc.him[node][i].f = df_from_double(him);
+          }
         }
         const T u = cc * T(gu[i]), v = cc * T(gv[i]);
         val.add(hre);
@@ -953,6 +977,44 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       if (k >= nact) continue;
       const int node = sh.alist[k];
       const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
+      if constexpr (!P::kMixed) {
+        // FP64 policy: the Newton pass in double-float (FP32 pairs, ~48-bit significands): phase,
+        // sin/cos, rotation and the six sums stay on the FP32 pipes
+        const f2 xo2 = df_from_double(sh.nx[node]), yo2 = df_from_double(sh.ny[node]);
+        f2 val{0.f, 0.f}, dx{0.f, 0.f}, dy{0.f, 0.f}, d2x{0.f, 0.f}, d2y{0.f, 0.f}, dxy{0.f, 0.f};
+        auto cell = [&](f2 hre, f2 him, f2 u, f2 v) {
+          const f2 a = df_add(df_mul(xo2, u), df_mul(yo2, v));
+          f2 sa, ca;
+          if (fabsf(a.hi) <= 0.785398f) {
+            df_sincos_small(a, &sa, &ca);
+          } else {
+            double s8, c8;
+            sincos(df_to_double(a), &s8, &c8);
+            sa = df_from_double(s8);
+            ca = df_from_double(c8);
+          }
+          const f2 rp = df_sub(df_mul(hre, ca), df_mul(him, sa));
+          const f2 ip = df_add(df_mul(hre, sa), df_mul(him, ca));
+          val = df_add(val, rp);
+          dx = df_sub(dx, df_mul(ip, u));
+          dy = df_sub(dy, df_mul(ip, v));
+          const f2 ru = df_mul(rp, u), rv = df_mul(rp, v);
+          d2x = df_sub(d2x, df_mul(ru, u));
+          d2y = df_sub(d2y, df_mul(rv, v));
+          dxy = df_sub(dxy, df_mul(ru, v));
+        };
+        int i = c0;
+        for (; i < ncache; i += kNodePart) cell(nc.hre[node][i].f, nc.him[node][i].f, nc.cu2[i], nc.cv2[i]);
+        for (; i < n; i += kNodePart) {
+          const T m = model(i, sfw, nn);
+          cell(df_from_double(T(dre[i]) * m), df_from_double(-T(dim[i]) * m), df_from_double(cc * T(gu[i])),
+               df_from_double(cc * T(gv[i])));
+        }
+        sh.part[1][node][c0] = df_to_double(val); sh.part[2][node][c0] = df_to_double(dx);
+        sh.part[3][node][c0] = df_to_double(dy); sh.part[4][node][c0] = df_to_double(d2x);
+        sh.part[5][node][c0] = df_to_double(d2y); sh.part[6][node][c0] = df_to_double(dxy);
+        continue;
+      }
       const T txo = T(sh.nx[node]), tyo = T(sh.ny[node]);
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
@@ -970,7 +1032,7 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
         dxy.sub(rp * u * v);
       };
       int i = c0;
-      for (; i < ncache; i += kNodePart) cell(T(nc.hre[node][i]), T(nc.him[node][i]), T(nc.cu[i]), T(nc.cv[i]));
+      for (; i < ncache; i += kNodePart) cell(T(nc.hre[node][i].d), T(nc.him[node][i].d), T(nc.cu[i]), T(nc.cv[i]));
       for (; i < n; i += kNodePart) {
         const T m = model(i, sfw, nn);
         cell(T(dre[i]) * m, -T(dim[i]) * m, cc * T(gu[i]), cc * T(gv[i]));
@@ -1052,7 +1114,110 @@ struct FitCtx {
   int nevals;
   double* trace;   // optional evaluation record (thread 0 writes)
   int trace_cap;
+  SampleBoard board;  // slot == nullptr: the sampling grid is evaluated by this CTA alone
+  int g;              // the galaxy's index in the batch (board rows)
+  int seq;            // chunks published so far
 };
+
+// ------------------------------------------------------------ sampling board
+constexpr unsigned long long kBoardWaitNs = 2000000000ull;  // wait limit of owners and idle helpers
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ size_t board_row(int g, int seq) { return ((size_t)g * 2 + (seq & 1)) * kBoardCap; }
+
+// a chunk's parameters as the owner published them (read after the claim, behind a fence)
+__device__ __forceinline__ SampleSlot board_params(const SampleSlot* sl) {
+  const volatile SampleSlot* v = sl;
+  SampleSlot q;
+  q.claim = 0;
+  q.npts = v->npts; q.p0 = v->p0; q.lo1 = v->lo1; q.lo2 = v->lo2; q.n2 = v->n2;
+  q.sampling = v->sampling; q.me1 = v->me1; q.me2 = v->me2; q.pad = 0;
+  return q;
+}
+
+// Grid point idx of a published chunk (likelihood.c:507-514): evaluates the log-likelihood unless
+// the point is the centre or outside |e| < 1 (err = -1), and publishes the result (thread 0 writes
+// value, then the chunk sequence as the point's flag).  CTA-collective.
+template <class P>
+__device__ void board_point(FitShared<typename P::S>& sh, NodeCache& nc, const typename P::Cell* gu,
+                            const typename P::Cell* gv, const typename P::Cell* dre, const typename P::Cell* dim,
+                            const typename P::Cell* sig2, int n, const SampleBoard& bd, int g, int seq, int idx,
+                            const SampleSlot& prm, int newton_before);
+
+template <class P>
+__device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, NodeCache& nc, const typename P::Cell* gu,
+                                      const typename P::Cell* gv, const typename P::Cell* dre,
+                                      const typename P::Cell* dim, const typename P::Cell* sig2,
+                                      int n, typename P::S e1, typename P::S e2, int* error);
+
+template <class P>
+__device__ void board_point(FitShared<typename P::S>& sh, NodeCache& nc, const typename P::Cell* gu,
+                            const typename P::Cell* gv, const typename P::Cell* dre, const typename P::Cell* dim,
+                            const typename P::Cell* sig2, int n, const SampleBoard& bd, int g, int seq, int idx,
+                            const SampleSlot& prm, int newton_before) {
+  using S = typename P::S;
+  const int p = prm.p0 + idx;
+  const int ie1 = prm.lo1 + 2 * (p / prm.n2), ie2 = prm.lo2 + 2 * (p % prm.n2);
+  const S x_e1 = S(prm.me1) + ie1 * prm.sampling;
+  const S x_e2 = S(prm.me2) + ie2 * prm.sampling;
+  const S mod2 = x_e1 * x_e1 + x_e2 * x_e2;
+  int err = -1;
+  S L = S(0);
+  if ((ie1 != 0 || ie2 != 0) && mod2 < S(1)) L = eval_loglike<P>(sh, nc, gu, gv, dre, dim, sig2, n, x_e1, x_e2, &err);
+  if (threadIdx.x == 0) {
+    const size_t o = board_row(g, seq) + idx;
+    bd.L[o] = (double)L;
+    bd.err[o] = err;
+    if (newton_before >= 0) atomicAdd(&bd.newton[g], sh.newton - newton_before);
+    __threadfence();
+    atomicExch(&bd.flag[o], seq);
+  }
+}
+
+// Owner side of one chunk: publish it, evaluate points until all are claimed, then wait (bounded)
+// for the helpers' results.  CTA-collective; returns with the results visible to every thread.
+template <class P>
+__device__ void board_chunk(FitCtx<P>& c, int seq, const SampleSlot& prm) {
+  FitShared<typename P::S>& sh = *c.sh;
+  const SampleBoard& bd = c.board;
+  SampleSlot* sl = bd.slot + c.g;
+  if (threadIdx.x == 0) {
+    volatile SampleSlot* v = sl;
+    v->npts = prm.npts; v->p0 = prm.p0; v->lo1 = prm.lo1; v->lo2 = prm.lo2; v->n2 = prm.n2;
+    v->sampling = prm.sampling; v->me1 = prm.me1; v->me2 = prm.me2;
+    __threadfence();
+    atomicExch(&sl->claim, (unsigned long long)seq << 32);
+  }
+  while (true) {
+    if (threadIdx.x == 0) sh.claim_idx = (int)(atomicAdd(&sl->claim, 1ull) & 0xffffffffull);
+    __syncthreads();
+    const int idx = sh.claim_idx;
+    if (idx >= prm.npts) break;
+    board_point<P>(sh, *c.nc, c.gu, c.gv, c.dre, c.dim, c.sig2, c.n, bd, c.g, seq, idx, prm, -1);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const size_t row = board_row(c.g, seq);
+    const unsigned long long t0 = global_ns();
+    for (int k = 0; k < prm.npts; ++k) {
+      const volatile int* f = bd.flag + row + k;
+      while (*f != seq) {
+        if (global_ns() - t0 > kBoardWaitNs) break;
+        __nanosleep(200);
+      }
+      if (*f != seq) {  // a helper did not deliver within the limit: the point counts as an error
+        bd.err[row + k] = 1;
+        sh.status |= 8;
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
 
 template <class P>
 __device__ __noinline__ typename P::S loglike(FitCtx<P>& c, typename P::S e1, typename P::S e2,
@@ -1256,26 +1421,70 @@ __device__ __noinline__ void likelihood_sampling(FitCtx<P>& c, typename P::S* me
     // converted to int, last index while (float)ie <= start/sampling
     const float q1 = start1 / sampling, q2 = start2 / sampling;
     const int lo1 = (int)(-start1 / sampling), lo2 = (int)(-start2 / sampling);
-    for (ie1 = lo1; (float)ie1 <= q1; ie1 += 2) {
-      for (ie2 = lo2; (float)ie2 <= q2; ie2 += 2) {
-        if (ie1 != 0 || ie2 != 0) {
+    if (c.board.slot) {
+      // the same points in the same order, evaluated through the sampling board
+      int n1 = 0, n2 = 0;
+      for (ie1 = lo1; (float)ie1 <= q1; ie1 += 2) n1++;
+      for (ie2 = lo2; (float)ie2 <= q2; ie2 += 2) n2++;
+      const int total = n1 * n2;
+      for (int p0 = 0; p0 < total; p0 += kBoardCap) {
+        SampleSlot prm;
+        prm.claim = 0; prm.pad = 0;
+        prm.npts = min(kBoardCap, total - p0);
+        prm.p0 = p0; prm.lo1 = lo1; prm.lo2 = lo2; prm.n2 = n2;
+        prm.sampling = sampling; prm.me1 = (double)max_e1; prm.me2 = (double)max_e2;
+        c.seq++;
+        board_chunk<P>(c, c.seq, prm);
+        const size_t row = board_row(c.g, c.seq);
+        for (int k = 0; k < prm.npts; ++k) {
+          const int e = c.board.err[row + k];
+          if (e < 0) continue;
+          const int p = p0 + k;
+          ie1 = lo1 + 2 * (p / n2);
+          ie2 = lo2 + 2 * (p % n2);
           x_e1 = max_e1 + ie1 * sampling;
           x_e2 = max_e2 + ie2 * sampling;
-          mod2 = x_e1 * x_e1 + x_e2 * x_e2;
-          if (mod2 < S(1)) {
-            L_e = loglike<P>(c, x_e1, x_e2, &error);
-            if (!error) {
-              L = s_exp(L_e - maxL);
-              if (L >= threshold && !isinf(L)) {
-                np++;
-                xL1 = x_e1 * L;
-                xL2 = x_e2 * L;
-                average_1 += xL1;
-                average_2 += xL2;
-                var1 += x_e1 * xL1;
-                var2 += x_e2 * xL2;
-                cov += x_e1 * xL2;
-                totL += L;
+          c.nevals++;
+          error = e;
+          if (!error) {
+            L_e = S(c.board.L[row + k]);
+            L = s_exp(L_e - maxL);
+            if (L >= threshold && !isinf(L)) {
+              np++;
+              xL1 = x_e1 * L;
+              xL2 = x_e2 * L;
+              average_1 += xL1;
+              average_2 += xL2;
+              var1 += x_e1 * xL1;
+              var2 += x_e2 * xL2;
+              cov += x_e1 * xL2;
+              totL += L;
+            }
+          }
+        }
+      }
+    } else {
+      for (ie1 = lo1; (float)ie1 <= q1; ie1 += 2) {
+        for (ie2 = lo2; (float)ie2 <= q2; ie2 += 2) {
+          if (ie1 != 0 || ie2 != 0) {
+            x_e1 = max_e1 + ie1 * sampling;
+            x_e2 = max_e2 + ie2 * sampling;
+            mod2 = x_e1 * x_e1 + x_e2 * x_e2;
+            if (mod2 < S(1)) {
+              L_e = loglike<P>(c, x_e1, x_e2, &error);
+              if (!error) {
+                L = s_exp(L_e - maxL);
+                if (L >= threshold && !isinf(L)) {
+                  np++;
+                  xL1 = x_e1 * L;
+                  xL2 = x_e2 * L;
+                  average_1 += xL1;
+                  average_2 += xL2;
+                  var1 += x_e1 * xL1;
+                  var2 += x_e2 * xL2;
+                  cov += x_e1 * xL2;
+                  totL += L;
+                }
               }
             }
           }
@@ -1355,11 +1564,102 @@ __device__ __forceinline__ size_t cells_smem_bytes(int max_cells) {
   return (size_t)5 * max_cells * sizeof(typename P::Cell);
 }
 
+// galaxy g's facet cells into the CTA's shared memory and its scalelength prior into sh.rprior;
+// returns the number of cells
+template <class P>
+__device__ int stage_galaxy(const FacetBatch& b, int g, typename P::Cell* gu, typename P::Cell* gv,
+                            typename P::Cell* dre, typename P::Cell* dim, typename P::Cell* sig2,
+                            FitShared<typename P::S>& sh) {
+  using Cell = typename P::Cell;
+  using S = typename P::S;
+  const int off = b.offset[g];
+  const int n = b.count[g];
+  const Cell* Gu = reinterpret_cast<const Cell*>(b.gu) + off;
+  const Cell* Gv = reinterpret_cast<const Cell*>(b.gv) + off;
+  const Cell* Dr = reinterpret_cast<const Cell*>(b.dre) + off;
+  const Cell* Di = reinterpret_cast<const Cell*>(b.dim) + off;
+  const Cell* Sg = reinterpret_cast<const Cell*>(b.sig2) + off;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    gu[i] = Gu[i]; gv[i] = Gv[i]; dre[i] = Dr[i]; dim[i] = Di[i]; sig2[i] = Sg[i];
+  }
+  for (int i = threadIdx.x; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[(size_t)g * kMaxNodes + i]);
+  return n;
+}
+
+// Helper side of the sampling board, run by a CTA once the galaxy queue is empty: warp 0 scans
+// the slots of the launch for a chunk with unclaimed points and claims one; the CTA evaluates it
+// with the galaxy's cells staged in its own shared memory.  Returns when every galaxy of the
+// launch is finished, or after kBoardWaitNs without finding work.
+template <class P>
+__device__ void board_help(const FacetBatch& b, FitShared<typename P::S>& sh, NodeCache& nc,
+                           typename P::Cell* gu, typename P::Cell* gv, typename P::Cell* dre,
+                           typename P::Cell* dim, typename P::Cell* sig2) {
+  const SampleBoard& bd = b.board;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int staged = -1, n = 0;
+  unsigned long long idle0 = global_ns();
+  while (true) {
+    if (warp == 0) {
+      int state = 0;
+      while (state == 0) {
+        if (*(volatile int*)bd.done_gal >= b.n_gal) { state = -1; break; }
+        for (int base = 0; base < b.n_gal && state == 0; base += 32) {
+          const int gg = (int)((blockIdx.x + (unsigned)base + lane) % (unsigned)b.n_gal);
+          bool cand = false;
+          if (base + lane < b.n_gal) {
+            const unsigned long long w = *(volatile unsigned long long*)&bd.slot[gg].claim;
+            const int npts = *(volatile int*)&bd.slot[gg].npts;
+            cand = (w >> 32) != 0 && (int)(w & 0xffffffffull) < npts;
+          }
+          unsigned m = __ballot_sync(0xffffffffu, cand);
+          while (m && state == 0) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            int got = 0;
+            if (lane == src) {
+              const unsigned long long w = atomicAdd(&bd.slot[gg].claim, 1ull);
+              __threadfence();
+              const SampleSlot prm = board_params(&bd.slot[gg]);
+              const int idx = (int)(w & 0xffffffffull);
+              if (idx < prm.npts) {
+                sh.claim_prm = prm;
+                sh.claim_g = gg;
+                sh.claim_seq = (int)(w >> 32);
+                sh.claim_idx = idx;
+                got = 1;
+              }
+            }
+            if (__shfl_sync(0xffffffffu, got, src)) state = 1;
+          }
+        }
+        if (state == 0) {
+          if (global_ns() - idle0 > kBoardWaitNs) state = -1;
+          else __nanosleep(1000);
+        }
+      }
+      if (lane == 0) sh.claim_state = state;
+    }
+    __syncthreads();
+    if (sh.claim_state < 0) return;
+    const int gg = sh.claim_g;
+    if (gg != staged) {
+      n = stage_galaxy<P>(b, gg, gu, gv, dre, dim, sig2, sh);
+      staged = gg;
+    }
+    const SampleSlot prm = sh.claim_prm;
+    const int seq = sh.claim_seq, idx = sh.claim_idx;
+    const int before = sh.newton;
+    __syncthreads();
+    board_point<P>(sh, nc, gu, gv, dre, dim, sig2, n, bd, gg, seq, idx, prm, before);
+    idle0 = global_ns();
+    __syncthreads();
+  }
+}
+
 template <class P>
 __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b) {
   using Cell = typename P::Cell;
-  using S = typename P::S;
-  __shared__ FitShared<S> sh;
+  __shared__ FitShared<typename P::S> sh;
   extern __shared__ __align__(16) unsigned char dyn[];
   NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
   Cell* gu = reinterpret_cast<Cell*>(dyn + sizeof(NodeCache));
@@ -1368,42 +1668,39 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
   Cell* dim = dre + b.max_cells;
   Cell* sig2 = dim + b.max_cells;
   const int tid = threadIdx.x;
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   while (true) {
     if (tid == 0) sh.g = atomicAdd(b.queue, 1);
     __syncthreads();
     const int g = sh.g;
     if (g >= b.n_gal) break;
     if (b.active && !b.active[g]) {
+      if (tid == 0 && b.board.slot) atomicAdd(b.board.done_gal, 1);
       __syncthreads();
       continue;
     }
-    const int off = b.offset[g];
-    const int n = b.count[g];
-    const Cell* Gu = reinterpret_cast<const Cell*>(b.gu) + off;
-    const Cell* Gv = reinterpret_cast<const Cell*>(b.gv) + off;
-    const Cell* Dr = reinterpret_cast<const Cell*>(b.dre) + off;
-    const Cell* Di = reinterpret_cast<const Cell*>(b.dim) + off;
-    const Cell* Sg = reinterpret_cast<const Cell*>(b.sig2) + off;
-    for (int i = tid; i < n; i += blockDim.x) {
-      gu[i] = Gu[i]; gv[i] = Gv[i]; dre[i] = Dr[i]; dim[i] = Di[i]; sig2[i] = Sg[i];
-    }
-    for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[(size_t)g * kMaxNodes + i]);
-    if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
+    const int n = stage_galaxy<P>(b, g, gu, gv, dre, dim, sig2, sh);
+    if (tid == 0) { sh.newton = 0; sh.status = 0; }
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
     FitCtx<P> c{&sh, &nc, gu, gv, dre, dim, sig2, n, 0,
-                b.trace ? b.trace + (size_t)g * b.trace_cap * 4 : nullptr, b.trace_cap};
+                b.trace ? b.trace + (size_t)g * b.trace_cap * 4 : nullptr, b.trace_cap, b.board, g, 0};
     FitOut o = fit_galaxy<P>(c, se1, se2, step, c_fit.np_max);
     __syncthreads();
     if (tid == 0) {
-      o.newton_iters = sh.newton;
+      o.newton_iters = sh.newton + (b.board.slot ? *(volatile int*)&b.board.newton[g] : 0);
       o.status |= sh.status;
       o.ncoords = n;
       b.out[g] = o;
+      if (b.board.slot) {
+        __threadfence();
+        atomicAdd(b.board.done_gal, 1);
+      }
     }
     __syncthreads();
   }
+  if (b.board.slot) board_help<P>(b, sh, nc, gu, gv, dre, dim, sig2);
 }
 
 // one loglikelihood evaluation of galaxy 0 of the batch (C entry point loglikelihood)
@@ -1572,7 +1869,7 @@ static int fit_launch_t(const FacetBatch& b, int grid, cudaStream_t st) {
 
 int fit_launch(const FacetBatch& b, Precision p, int grid, cudaStream_t st) {
   if (b.n_gal <= 0) return 0;
-  if (grid > b.n_gal) grid = b.n_gal;
+  if (!b.board.slot && grid > b.n_gal) grid = b.n_gal;
   if (grid < 1) grid = 1;
   return p == kF64 ? fit_launch_t<PolicyF64>(b, grid, st) : fit_launch_t<PolicyMixed>(b, grid, st);
 }

@@ -19,6 +19,31 @@ struct FitOut {
 
 enum Precision { kF64 = 0, kMixed = 1 };
 
+// Sampling board of one fit launch.  The grid of the likelihood sampling (likelihood.c:502-532)
+// holds independent evaluations; the CTA fitting a galaxy publishes them a chunk at a time, and
+// CTAs whose galaxy queue is empty claim points and evaluate them (the bright galaxies with a
+// narrow posterior need hundreds of grid points and would otherwise hold a launch alone).  The
+// owner accumulates the results in the reference's loop order, so the outcome does not depend on
+// which CTA evaluated a point.  Results are double-buffered by the chunk sequence's parity.
+constexpr int kBoardCap = 512;  // points per published chunk
+struct SampleSlot {
+  unsigned long long claim;     // (chunk sequence << 32) | next point index
+  int npts;                     // points in the chunk
+  int p0;                       // index of the chunk's first point in its grid level
+  int lo1, lo2, n2;             // grid: ie1 = lo1 + 2 (p / n2), ie2 = lo2 + 2 (p % n2)
+  float sampling;
+  double me1, me2;              // grid centre
+  unsigned long long pad;
+};
+struct SampleBoard {
+  SampleSlot* slot;             // [n_gal]
+  double* L;                    // [n_gal][2][kBoardCap] log-likelihood of each point
+  int* err;                     // [n_gal][2][kBoardCap] error flag; -1: point outside the grid's domain
+  int* flag;                    // [n_gal][2][kBoardCap] sequence of the chunk the result belongs to
+  int* newton;                  // [n_gal] Newton iterations of the helpers' evaluations
+  int* done_gal;                // galaxies finished in this launch
+};
+
 // A batch of facets packed back to back.  Cell arrays hold either double (kF64) or float
 // (kMixed) values; rprior and start are always double.
 struct FacetBatch {
@@ -38,6 +63,7 @@ struct FacetBatch {
   int* queue;              // work counter, zeroed before launch
   double* trace;           // optional [n_gal][trace_cap][4]: (e1, e2, L, error) per evaluation
   int trace_cap;
+  SampleBoard board;       // sampling board (slot == nullptr: each CTA samples its galaxy alone)
 };
 
 struct FitConfigHost {
