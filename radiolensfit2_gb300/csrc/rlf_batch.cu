@@ -22,8 +22,24 @@ namespace rlf {
 struct BatchChan {
   float spec;      // spectral factor
   float wn2;       // wavenumber^2
+  float dl;        // wn2 / wn2 at the centre of the channel's 16-channel chunk - 1
+  float pad;
 };
+// A galaxy profile P(x), x = scale factor * wn2 * (u^2 + v^2), across the channels of a 16-channel
+// chunk is P(x_c (1 + dl)) with x_c at the chunk's centre and |dl| below ~1% for the usual
+// channelisations; there it is the cubic  sum_j cf_j dl^j  (profile_poly) to ~1e-9 of the peak, and
+// sums over the chunk's channels weighted by the spectral factors reduce to the moments
+// M_j = sum_k spec_k dl_k^j.  c_chunk_poly is set when every chunk is within that range.
+struct BatchChunk {
+  float wn2c;      // wn2 at the chunk's centre
+  float mom[4];    // M_0 .. M_3
+  float pad[3];
+};
+constexpr int kChunks = kMaxCh / 16;
 __constant__ BatchChan c_bch[kMaxCh];
+__constant__ BatchChunk c_chunk[kChunks];
+__constant__ int c_chunk_poly;
+static int g_chunk_poly[64];  // host copy of c_chunk_poly per device (selects the kernel variant)
 __constant__ float c_il0_hi, c_il0_lo, c_dil_hi, c_dil_lo;  // inv_lambda(0) and its channel step
 __constant__ int c_bnch;
 
@@ -52,10 +68,36 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   }
   if (worst * max_delay_m > 1e-9) return -1;
   static BatchChan h[kMaxCh];
-  for (int c = 0; c < n_ch; ++c) {
-    h[c].spec = (float)spec[c];
-    h[c].wn2 = (float)(wavenumbers[c] * wavenumbers[c]);
+  static BatchChunk hc[kChunks];
+  double dmax = 0.0;
+  for (int c0 = 0; c0 < n_ch; c0 += 16) {
+    const int c1 = std::min(n_ch, c0 + 16);
+    double lo = 1e300, hi = -1e300;
+    for (int c = c0; c < c1; ++c) {
+      const double w2 = wavenumbers[c] * wavenumbers[c];
+      lo = std::min(lo, w2);
+      hi = std::max(hi, w2);
+    }
+    const double wc = 0.5 * (lo + hi);
+    double mom[4] = {0, 0, 0, 0};
+    for (int c = c0; c < c1; ++c) {
+      const double d = wavenumbers[c] * wavenumbers[c] / wc - 1.0;
+      dmax = std::max(dmax, fabs(d));
+      h[c].spec = (float)spec[c];
+      h[c].wn2 = (float)(wavenumbers[c] * wavenumbers[c]);
+      h[c].dl = (float)d;
+      h[c].pad = 0.f;
+      double dp = 1.0;
+      for (int j = 0; j < 4; ++j) { mom[j] += spec[c] * dp; dp *= d; }
+    }
+    BatchChunk& k = hc[c0 / 16];
+    k.wn2c = (float)wc;
+    for (int j = 0; j < 4; ++j) k.mom[j] = (float)mom[j];
+    k.pad[0] = k.pad[1] = k.pad[2] = 0.f;
   }
+  // truncation of the cubic: below 2.5 dl^4 of the peak (exponential profile; less for the
+  // Gaussian one over the range where it is not negligible)
+  const int poly = 2.5 * dmax * dmax * dmax * dmax <= 1e-8 ? 1 : 0;
   const float il0_hi = (float)il0, il0_lo = (float)(il0 - (double)il0_hi);
   const float dil_hi = (float)dil, dil_lo = (float)(dil - (double)dil_hi);
   cudaError_t e = cudaMemcpyToSymbolAsync(c_bch, h, sizeof(BatchChan) * n_ch, 0, cudaMemcpyHostToDevice, st);
@@ -64,6 +106,11 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_dil_hi, &dil_hi, 4, 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_dil_lo, &dil_lo, 4, 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_bnch, &n_ch, 4, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk, hc, sizeof(BatchChunk) * ((n_ch + 15) / 16), 0,
+                                                     cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_poly, &poly, 4, 0, cudaMemcpyHostToDevice, st);
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) g_chunk_poly[dev] = poly;
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: batch channels: %s\n", cudaGetErrorString(e)); return (int)e; }
   return 0;
@@ -286,8 +333,31 @@ __device__ __forceinline__ float profile(float x, int gauss) {
   return gauss ? __expf(-0.5f * x) : round_shape(x);
 }
 
+// P(x_c (1 + dl)) = cf0 + cf1 dl + cf2 dl^2 + cf3 dl^3 around the chunk centre x_c: the exponential
+// profile (1 + x)^(-3/2) = P_c (1 + r dl)^(-3/2), r = x_c / (1 + x_c), from the binomial series;
+// the Gaussian exp(-x/2) = P_c exp(-(x_c/2) dl) from the exponential series.
+template <int GAUSS>
+__device__ __forceinline__ void profile_poly(float xc, float cf[4]) {
+  if (GAUSS) {
+    const float h = -0.5f * xc;
+    cf[0] = __expf(h);
+    cf[1] = cf[0] * h;
+    cf[2] = cf[1] * h * 0.5f;
+    cf[3] = cf[2] * h * (1.f / 3.f);
+  } else {
+    const float y = rsqrtf(1.f + xc);
+    const float P = y * y * y, r = xc * y * y;
+    cf[0] = P;
+    cf[1] = -1.5f * P * r;
+    cf[2] = 1.875f * P * r * r;
+    cf[3] = -2.1875f * P * r * r * r;
+  }
+}
+__device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(fmaf(fmaf(c[3], d, c[2]), d, c[1]), d, c[0]); }
+
 // one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order
-template <int GAUSS, bool SIMPLE>
+// (POLY: the profiles from the chunk polynomial, one profile evaluation per galaxy and chunk)
+template <int GAUSS, bool SIMPLE, bool POLY>
 __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
@@ -328,6 +398,18 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
     float2* fac = acc + s.off;
     // fitted model: |k'|^2 = A u^2 + B uv + C v^2 (sheared), as a factor on wn^2 (u^2 + v^2)
     const float f1 = s.apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
+    // chunk polynomials of the round model (c0p) and of flux * (fitted - round) (dfp)
+    float c0p[4], dfp[4];
+    if (POLY) {
+      const float xq = c_chunk[c0 / kChunk].wn2c * rw.q;
+      profile_poly<GAUSS>(g.sf0 * xq, c0p);
+      if (s.apply) {
+        float c1p[4];
+        profile_poly<GAUSS>(f1 * xq, c1p);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dfp[j] = g.flux * (c1p[j] - c0p[j]);
+      }
+    }
     if (SIMPLE) {
       // one run: all 16 channels valid and in the cell d & 0xffff
       float cr, ci;
@@ -339,10 +421,32 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
           const float ni_ = fmaf(sr, wi, fmaf(si, wr, pi[k]));
           sr = nr_;
           si = ni_;
-          rs = fmaf(profile(g.sf0 * XB(k), GAUSS), c_bch[c0 + k].spec, rs);
+          if (!POLY) rs = fmaf(profile(g.sf0 * XB(k), GAUSS), c_bch[c0 + k].spec, rs);
+        }
+        if (POLY) {
+          const BatchChunk& ck = c_chunk[c0 / kChunk];
+          rs = fmaf(c0p[3], ck.mom[3], fmaf(c0p[2], ck.mom[2], fmaf(c0p[1], ck.mom[1], c0p[0] * ck.mom[0])));
         }
         cr = fmaf(sr, zr0, fmaf(-si, zi0, rs * g.flux));
         ci = fmaf(sr, zi0, si * zr0);
+      } else if (POLY) {
+        float ar = 0.f, ai = 0.f, zr = zr0, zi = zi0;
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+          ar = fmaf(pr[k], zr, fmaf(-pi[k], zi, ar));
+          ai = fmaf(pr[k], zi, fmaf(pi[k], zr, ai));
+          const float a = c_bch[c0 + k].spec * poly3(dfp, c_bch[c0 + k].dl);
+          pr[k] = fmaf(-a, zr, pr[k]);
+          pi[k] = fmaf(a, zi, pi[k]);
+          const float nzr = fmaf(zr, wr, -zi * wi);
+          const float nzi = fmaf(zr, wi, zi * wr);
+          zr = nzr;
+          zi = nzi;
+        }
+        const BatchChunk& ck = c_chunk[c0 / kChunk];
+        const float rs = fmaf(c0p[3], ck.mom[3], fmaf(c0p[2], ck.mom[2], fmaf(c0p[1], ck.mom[1], c0p[0] * ck.mom[0])));
+        cr = fmaf(rs, g.flux, ar);
+        ci = ai;
       } else {
         float ar = 0.f, ai = 0.f, rs = 0.f, zr = zr0, zi = zi0;
 #pragma unroll
@@ -380,7 +484,7 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
         if (k < nk) {
           const float spec = c_bch[c0 + k].spec;
           const float xbk = XB(k);
-          const float s0 = profile(g.sf0 * xbk, GAUSS);
+          const float s0 = POLY ? poly3(c0p, c_bch[c0 + k].dl) : profile(g.sf0 * xbk, GAUSS);
           const uint16_t c = (mask & (1u << k)) ? cl[(size_t)(c0 + k) * n_rows + r] : cell0;
           if (c != kNoCell) {
             const float cr = fmaf(pr[k], zr, fmaf(-pi[k], zi, s0 * spec * g.flux));
@@ -389,7 +493,8 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
             atomicAdd(&fac[c].y, ci);
           }
           if (s.apply) {
-            const float a = g.flux * spec * (profile(f1 * xbk, GAUSS) - s0);
+            const float a = POLY ? spec * poly3(dfp, c_bch[c0 + k].dl)
+                                 : g.flux * spec * (profile(f1 * xbk, GAUSS) - s0);
             pr[k] = fmaf(-a, zr, pr[k]);
             pi[k] = fmaf(a, zi, pi[k]);
           }
@@ -404,7 +509,7 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
 #undef XB
 }
 
-template <int GAUSS>
+template <int GAUSS, bool POLY>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
                                                                 const float2* __restrict__ sky, SeqBatch b,
@@ -432,9 +537,9 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
   const long long first = blockIdx.x * (long long)blockDim.x + tid;
   const long long ns = *b.n_simple;
   for (long long q = first; q < ns; q += stride)
-    seq_item<GAUSS, true>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    seq_item<GAUSS, true, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   for (long long q = ns + first; q < total; q += stride)
-    seq_item<GAUSS, false>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    seq_item<GAUSS, false, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;
   for (int i = tid; i < b.total_cells; i += blockDim.x) out[i] = acc[i];
@@ -449,10 +554,19 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   }
   const size_t smem = seq_smem_bytes(b.n_gal, b.total_cells, b.n_sizes);
   if (smem > 227 * 1024) { fprintf(stderr, "rlf: sequential extraction batch too large (%zu B)\n", smem); return 1; }
-  const void* kern = gaussian ? (const void*)k_extract_seq<1> : (const void*)k_extract_seq<0>;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int poly = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
+  const void* kern = gaussian ? (poly ? (const void*)k_extract_seq<1, true> : (const void*)k_extract_seq<1, false>)
+                              : (poly ? (const void*)k_extract_seq<0, true> : (const void*)k_extract_seq<0, false>);
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (gaussian) k_extract_seq<1><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
-  else k_extract_seq<0><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+  if (gaussian) {
+    if (poly) k_extract_seq<1, true><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+    else k_extract_seq<1, false><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+  } else {
+    if (poly) k_extract_seq<0, true><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+    else k_extract_seq<0, false><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
+  }
   return check("k_extract_seq");
 }
 
