@@ -22,10 +22,10 @@ int launch_row_table(int n_rows, const double* uu, const double* vv, const doubl
                      cudaStream_t st);
 // ---- sequential batch extraction (exact in-batch removal order)
 #ifndef RLF_SEQ_THREADS
-#define RLF_SEQ_THREADS 384
+#define RLF_SEQ_THREADS 768
 #endif
 #ifndef RLF_SEQ_CTAS_PER_SM
-#define RLF_SEQ_CTAS_PER_SM 2
+#define RLF_SEQ_CTAS_PER_SM 1
 #endif
 #ifndef RLF_SEQ_FACET_KB
 #define RLF_SEQ_FACET_KB 96
