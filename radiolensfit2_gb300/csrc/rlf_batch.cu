@@ -648,8 +648,10 @@ int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, cons
 
 // ---------------------------------------------------------------- removal
 // grid-stride over (row, chunk of kRemCh channels); galaxies staged through shared memory in
-// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.
-template <int GAUSS>
+// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  POLY: the profiles of a chunk from
+// its cubic in dl (profile_poly), one profile evaluation per model, galaxy and chunk.
+static_assert(kRemCh == kChunk, "removal chunks must be the chunks of the channel polynomials");
+template <int GAUSS, bool POLY>
 __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __restrict__ rows, float2* data,
                                                       float2* sky, const GalaxyParams* __restrict__ gals,
                                                       const FitOut* __restrict__ fit, int n_gal) {
@@ -683,19 +685,33 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
         const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
         const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
         float zs, zc, ws, wc;
-        sincospif(2.f * turns_at(T0, dT, ch0), &zs, &zc);
-        sincospif(2.f * (dT.hi + dT.lo), &ws, &wc);
+        sincos_turn(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
+        sincos_turn(dT.hi + dT.lo, &ws, &wc);
         float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
         const float k1q = g.A * (rw.u_hi * rw.u_hi) + g.B * rw.uv + g.Cc * (rw.v_hi * rw.v_hi);
+        float c0p[4], c1p[4];
+        if (POLY) {
+          const float wc2 = c_chunk[ch0 / kChunk].wn2c;
+          profile_poly<GAUSS>(g.sf0 * wc2 * rw.q, c0p);
+          profile_poly<GAUSS>(g.sf1 * wc2 * k1q, c1p);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) { c0p[j] *= g.flux; c1p[j] *= g.flux; }
+        }
 #pragma unroll
         for (int k = 0; k < kRemCh; ++k) {
           const int ch = ch0 + k;
           if (ch < nch) {
             const BatchChan bc = c_bch[ch];
-            const float x0 = g.sf0 * bc.wn2 * rw.q;
-            const float x1 = g.sf1 * bc.wn2 * k1q;
-            const float a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * bc.spec * g.flux;
-            const float a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * bc.spec * g.flux;
+            float a0, a1;
+            if (POLY) {
+              a0 = bc.spec * poly3(c0p, bc.dl);
+              a1 = bc.spec * poly3(c1p, bc.dl);
+            } else {
+              const float x0 = g.sf0 * bc.wn2 * rw.q;
+              const float x1 = g.sf1 * bc.wn2 * k1q;
+              a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * bc.spec * g.flux;
+              a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * bc.spec * g.flux;
+            }
             ar[k] = fmaf(a0, zr, ar[k]);
             ai[k] = fmaf(a0, zi, ai[k]);
             br[k] = fmaf(a1, zr, br[k]);
@@ -734,8 +750,14 @@ int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = sms * 4;
-  if (gaussian) k_remove_batch<1><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
-  else k_remove_batch<0><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
+  const int poly = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
+  if (gaussian) {
+    if (poly) k_remove_batch<1, true><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
+    else k_remove_batch<1, false><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
+  } else {
+    if (poly) k_remove_batch<0, true><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
+    else k_remove_batch<0, false><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
+  }
   return check("k_remove_batch");
 }
 
