@@ -532,14 +532,28 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
   }
   __syncthreads();
   const int nch = c_bnch;
-  const long long total = (long long)n_rows * ((nch + kChunk - 1) / kChunk);
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long first = blockIdx.x * (long long)blockDim.x + tid;
-  const long long ns = *b.n_simple;
-  for (long long q = first; q < ns; q += stride)
-    seq_item<GAUSS, true, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
-  for (long long q = ns + first; q < total; q += stride)
-    seq_item<GAUSS, false, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+  const int total = (int)((long long)n_rows * ((nch + kChunk - 1) / kChunk));
+  const int ns = *b.n_simple;
+  const int lane = tid & 31;
+  // each warp takes 32 consecutive items at a time from a device counter, the single-run items
+  // first: the other items cost several times more and a static split would leave their tail to a
+  // few CTAs
+  while (true) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&b.queue[0], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= ns) break;
+    const int q = base + lane;
+    if (q < ns) seq_item<GAUSS, true, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+  }
+  while (true) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&b.queue[1], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const int q = ns + base + lane;
+    if (ns + base >= total) break;
+    if (q < total) seq_item<GAUSS, false, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+  }
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;
   for (int i = tid; i < b.total_cells; i += blockDim.x) out[i] = acc[i];
@@ -554,6 +568,8 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   }
   const size_t smem = seq_smem_bytes(b.n_gal, b.total_cells, b.n_sizes);
   if (smem > 227 * 1024) { fprintf(stderr, "rlf: sequential extraction batch too large (%zu B)\n", smem); return 1; }
+  const cudaError_t qe = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int), st);
+  if (qe != cudaSuccess) { fprintf(stderr, "rlf: extraction queue: %s\n", cudaGetErrorString(qe)); return (int)qe; }
   int dev = 0;
   cudaGetDevice(&dev);
   const int poly = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;

@@ -57,6 +57,8 @@ struct SeqBatch {
   const uint16_t* cells[kSeqMaxSizes];
   const int* items;           // work items (row, 16-channel chunk) = chunk * n_rows + row: the
   const int* n_simple;        // *n_simple single-run ones first, then the others
+  int* queue;                 // [2] work counters of the extraction (single-run, other items),
+                              // zeroed by launch_extract_seq
 };
 size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes);
 // split the batch's work items into single-run ones (front) and the others (back) for

@@ -163,7 +163,7 @@ struct rlf_observation {
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
   rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
   rlf::DevBuf<int> items;           // work items of the sequential batch extraction
-  rlf::DevBuf<int> item_count;      // [2] simple / other work items
+  rlf::DevBuf<int> item_count;      // [4] simple / other work items, then the extraction's work counters
   double max_delay_m = 0;
   int n_part = 0;
   double ms[4] = {0, 0, 0, 0};
@@ -499,11 +499,12 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       }
       RLF_OK(ob->bpartial.ensure((size_t)seq_ctas * sb.total_cells));
       const long long n_items = (long long)ob->n_rows * ((ob->n_ch + 15) / 16);
-      if (n_items > 0x7fffffffLL) { fprintf(stderr, "rlf: %lld row-chunks exceed the batched extraction\n", n_items); return 1; }
+      if (n_items > 0x7fffffffLL - (1LL << 24)) { fprintf(stderr, "rlf: %lld row-chunks exceed the batched extraction\n", n_items); return 1; }
       RLF_OK(ob->items.ensure((size_t)n_items));
-      RLF_OK(ob->item_count.ensure(2));
+      RLF_OK(ob->item_count.ensure(4));
       sb.items = ob->items.p;
       sb.n_simple = ob->item_count.p;
+      sb.queue = ob->item_count.p + 2;
       RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;

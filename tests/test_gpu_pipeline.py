@@ -91,6 +91,9 @@ def test_pipeline_modes(orc, case, sky):
     assert np.max(np.abs(f["e1"][good] - e_ref[good, 0])) < 1e-7
     assert np.max(np.abs(f["e2"][good] - e_ref[good, 1])) < 1e-7
     assert np.allclose(f["maxL"][good], L_ref[good], rtol=1e-9)
+    de64 = np.maximum(np.abs(f["e1"][good] - e_ref[good, 0]), np.abs(f["e2"][good] - e_ref[good, 1]))
+    print(f"f64: |de| max {de64.max():.2e}; |dL/L| max "
+          f"{np.max(np.abs(f['maxL'][good] - L_ref[good]) / np.abs(L_ref[good])):.2e}")
     stats = {}
     for name in ("mixed", "mixed-fit", "batched", "batched-1round"):
         r = out[name]
