@@ -44,12 +44,22 @@ typedef struct {
                         extracts every galaxy of the batch from the same data; each further round
                         removes the previous round's fitted models of the earlier galaxies of the
                         batch from each facet, converging to the one-galaxy-at-a-time result. */
+  int fresh_obs;     /* data_processing: 0 (default) keeps the observation's device copies of uvw,
+                        sigma2_vis, flag and the facet tables built from them between calls that pass
+                        the same arrays (same addresses and sizes, same sampled contents), as the
+                        reference driver's two passes do; visibilities and sky model are uploaded on
+                        every call.  1 rebuilds everything on every call (arrays changed in place). */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
  * Defaults: RLF_F64, batch 1, exponential profile. Returns 0. */
 int rlf_configure(const rlf_options *opt);
 const char *rlf_version(void);
+/* No counterpart in the reference.  Frees the observation data_processing keeps between calls. */
+void rlf_release(void);
+/* No counterpart in the reference.  Host<->device bytes this library has copied since it was
+ * loaded (visibilities, arrays, results; not the small constant tables). */
+void rlf_transfer_bytes(unsigned long long *h2d, unsigned long long *d2h);
 int rlf_device_count(void);
 /* number of CUDA kernels this library has launched since it was loaded */
 long long rlf_launch_count(void);

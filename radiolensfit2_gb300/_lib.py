@@ -35,7 +35,7 @@ class Options(C.Structure):
     """rlf_options (include/rlf_gb300.h)"""
     _fields_ = [("precision", C.c_int), ("batch", C.c_int), ("gaussian", C.c_int),
                 ("refit", C.c_int), ("verbose", C.c_int), ("start", PD), ("fit_precision", C.c_int),
-                ("rounds", C.c_int)]
+                ("rounds", C.c_int), ("fresh_obs", C.c_int)]
 
 
 _lib = None
@@ -53,6 +53,8 @@ def load():
         "rlf_version": (C.c_char_p, []),
         "rlf_device_count": (C.c_int, []),
         "rlf_launch_count": (C.c_longlong, []),
+        "rlf_release": (None, []),
+        "rlf_transfer_bytes": (None, [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
         "rlf_fp32_peak_gflops": (D, []),
         "rlf_configure": (C.c_int, [C.POINTER(Options)]),
         "rlf_obs_create": (C.c_void_p, [C.c_int, C.c_int, PD, PD, PD, PD, PD, D, PF, PU8, C.c_int]),
@@ -114,7 +116,8 @@ def load():
 
 
 EXPORTED = [
-    "rlf_version", "rlf_device_count", "rlf_launch_count", "rlf_fp32_peak_gflops", "rlf_configure", "rlf_obs_create", "rlf_obs_destroy",
+    "rlf_version", "rlf_device_count", "rlf_launch_count", "rlf_fp32_peak_gflops", "rlf_configure", "rlf_release",
+    "rlf_transfer_bytes", "rlf_obs_create", "rlf_obs_destroy",
     "rlf_obs_set_vis", "rlf_obs_set_data_c64", "rlf_obs_get_vis", "rlf_obs_simulate",
     "rlf_obs_sky_model", "rlf_obs_snapshot", "rlf_obs_restore", "rlf_obs_process",
     "rlf_obs_last_timing", "rlf_obs_last_stats", "rlf_obs_extract", "rlf_debug_fit_trace", "rlf_debug_loglike_nodes", "rlf_gridding_visibilities_noalloc", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",

@@ -72,6 +72,14 @@ namespace rlf {
     if (r_) return r_;            \
   } while (0)
 
+// host <-> device bytes moved by this library (rlf_transfer_bytes); every copy goes through here
+static unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
+static cudaError_t copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+  if (kind == cudaMemcpyHostToDevice) __atomic_add_fetch(&g_h2d_bytes, (unsigned long long)bytes, __ATOMIC_RELAXED);
+  if (kind == cudaMemcpyDeviceToHost) __atomic_add_fetch(&g_d2h_bytes, (unsigned long long)bytes, __ATOMIC_RELAXED);
+  return cudaMemcpyAsync(dst, src, bytes, kind, st);
+}
+
 template <class T>
 struct DevBuf {
   T* p = nullptr;
@@ -97,18 +105,18 @@ struct DevBuf {
   }
   int upload(const T* h, size_t count, cudaStream_t st) {
     RLF_OK(ensure(count));
-    if (count) RLF_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    if (count) RLF_CUDA(copy_async(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
     return 0;
   }
   int download(T* h, size_t count, cudaStream_t st) const {
-    if (count) RLF_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+    if (count) RLF_CUDA(copy_async(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
     return 0;
   }
 };
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -536,7 +544,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       if (facets_out) break;
       // ---- fit
       if (u.seq && rd == nr - 1 && nr > 1)
-        RLF_CUDA(cudaMemcpyAsync(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
+        RLF_CUDA(copy_async(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
       RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
       if (fb.board.slot) {
         RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bn * sizeof(SampleSlot), st));
@@ -557,9 +565,9 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     if (facets_out) {
       // extraction only: hand the packed facets of this unit back as doubles
       std::vector<int> nc(bn);
-      RLF_CUDA(cudaMemcpyAsync(nc.data(), dnc.p + b0, bn * sizeof(int), cudaMemcpyDeviceToHost, st));
+      RLF_CUDA(copy_async(nc.data(), dnc.p + b0, bn * sizeof(int), cudaMemcpyDeviceToHost, st));
       std::vector<unsigned char> h(5 * plane);
-      RLF_CUDA(cudaMemcpyAsync(h.data(), cells.p, h.size(), cudaMemcpyDeviceToHost, st));
+      RLF_CUDA(copy_async(h.data(), cells.p, h.size(), cudaMemcpyDeviceToHost, st));
       RLF_CUDA(cudaStreamSynchronize(st));
       for (int k = 0; k < bn; ++k) {
         ncoords_out[b0 + k] = nc[k];
@@ -592,7 +600,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   }
   if (!facets_out) RLF_OK(dout.download(out.data(), n, st));
   unsigned long long changed = 0;
-  if (dchanged.p) RLF_CUDA(cudaMemcpyAsync(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
+  if (dchanged.p) RLF_CUDA(copy_async(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   ob->stats[RLF_STAT_CHANGED] += (long long)changed;
   if (ms3) pt.sum(ms3);
@@ -687,7 +695,7 @@ static int obs_put_c128(rlf_observation* ob, const double* h, bool sky, cudaStre
   const long long n = ob->n_vis;
   if (ob->precision == RLF_F64) {
     double2* d = sky ? ob->sky64.p : ob->data64.p;
-    if (h) RLF_CUDA(cudaMemcpyAsync(d, h, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    if (h) RLF_CUDA(copy_async(d, h, n * sizeof(double2), cudaMemcpyHostToDevice, st));
     else RLF_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double2), st));
     return 0;
   }
@@ -699,7 +707,7 @@ static int obs_put_c128(rlf_observation* ob, const double* h, bool sky, cudaStre
   RLF_OK(tmp.ensure((size_t)std::min(chunk, n)));
   for (long long i = 0; i < n; i += chunk) {
     const long long c = std::min(chunk, n - i);
-    RLF_CUDA(cudaMemcpyAsync(tmp.p, h + 2 * i, c * sizeof(double2), cudaMemcpyHostToDevice, st));
+    RLF_CUDA(copy_async(tmp.p, h + 2 * i, c * sizeof(double2), cudaMemcpyHostToDevice, st));
     RLF_OK(launch_convert_c64_to_f32(c, tmp.p, d + i, st));
   }
   RLF_CUDA(cudaStreamSynchronize(st));
@@ -710,7 +718,7 @@ static int obs_get_c128(rlf_observation* ob, double* h, bool sky, cudaStream_t s
   const long long n = ob->n_vis;
   if (!h) return 0;
   if (ob->precision == RLF_F64) {
-    RLF_CUDA(cudaMemcpyAsync(h, sky ? ob->sky64.p : ob->data64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(copy_async(h, sky ? ob->sky64.p : ob->data64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     RLF_CUDA(cudaStreamSynchronize(st));
     return 0;
   }
@@ -721,7 +729,7 @@ static int obs_get_c128(rlf_observation* ob, double* h, bool sky, cudaStream_t s
   for (long long i = 0; i < n; i += chunk) {
     const long long c = std::min(chunk, n - i);
     RLF_OK(launch_convert_f32_to_c64(c, d + i, tmp.p, st));
-    RLF_CUDA(cudaMemcpyAsync(h + 2 * i, tmp.p, c * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(copy_async(h + 2 * i, tmp.p, c * sizeof(double2), cudaMemcpyDeviceToHost, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   }
   return 0;
@@ -853,7 +861,7 @@ int rlf_obs_set_data_c64(rlf_observation* obs, const float* data_c64) {
     RLF_OK(launch_convert_f32_to_c64(n, tmp.p, obs->data64.p, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   } else {
-    RLF_CUDA(cudaMemcpyAsync(obs->data32.p, data_c64, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    RLF_CUDA(copy_async(obs->data32.p, data_c64, n * sizeof(float2), cudaMemcpyHostToDevice, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   }
   return 0;
@@ -942,13 +950,13 @@ int rlf_obs_snapshot(rlf_observation* obs) {
   if (obs->precision == RLF_F64) {
     RLF_OK(obs->data64_0.ensure(n));
     RLF_OK(obs->sky64_0.ensure(n));
-    RLF_CUDA(cudaMemcpyAsync(obs->data64_0.p, obs->data64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    RLF_CUDA(cudaMemcpyAsync(obs->sky64_0.p, obs->sky64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->data64_0.p, obs->data64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->sky64_0.p, obs->sky64.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   } else {
     RLF_OK(obs->data32_0.ensure(n));
     RLF_OK(obs->sky32_0.ensure(n));
-    RLF_CUDA(cudaMemcpyAsync(obs->data32_0.p, obs->data32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-    RLF_CUDA(cudaMemcpyAsync(obs->sky32_0.p, obs->sky32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->data32_0.p, obs->data32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->sky32_0.p, obs->sky32.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
   }
   RLF_CUDA(cudaStreamSynchronize(st));
   return 0;
@@ -960,12 +968,12 @@ int rlf_obs_restore(rlf_observation* obs) {
   const size_t n = (size_t)obs->n_vis;
   if (obs->precision == RLF_F64) {
     if (!obs->data64_0.p) return 1;
-    RLF_CUDA(cudaMemcpyAsync(obs->data64.p, obs->data64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    RLF_CUDA(cudaMemcpyAsync(obs->sky64.p, obs->sky64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->data64.p, obs->data64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->sky64.p, obs->sky64_0.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   } else {
     if (!obs->data32_0.p) return 1;
-    RLF_CUDA(cudaMemcpyAsync(obs->data32.p, obs->data32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-    RLF_CUDA(cudaMemcpyAsync(obs->sky32.p, obs->sky32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->data32.p, obs->data32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    RLF_CUDA(copy_async(obs->sky32.p, obs->sky32_0.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
   }
   return 0;
 }
@@ -1044,7 +1052,7 @@ unsigned int evaluate_uv_grid_size(int rank, int nprocs, double len, double* wav
   if (launch_cell_index(o, g_lib.b0.p, sizeg, g_lib.u16.p, st)) return 0;
   if (launch_count_cells(o, g_lib.u16.p, sizeg, g_lib.ucount.p, st)) return 0;
   unsigned n = 0;
-  cudaMemcpyAsync(&n, g_lib.ucount.p + (size_t)sizeg * sizeg, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  copy_async(&n, g_lib.ucount.p + (size_t)sizeg * sizeg, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   return n;
 }
@@ -1057,10 +1065,10 @@ unsigned int evaluate_facet_coords(double* grid_u, double* grid_v, double len, u
   if (g_lib.d0.upload(count_w, nc, st) || g_lib.d1.ensure(nc) || g_lib.d2.ensure(nc) || g_lib.ucount.ensure(1)) return 0;
   if (launch_facet_coords(g_lib.d1.p, g_lib.d2.p, len, sizeg, g_lib.d0.p, g_lib.ucount.p, st)) return 0;
   unsigned n = 0;
-  cudaMemcpyAsync(&n, g_lib.ucount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  copy_async(&n, g_lib.ucount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
-  cudaMemcpyAsync(grid_u, g_lib.d1.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(grid_v, g_lib.d2.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(grid_u, g_lib.d1.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(grid_v, g_lib.d2.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   return n;
 }
@@ -1087,13 +1095,13 @@ void gridding_visibilities(double* wavenumbers, unsigned int num_channels, unsig
   if (launch_grid_vis_f64(o, g_lib.c0.p, g_lib.f0.p, g_lib.b0.p, sizeg, g_lib.d2.p, n_part, st)) return;
   if (launch_grid_vis_finalize(g_lib.d2.p, n_part, sizeg, g_lib.c1.p, g_lib.d3.p, g_lib.d4.p, st)) return;
   std::vector<double> sw(nc);
-  cudaMemcpyAsync(sw.data(), g_lib.d4.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(sw.data(), g_lib.d4.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   size_t n = 0;
   for (size_t p = 0; p < nc; ++p) n += sw[p] != 0.0;
   memcpy(sum_w, sw.data(), nc * sizeof(double));
-  cudaMemcpyAsync(new_vis, g_lib.c1.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(new_sigma2, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(new_vis, g_lib.c1.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  copy_async(new_sigma2, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 }
 
@@ -1105,8 +1113,8 @@ void average_facets(unsigned long int size, complexd* grid_vis, double* grid_sig
       g_lib.d0.upload(grid_sigma2, size, st) || g_lib.d1.upload(sum_w, size, st))
     return;
   if (launch_average_facets((long long)size, g_lib.c0.p, g_lib.d0.p, g_lib.d1.p, st)) return;
-  cudaMemcpyAsync(grid_vis, g_lib.c0.p, size * sizeof(double2), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(grid_sigma2, g_lib.d0.p, size * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(grid_vis, g_lib.c0.p, size * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  copy_async(grid_sigma2, g_lib.d0.p, size * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 }
 
@@ -1121,7 +1129,7 @@ void model_galaxy_visibilities_at_zero(double e1, double e2, double scale, unsig
   if (launch_model_at_zero(e1, e2, scale, (int)num_coords, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p,
                            g_lib.opt.gaussian, st))
     return;
-  cudaMemcpyAsync(Modvis, g_lib.d3.p, num_coords * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(Modvis, g_lib.d3.p, num_coords * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 }
 
@@ -1139,7 +1147,7 @@ void data_galaxy_visibilities(double spectra, double wavenumber, double band_fac
   if (launch_galaxy_vis_channel((int)num_coords, spectra, wavenumber, e1, e2, scale, flux, l, m, g_lib.d0.p,
                                 g_lib.d1.p, g_lib.d2.p, g_lib.c0.p, g_lib.opt.gaussian, st))
     return;
-  cudaMemcpyAsync(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  copy_async(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 }
 
@@ -1155,7 +1163,7 @@ void data_visibilities_phase_shift(double wavenumber, double l, double m, unsign
   if (launch_phase_shift_channel((int)num_coords, wavenumber, l, m, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.c0.p,
                                  st))
     return;
-  cudaMemcpyAsync(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  copy_async(vis, g_lib.c0.p, num_coords * sizeof(double2), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 }
 
@@ -1175,8 +1183,8 @@ double loglikelihood_r(double ee1, double ee2, double scale, unsigned long int n
                              g_lib.d5.p, g_lib.d6.p, g_lib.opt.gaussian, st))
     return kBad;
   double L[2];
-  cudaMemcpyAsync(L, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(visM, g_lib.d5.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(L, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(visM, g_lib.d5.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   return L[0];
 }
@@ -1195,7 +1203,7 @@ int cross_correlation(unsigned long int n_uv_coords, double* grid_u, double* gri
   if (launch_cross_correlation((int)n, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p, g_lib.d4.p, g_lib.d6.p, st))
     return 1;
   double r[4];
-  cudaMemcpyAsync(r, g_lib.d6.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(r, g_lib.d6.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   *ho = r[0];
   *det_sigma = r[1];
@@ -1212,7 +1220,7 @@ double loglikelihood(void* params, double ee1, double ee2, int* error) {
   if (f.load(par, st) || g_lib.d6.ensure(2)) return kBad;
   if (launch_loglikelihood(f.fb, ee1, ee2, g_lib.d6.p, nullptr, st)) return kBad;
   double r[2];
-  cudaMemcpyAsync(r, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(r, g_lib.d6.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   *error = (int)r[1];
   return r[0];
@@ -1238,7 +1246,7 @@ void likelihood_sampling(double* mes_e1, double* mes_e2, double maxL, void* para
   if (f.load(par, st) || g_lib.d6.ensure(5)) return;
   if (launch_likelihood_sampling(f.fb, *mes_e1, *mes_e2, maxL, np_max, g_lib.d6.p, st)) return;
   double r[5];
-  cudaMemcpyAsync(r, g_lib.d6.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(r, g_lib.d6.p, 5 * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   *mes_e1 = r[0]; *mes_e2 = r[1]; *var_e1 = r[2]; *var_e2 = r[3]; *oneDimvar = r[4];
 }
@@ -1255,10 +1263,10 @@ void rlf_set_posterior_values(int numR, double* L_r, double* rprior, double* Ro,
   if (launch_set_posterior_values(numR, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, g_lib.d3.p, g_lib.d4.p, g_lib.i0.p, st))
     return;
   int n = 0;
-  cudaMemcpyAsync(&n, g_lib.i0.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+  copy_async(&n, g_lib.i0.p, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
-  cudaMemcpyAsync(xmarvals, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(ymarvals, g_lib.d4.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(xmarvals, g_lib.d3.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(ymarvals, g_lib.d4.p, n * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   *numvals = n;
 }
@@ -1272,8 +1280,8 @@ double rlf_marginalise_posterior_r(int num_marvals, double* xmarvals, double* ym
     return kBad;
   if (launch_marginalise_posterior_r(num_marvals, g_lib.d0.p, g_lib.d1.p, g_lib.d2.p, st)) return kBad;
   double L = kBad;
-  cudaMemcpyAsync(&L, g_lib.d2.p, sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(ymarvals, g_lib.d1.p, num_marvals * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(&L, g_lib.d2.p, sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(ymarvals, g_lib.d1.p, num_marvals * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   g_marf_x.assign(xmarvals, xmarvals + num_marvals);
   g_marf_y.assign(ymarvals, ymarvals + num_marvals);
@@ -1324,7 +1332,7 @@ int source_fitting(int rank, likelihood_params* par, double* mes_e1, double* mes
   f.fb.queue = g_lib.i0.p;
   if (fit_launch(f.fb, kF64, 1, st)) return 1;
   FitOut o;
-  cudaMemcpyAsync(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st);
+  copy_async(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   *mes_e1 = o.e1; *mes_e2 = o.e2; *var_e1 = o.var_e1; *var_e2 = o.var_e2; *oneDimvar = o.oneDimvar; *maxL = o.maxL;
   if (g_lib.opt.verbose) {
@@ -1374,8 +1382,8 @@ int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int prec
   f.fb.trace_cap = cap;
   RLF_OK(fit_launch(f.fb, precision == RLF_MIXED ? kMixed : kF64, 1, st));
   FitOut o;
-  RLF_CUDA(cudaMemcpyAsync(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st));
-  RLF_CUDA(cudaMemcpyAsync(trace, dt.p, (size_t)cap * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(copy_async(&o, g_lib.fo.p, sizeof(FitOut), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(copy_async(trace, dt.p, (size_t)cap * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   out6[0] = o.e1; out6[1] = o.e2; out6[2] = o.max_e1; out6[3] = o.max_e2; out6[4] = o.maxL; out6[5] = o.nevals;
   return 0;
@@ -1393,7 +1401,7 @@ int rlf_debug_loglike_nodes(void* pv, double e1, double e2, int precision, doubl
   RLF_OK(d.ensure(2 + kMaxNodes));
   RLF_OK(launch_loglikelihood_prec(f.fb, e1, e2, d.p, d.p + 2, precision == RLF_MIXED ? kMixed : kF64, st));
   double h[2 + kMaxNodes];
-  RLF_CUDA(cudaMemcpyAsync(h, d.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+  RLF_CUDA(copy_async(h, d.p, sizeof(h), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   out2[0] = h[0]; out2[1] = h[1];
   for (int k = 0; k < par->numr && k < kMaxNodes; ++k) node_L[k] = h[2 + k];
@@ -1415,8 +1423,8 @@ void source_extraction(int rank, unsigned int facet, likelihood_params* par, com
                                    RLF_F64, st);
   if (!ob) return;
   const long long nv = ob->n_vis;
-  cudaMemcpyAsync(ob->data64.p, visData, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(ob->sky64.p, visSkyMod, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
+  copy_async(ob->data64.p, visData, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
+  copy_async(ob->sky64.p, visSkyMod, nv * sizeof(double2), cudaMemcpyHostToDevice, st);
   FacetCache* fc = nullptr;
   if (obs_facet(ob, facet, &fc, st)) { delete ob; return; }
   GalaxyParams g;
@@ -1447,9 +1455,9 @@ void source_extraction(int rank, unsigned int facet, likelihood_params* par, com
       launch_facet_finalize(1, dfac.p, sums, 1, 0, dss.p, dsw.p, len, fo, st)) { delete ob; return; }
   int n = 0;
   std::vector<double> h((size_t)5 * nc);
-  cudaMemcpyAsync(&n, dnc.p, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(h.data(), cells.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(sum_w, fc->sw.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(&n, dnc.p, sizeof(int), cudaMemcpyDeviceToHost, st);
+  copy_async(h.data(), cells.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+  copy_async(sum_w, fc->sw.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   for (int i = 0; i < n; ++i) {
     facet_vis[i].real = h[(size_t)2 * nc + i];
@@ -1472,7 +1480,7 @@ void sky_model(double* wavenumbers, double* spec, double channel_bandwidth_hz, i
   rlf_observation* ob = obs_create((int)num_coords, (int)num_channels, uu_metres, vv_metres, ww_metres, wavenumbers,
                                    spec, 1.0, s2.data(), nullptr, RLF_F64, st);
   if (!ob) return;
-  cudaMemcpyAsync(ob->sky64.p, visMod, ob->n_vis * sizeof(double2), cudaMemcpyHostToDevice, st);
+  copy_async(ob->sky64.p, visMod, ob->n_vis * sizeof(double2), cudaMemcpyHostToDevice, st);
   std::vector<GalaxyParams> g = make_gals((int)n_gal, gflux, gscale, nullptr, nullptr, l, m, 1.0, 0);
   DevBuf<GalaxyParams> dg;
   if (dg.upload(g.data(), g.size(), st)) { delete ob; return; }
@@ -1481,10 +1489,56 @@ void sky_model(double* wavenumbers, double* spec, double channel_bandwidth_hz, i
     const int gn = (int)std::min<unsigned>(256, n_gal - g0);
     if (launch_sky_model_f64(o, ob->sky64.p, dg.p + g0, gn, 0, g_lib.opt.gaussian, st)) { delete ob; return; }
   }
-  cudaMemcpyAsync(visMod, ob->sky64.p, ob->n_vis * sizeof(double2), cudaMemcpyDeviceToHost, st);
+  copy_async(visMod, ob->sky64.p, ob->n_vis * sizeof(double2), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   delete ob;
 }
+
+// The observation of the last data_processing call, kept with its device copies (uvw, variances,
+// flags, row table) and the facet tables built from them while later calls pass the same arrays:
+// the reference driver passes the same uvw, sigma2_vis, flag and channel arrays to both passes
+// (RadioLensfit2.cpp:597-606).  The key holds the arrays' addresses and sizes and a fingerprint of
+// their sampled contents (all channel values, 4096 evenly spaced rows and visibilities), so a
+// different observation placed at the same addresses is rebuilt.  Visibilities and sky model are
+// uploaded on every call.  rlf_options.fresh_obs = 1 rebuilds on every call; rlf_release frees it.
+struct ObsKey {
+  int n_rows = 0, n_ch = 0, precision = -1, has_flag = 0;
+  const void *uu = nullptr, *vv = nullptr, *ww = nullptr, *sigma2 = nullptr, *flag = nullptr;
+  double len = 0;
+  unsigned long long fp = 0;
+  bool operator==(const ObsKey& o) const {
+    return n_rows == o.n_rows && n_ch == o.n_ch && precision == o.precision && has_flag == o.has_flag && uu == o.uu &&
+           vv == o.vv && ww == o.ww && sigma2 == o.sigma2 && flag == o.flag && len == o.len && fp == o.fp;
+  }
+};
+static unsigned long long fnv1a(unsigned long long h, const void* p, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+  return h;
+}
+static ObsKey obs_key(int n_rows, int n_ch, const double* uu, const double* vv, const double* ww,
+                      const double* wavenumbers, const double* spec, double len, const float* sigma2,
+                      const uint8_t* flag, int precision) {
+  ObsKey k;
+  k.n_rows = n_rows; k.n_ch = n_ch; k.precision = precision; k.has_flag = flag != nullptr;
+  k.uu = uu; k.vv = vv; k.ww = ww; k.sigma2 = sigma2; k.flag = flag; k.len = len;
+  unsigned long long h = 1469598103934665603ull;
+  h = fnv1a(h, wavenumbers, sizeof(double) * n_ch);
+  h = fnv1a(h, spec, sizeof(double) * n_ch);
+  const long long nv = (long long)n_rows * n_ch;
+  for (int i = 0; i <= 4096; ++i) {
+    const long long r = (long long)(n_rows - 1) * i / 4096, v = (nv - 1) * i / 4096;
+    h = fnv1a(h, uu + r, sizeof(double));
+    h = fnv1a(h, vv + r, sizeof(double));
+    h = fnv1a(h, ww + r, sizeof(double));
+    h = fnv1a(h, sigma2 + v, sizeof(float));
+    if (flag) h = fnv1a(h, flag + v, 1);
+  }
+  k.fp = h;
+  return k;
+}
+static rlf_observation* g_obs_cached = nullptr;
+static ObsKey g_obs_key;
 
 // data_processing.c:47-147: one pass over the catalogue (re_fitting = false) or the bad list
 void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, double len, unsigned int num_coords,
@@ -1497,12 +1551,27 @@ void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, doub
   cudaStream_t st;
   if (lib_stream(&st)) return;
   const rlf_options opt = g_lib.opt;
-  rlf_observation* ob = obs_create((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres,
-                                   par->wavenumbers, par->spec, len, sigma2_vis, reinterpret_cast<const uint8_t*>(flag),
-                                   opt.precision, st);
-  if (!ob) return;
+  const uint8_t* flag8 = reinterpret_cast<const uint8_t*>(flag);
+  rlf_observation* ob = nullptr;
+  const ObsKey key = obs_key((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres, par->wavenumbers,
+                             par->spec, len, sigma2_vis, flag8, opt.precision);
+  if (!opt.fresh_obs && g_obs_cached && key == g_obs_key) {
+    ob = g_obs_cached;
+  } else {
+    delete g_obs_cached;
+    g_obs_cached = nullptr;
+    ob = obs_create((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres, par->wavenumbers, par->spec,
+                    len, sigma2_vis, flag8, opt.precision, st);
+    if (!ob) return;
+    if (!opt.fresh_obs) { g_obs_cached = ob; g_obs_key = key; }
+  }
+  // the observation is freed on the way out unless it is the cached one
+  struct Release {
+    rlf_observation* o;
+    ~Release() { if (o != g_obs_cached) delete o; }
+  } release{ob};
   if (obs_put_c128(ob, reinterpret_cast<const double*>(visData), false, st) ||
-      obs_put_c128(ob, reinterpret_cast<const double*>(visSkyMod), true, st)) { delete ob; return; }
+      obs_put_c128(ob, reinterpret_cast<const double*>(visSkyMod), true, st)) return;
   // galaxies: the catalogue (in order) or the bad list
   std::vector<int> order(nsources > 0 ? nsources : 0);
   for (int g = 0; g < nsources; ++g) order[g] = re_fitting ? (int)bad_list[g] : g;
@@ -1512,7 +1581,7 @@ void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, doub
   std::vector<GalaxyParams> gals = make_gals(ncat, gflux, gscale, nullptr, nullptr, l, m, len, fmax);
   std::vector<FitOut> out;
   double ms3[3] = {0, 0, 0};
-  if (run_pass(ob, gals, order, par->numr, par->ro, opt, out, st, ms3)) { delete ob; return; }
+  if (run_pass(ob, gals, order, par->numr, par->ro, opt, out, st, ms3)) return;
   int nbad = 0;
   for (int g = 0; g < nsources; ++g) {
     const int gal = order[g];
@@ -1540,7 +1609,17 @@ void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, doub
   *fitting_time += ms3[1] / 1000.0;
   obs_get_c128(ob, reinterpret_cast<double*>(visData), false, st);
   obs_get_c128(ob, reinterpret_cast<double*>(visSkyMod), true, st);
-  delete ob;
+}
+
+void rlf_release(void) {
+  delete g_obs_cached;
+  g_obs_cached = nullptr;
+  g_obs_key = ObsKey{};
+}
+
+void rlf_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
+  if (h2d) *h2d = __atomic_load_n(&g_h2d_bytes, __ATOMIC_RELAXED);
+  if (d2h) *d2h = __atomic_load_n(&g_d2h_bytes, __ATOMIC_RELAXED);
 }
 
 }  // extern "C"

@@ -308,3 +308,73 @@ def test_device_pipeline_f64_matches_oracle(orc, case, sky):
     d, s = dev.get_vis()
     assert rel(d, d_ref) < 1e-11
     assert np.max(np.abs(s - s_ref)) < 1e-11 * np.max(np.abs(sky))
+
+
+def _data_processing(lib, case, data, skym, uu, vv, ww, sigma2, flag):
+    """one catalogue pass of the drop-in data_processing on the given host arrays"""
+    o, c = case.obs, case.cat
+    fmax = K.facet_size(K.RMAX, case.len)
+    p = LikelihoodParams()
+    ro = case.ro.copy()
+    pr = np.zeros(case.numr)
+    p.numr, p.ro, p.rprior, p.nchannels = case.numr, dptr(ro), dptr(pr), o.n_ch
+    p.spec, p.wavenumbers = dptr(o.spec), dptr(o.wavenumbers)
+    bad_list = np.zeros(c.n, np.uint32)
+    bad = C.c_int(0)
+    ft = C.c_double(0)
+    snr = np.zeros(c.n)
+    sumw = np.zeros(fmax * fmax)
+    gal = np.zeros(1, np.complex128)
+    lib.data_processing(False, bad_list.ctypes.data_as(_lib.PU), c.n, case.len, o.n_rows, None, C.byref(p),
+                        dptr(c.l), dptr(c.m), dptr(c.flux), dptr(c.scale), dptr(c.e1), dptr(c.e2), dptr(snr),
+                        dptr(sumw), cptr(gal), cptr(skym), cptr(data), fptr(sigma2), bptr(flag),
+                        dptr(uu), dptr(vv), dptr(ww), C.byref(ft), C.byref(bad))
+    return bad.value, bad_list
+
+
+def test_data_processing_keeps_observation(lib, orc):
+    """data_processing keeps the observation (device uvw, variances, flags, facet tables) between
+    calls that pass the same arrays, uploading only visibilities and sky model, and rebuilds it
+    when the contents at the same addresses change (here: uvw scaled, other variances and flags)."""
+    A = Case(flag_frac=0.03, n_gal=6)
+    B = Case(seed=5, flag_frac=0.05, noise=700.0, n_gal=6)
+    opt = _lib.Options()
+    opt.precision, opt.batch, opt.refit, opt.fresh_obs = _lib.RLF_F64, 1, 1, 0
+    lib.rlf_configure(C.byref(opt))
+    lib.rlf_release()
+    uu, vv, ww = A.obs.uu.copy(), A.obs.vv.copy(), A.obs.ww.copy()
+    sigma2, flag = A.sigma2.copy(), A.flag.copy()
+    sky_a = oracle_sky_model(orc, A)
+    d_ref, s_ref, bad_ref, bl_ref, _ = oracle_data_processing(orc, A, A.data, sky_a)
+    h0, o0 = C.c_ulonglong(0), C.c_ulonglong(0)
+    h1, o1 = C.c_ulonglong(0), C.c_ulonglong(0)
+    moved = []
+    for _ in range(2):
+        data, skym = A.data.copy(), sky_a.copy()
+        lib.rlf_transfer_bytes(C.byref(h0), C.byref(o0))
+        bad, bl = _data_processing(lib, A, data, skym, uu, vv, ww, sigma2, flag)
+        lib.rlf_transfer_bytes(C.byref(h1), C.byref(o1))
+        moved.append(h1.value - h0.value)
+        assert bad == bad_ref and np.array_equal(bl[:bad], bl_ref[:bad])
+        assert rel(data, d_ref) < 1e-11
+        assert np.max(np.abs(skym - s_ref)) < 1e-11 * np.max(np.abs(sky_a))
+    vis_bytes = 2 * 16 * A.obs.n_vis
+    # the second call moved the visibilities and sky model and the per-call galaxy tables only
+    assert moved[1] < moved[0]
+    assert vis_bytes <= moved[1] < vis_bytes + (1 << 20)
+    # another observation in the same host buffers
+    np.copyto(uu, A.obs.uu * 1.001)
+    np.copyto(vv, A.obs.vv * 1.001)
+    np.copyto(ww, A.obs.ww * 1.001)
+    np.copyto(sigma2, B.sigma2)
+    np.copyto(flag, B.flag)
+    B.obs.uu, B.obs.vv, B.obs.ww = uu.copy(), vv.copy(), ww.copy()
+    B.flag = flag.copy()
+    sky_b = oracle_sky_model(orc, B)
+    d_ref, s_ref, bad_ref, bl_ref, _ = oracle_data_processing(orc, B, B.data, sky_b)
+    data, skym = B.data.copy(), sky_b.copy()
+    bad, bl = _data_processing(lib, B, data, skym, uu, vv, ww, sigma2, flag)
+    assert bad == bad_ref and np.array_equal(bl[:bad], bl_ref[:bad])
+    assert rel(data, d_ref) < 1e-11
+    assert np.max(np.abs(skym - s_ref)) < 1e-11 * np.max(np.abs(sky_b))
+    lib.rlf_release()
