@@ -40,6 +40,7 @@ __constant__ BatchChan c_bch[kMaxCh];
 __constant__ BatchChunk c_chunk[kChunks];
 __constant__ int c_chunk_poly;
 static int g_chunk_poly[64];  // host copy of c_chunk_poly per device (selects the kernel variant)
+static int g_nch[64];         // host copy of c_bnch per device
 __constant__ float c_il0_hi, c_il0_lo, c_dil_hi, c_dil_lo;  // inv_lambda(0) and its channel step
 __constant__ int c_bnch;
 
@@ -110,7 +111,10 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
                                                      cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_poly, &poly, 4, 0, cudaMemcpyHostToDevice, st);
   int dev = 0;
-  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) g_chunk_poly[dev] = poly;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    g_chunk_poly[dev] = poly;
+    g_nch[dev] = n_ch;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: batch channels: %s\n", cudaGetErrorString(e)); return (int)e; }
   return 0;
@@ -355,16 +359,20 @@ __device__ __forceinline__ void profile_poly(float xc, float cf[4]) {
 }
 __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(fmaf(fmaf(c[3], d, c[2]), d, c[1]), d, c[0]); }
 
-// one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order
-// (POLY: the profiles from the chunk polynomial, one profile evaluation per galaxy and chunk)
-template <int GAUSS, bool SIMPLE, bool POLY>
+// one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order.
+// MODE 0: exact per-channel profiles; 1: the profiles from the chunk polynomial, one profile
+// evaluation per galaxy and chunk; 2: as 1 for an observation of exactly one 16-channel chunk, so
+// that the channel constants are compile-time operands.
+template <int GAUSS, bool SIMPLE, int MODE>
 __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
+  constexpr bool POLY = MODE > 0;
+  constexpr bool ONE = MODE == 2;
   const int tid = threadIdx.x;
-  const int r = t % n_rows;
-  const int c0 = (t / n_rows) * kChunk;
-  const int nk = min(kChunk, nch - c0);
+  const int r = ONE ? t : t % n_rows;
+  const int c0 = ONE ? 0 : (t / n_rows) * kChunk;
+  const int nk = ONE ? kChunk : min(kChunk, nch - c0);
   const RowF rw = rows[r];
   float pr[kChunk], pi[kChunk];
 #pragma unroll
@@ -509,7 +517,7 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
 #undef XB
 }
 
-template <int GAUSS, bool POLY>
+template <int GAUSS, int MODE>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
                                                                 const float2* __restrict__ sky, SeqBatch b,
@@ -544,7 +552,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= ns) break;
     const int q = base + lane;
-    if (q < ns) seq_item<GAUSS, true, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (q < ns) seq_item<GAUSS, true, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   while (true) {
     int base = 0;
@@ -552,7 +560,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     base = __shfl_sync(0xffffffffu, base, 0);
     const int q = ns + base + lane;
     if (ns + base >= total) break;
-    if (q < total) seq_item<GAUSS, false, POLY>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (q < total) seq_item<GAUSS, false, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;
@@ -572,17 +580,17 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   if (qe != cudaSuccess) { fprintf(stderr, "rlf: extraction queue: %s\n", cudaGetErrorString(qe)); return (int)qe; }
   int dev = 0;
   cudaGetDevice(&dev);
-  const int poly = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
-  const void* kern = gaussian ? (poly ? (const void*)k_extract_seq<1, true> : (const void*)k_extract_seq<1, false>)
-                              : (poly ? (const void*)k_extract_seq<0, true> : (const void*)k_extract_seq<0, false>);
+  const bool known = dev >= 0 && dev < 64;
+  const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+  const void* kernels[2][3] = {{(const void*)k_extract_seq<0, 0>, (const void*)k_extract_seq<0, 1>,
+                                (const void*)k_extract_seq<0, 2>},
+                               {(const void*)k_extract_seq<1, 0>, (const void*)k_extract_seq<1, 1>,
+                                (const void*)k_extract_seq<1, 2>}};
+  const void* kern = kernels[gaussian ? 1 : 0][mode];
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (gaussian) {
-    if (poly) k_extract_seq<1, true><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
-    else k_extract_seq<1, false><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
-  } else {
-    if (poly) k_extract_seq<0, true><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
-    else k_extract_seq<0, false><<<ctas, kSeqThreads, smem, st>>>(n_rows, rows, data, sky, b, partial);
-  }
+  void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&data, (void*)&sky, (void*)&b, (void*)&partial};
+  const cudaError_t le = cudaLaunchKernel(kern, dim3(ctas), dim3(kSeqThreads), args, smem, st);
+  if (le != cudaSuccess) { fprintf(stderr, "rlf: k_extract_seq: %s\n", cudaGetErrorString(le)); return (int)le; }
   return check("k_extract_seq");
 }
 
