@@ -33,8 +33,8 @@ namespace rlf {
 // several galaxies per SM, so that one galaxy's serial phases overlap another's cell passes
 constexpr int kFitWarps = RLF_FIT_WARPS;
 constexpr int kFitThreads = kFitWarps * 32;
-constexpr int kFitMinBlocks = kFitWarps <= 8 ? 3 : (kFitWarps <= 12 ? 2 : 1);
-constexpr int kQagCap = 256;       // intervals held by the device QAG
+constexpr int kFitMinBlocks = kFitWarps <= 6 ? 4 : (kFitWarps <= 8 ? 3 : (kFitWarps <= 12 ? 2 : 1));
+constexpr int kQagCap = 128;       // intervals held by the device QAG (more: status bit 2, an error)
 constexpr int kNewtonMax = 50;     // likelihood.c:290
 constexpr int kSimplexMax = 50;    // galaxy_fitting.c:80
 constexpr int kModelCache = 4;     // facet cells per lane whose model stays in registers
@@ -411,27 +411,50 @@ __device__ typename P::S node_loglike(const typename P::Cell* gu, const typename
 }
 
 // ------------------------------------------------------------- shared state
-// Per-node caches of the phased node evaluation (eval_nodes), in dynamic shared memory: the first
-// kNodeCache cells of every node.  Phase A leaves the unnormalised model in hre; phase B replaces
-// it by the real part of data x normalised model and fills him (the model does not change during
-// the Newton search, so the Newton passes read both back and evaluate no model).
+// Per-node state of the phased node evaluation (eval_nodes), in dynamic shared memory sized by the
+// number of scalelength nodes (row 0 unused, as Ro[0]): the partial sums each node's lanes leave, and
+// caches of the first kNodeCache cells of every node.  Phase A leaves the unnormalised model in hre;
+// phase B replaces it by the real part of data x normalised model and fills him (the model does not
+// change during the Newton search, so the Newton passes read both back and evaluate no model).
 // The FP64 policy keeps the Newton inputs as double-float pairs (f2), the mixed policy as double.
 union CacheSlot {
   double d;
   f2 f;
 };
 struct NodeCache {
-  CacheSlot hre[kMaxNodes][kNodeStride];
-  CacheSlot him[kMaxNodes][kNodeStride];
-  double cu[kNodeCache], cv[kNodeCache];  // 2 pi u and 2 pi v of the cells
-  f2 cu2[kNodeCache], cv2[kNodeCache];    // the same as double-float pairs
-  double isg[kNodeCache];                 // 1 / variance of the cells
+  double* part;       // [7][nr][kNodePart]: 0 model norm; 1..6 val, dx, dy, d2x, d2y, dxy
+  CacheSlot* hre;     // [nr][kNodeStride]
+  CacheSlot* him;     // [nr][kNodeStride]
+  double *cu, *cv;    // [kNodeCache] 2 pi u and 2 pi v of the cells
+  double* isg;        // [kNodeCache] 1 / variance of the cells
+  f2 *cu2, *cv2;      // [kNodeCache] 2 pi u, 2 pi v as double-float pairs
+  int nr;
+  __device__ __forceinline__ double* P(int k, int node) const { return part + ((size_t)k * nr + node) * kNodePart; }
+  __device__ __forceinline__ CacheSlot& H(int node, int i) const { return hre[node * kNodeStride + i]; }
+  __device__ __forceinline__ CacheSlot& M(int node, int i) const { return him[node * kNodeStride + i]; }
 };
+// bytes of a NodeCache for nr node rows (a multiple of 16)
+__host__ __device__ __forceinline__ size_t node_cache_bytes(int nr) {
+  return (size_t)7 * nr * kNodePart * sizeof(double) + (size_t)2 * nr * kNodeStride * sizeof(CacheSlot) +
+         (size_t)kNodeCache * (3 * sizeof(double) + 2 * sizeof(f2));
+}
+__device__ __forceinline__ NodeCache node_cache_view(unsigned char* base, int nr) {
+  NodeCache c;
+  c.nr = nr;
+  c.part = reinterpret_cast<double*>(base);
+  c.hre = reinterpret_cast<CacheSlot*>(c.part + (size_t)7 * nr * kNodePart);
+  c.him = c.hre + (size_t)nr * kNodeStride;
+  c.cu = reinterpret_cast<double*>(c.him + (size_t)nr * kNodeStride);
+  c.cv = c.cu + kNodeCache;
+  c.isg = c.cv + kNodeCache;
+  c.cu2 = reinterpret_cast<f2*>(c.isg + kNodeCache);
+  c.cv2 = c.cu2 + kNodeCache;
+  return c;
+}
 
 template <class S>
 struct FitShared {
-  // phased node evaluation (eval_nodes): per-node partial sums and state
-  double part[7][kMaxNodes][kNodePart];  // 0: model norm; 1..6: val, dx, dy, d2x, d2y, dxy
+  // phased node evaluation (eval_nodes): per-node state
   double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
   double nnorm[kMaxNodes];                // 1 / the node's model normalisation
   int alist[kMaxNodes];                   // nodes with a Newton pass pending
@@ -883,21 +906,21 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       int i = c0;
       for (; i < ncache; i += kNodePart) {
         const T m = cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
-        nc.hre[node][i].d = (double)m;
+        nc.H(node, i).d = (double)m;
         acc.add(m * m * T(nc.isg[i]));
       }
       for (; i < n; i += kNodePart) {
         const T m = cell_shape_fit<T>(gaussian, a1, a2, a3, T(gu[i]), T(gv[i]), sfw);
         acc.add(m * m / T(sig2[i]));
       }
-      sh.part[0][node][c0] = acc_value(acc);
+      nc.P(0, node)[c0] = acc_value(acc);
     }
   }
   __syncthreads();
   if (warp == 0) {
     const int node = lane;
     if (node >= 1 && node < numR) {
-      const double s_norm = sqrt(node_sum(sh.part[0][node]));
+      const double s_norm = sqrt(node_sum(nc.P(0, node)));
       sh.nnorm[node] = 1.0 / s_norm;
     }
   }
@@ -910,15 +933,15 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
       for (int i = c0; i < n; i += kNodePart) {
-        const T m = i < kNodeCache ? T(nc.hre[node][i].d) * nn : model(i, sfw, nn);
+        const T m = i < kNodeCache ? T(nc.H(node, i).d) * nn : model(i, sfw, nn);
         const T hre = T(dre[i]) * m, him = -T(dim[i]) * m;
         if (i < kNodeCache) {
           if constexpr (P::kMixed) {
-            nc.hre[node][i].d = (double)hre;
-            nc.him[node][i].d = (double)him;
+            nc.H(node, i).d = (double)hre;
+            nc.M(node, i).d = (double)him;
           } else {
-            nc.hre[node][i].f = df_from_double(hre);
-            nc.him[node][i].f = df_from_double(him);
+            nc.H(node, i).f = df_from_double(hre);
+            nc.M(node, i).f = df_from_double(him);
           }
         }
         const T u = cc * T(gu[i]), v = cc * T(gv[i]);
@@ -929,9 +952,9 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
         d2y.sub(hre * v * v);
         dxy.sub(hre * u * v);
       }
-      sh.part[1][node][c0] = acc_value(val); sh.part[2][node][c0] = acc_value(dx);
-      sh.part[3][node][c0] = acc_value(dy); sh.part[4][node][c0] = acc_value(d2x);
-      sh.part[5][node][c0] = acc_value(d2y); sh.part[6][node][c0] = acc_value(dxy);
+      nc.P(1, node)[c0] = acc_value(val); nc.P(2, node)[c0] = acc_value(dx);
+      nc.P(3, node)[c0] = acc_value(dy); nc.P(4, node)[c0] = acc_value(d2x);
+      nc.P(5, node)[c0] = acc_value(d2y); nc.P(6, node)[c0] = acc_value(dxy);
     }
   }
   __syncthreads();
@@ -947,8 +970,8 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
       bool act = false;
       if (mine && pending) {
         const int node = lane;
-        Sval = node_sum(sh.part[1][node]); Sdx = node_sum(sh.part[2][node]); Sdy = node_sum(sh.part[3][node]);
-        Sd2x = node_sum(sh.part[4][node]); Sd2y = node_sum(sh.part[5][node]); Sdxy = node_sum(sh.part[6][node]);
+        Sval = node_sum(nc.P(1, node)); Sdx = node_sum(nc.P(2, node)); Sdy = node_sum(nc.P(3, node));
+        Sd2x = node_sum(nc.P(4, node)); Sd2y = node_sum(nc.P(5, node)); Sdxy = node_sum(nc.P(6, node));
         det = Sd2x * Sd2y - Sdxy * Sdxy;
         if (iter > 0) norm = normv;
         if (det > 0 && norm > tol && iter < kNewtonMax) {
@@ -1004,15 +1027,15 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
           dxy = df_sub(dxy, df_mul(ru, v));
         };
         int i = c0;
-        for (; i < ncache; i += kNodePart) cell(nc.hre[node][i].f, nc.him[node][i].f, nc.cu2[i], nc.cv2[i]);
+        for (; i < ncache; i += kNodePart) cell(nc.H(node, i).f, nc.M(node, i).f, nc.cu2[i], nc.cv2[i]);
         for (; i < n; i += kNodePart) {
           const T m = model(i, sfw, nn);
           cell(df_from_double(T(dre[i]) * m), df_from_double(-T(dim[i]) * m), df_from_double(cc * T(gu[i])),
                df_from_double(cc * T(gv[i])));
         }
-        sh.part[1][node][c0] = df_to_double(val); sh.part[2][node][c0] = df_to_double(dx);
-        sh.part[3][node][c0] = df_to_double(dy); sh.part[4][node][c0] = df_to_double(d2x);
-        sh.part[5][node][c0] = df_to_double(d2y); sh.part[6][node][c0] = df_to_double(dxy);
+        nc.P(1, node)[c0] = df_to_double(val); nc.P(2, node)[c0] = df_to_double(dx);
+        nc.P(3, node)[c0] = df_to_double(dy); nc.P(4, node)[c0] = df_to_double(d2x);
+        nc.P(5, node)[c0] = df_to_double(d2y); nc.P(6, node)[c0] = df_to_double(dxy);
         continue;
       }
       const T txo = T(sh.nx[node]), tyo = T(sh.ny[node]);
@@ -1032,14 +1055,14 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
         dxy.sub(rp * u * v);
       };
       int i = c0;
-      for (; i < ncache; i += kNodePart) cell(T(nc.hre[node][i].d), T(nc.him[node][i].d), T(nc.cu[i]), T(nc.cv[i]));
+      for (; i < ncache; i += kNodePart) cell(T(nc.H(node, i).d), T(nc.M(node, i).d), T(nc.cu[i]), T(nc.cv[i]));
       for (; i < n; i += kNodePart) {
         const T m = model(i, sfw, nn);
         cell(T(dre[i]) * m, -T(dim[i]) * m, cc * T(gu[i]), cc * T(gv[i]));
       }
-      sh.part[1][node][c0] = acc_value(val); sh.part[2][node][c0] = acc_value(dx);
-      sh.part[3][node][c0] = acc_value(dy); sh.part[4][node][c0] = acc_value(d2x);
-      sh.part[5][node][c0] = acc_value(d2y); sh.part[6][node][c0] = acc_value(dxy);
+      nc.P(1, node)[c0] = acc_value(val); nc.P(2, node)[c0] = acc_value(dx);
+      nc.P(3, node)[c0] = acc_value(dy); nc.P(4, node)[c0] = acc_value(d2x);
+      nc.P(5, node)[c0] = acc_value(d2y); nc.P(6, node)[c0] = acc_value(dxy);
     }
     __syncthreads();
   }
@@ -1564,39 +1587,32 @@ __device__ __forceinline__ size_t cells_smem_bytes(int max_cells) {
   return (size_t)5 * max_cells * sizeof(typename P::Cell);
 }
 
-// galaxy g's facet cells into the CTA's shared memory and its scalelength prior into sh.rprior;
-// returns the number of cells
+// galaxy g's facet cells (read in place from global memory: a few KB, read-only during the fit,
+// they stay in L1) and its scalelength prior into sh.rprior; returns the number of cells
 template <class P>
-__device__ int stage_galaxy(const FacetBatch& b, int g, typename P::Cell* gu, typename P::Cell* gv,
-                            typename P::Cell* dre, typename P::Cell* dim, typename P::Cell* sig2,
-                            FitShared<typename P::S>& sh) {
+__device__ int bind_galaxy(const FacetBatch& b, int g, const typename P::Cell** cells, FitShared<typename P::S>& sh) {
   using Cell = typename P::Cell;
   using S = typename P::S;
   const int off = b.offset[g];
-  const int n = b.count[g];
-  const Cell* Gu = reinterpret_cast<const Cell*>(b.gu) + off;
-  const Cell* Gv = reinterpret_cast<const Cell*>(b.gv) + off;
-  const Cell* Dr = reinterpret_cast<const Cell*>(b.dre) + off;
-  const Cell* Di = reinterpret_cast<const Cell*>(b.dim) + off;
-  const Cell* Sg = reinterpret_cast<const Cell*>(b.sig2) + off;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    gu[i] = Gu[i]; gv[i] = Gv[i]; dre[i] = Dr[i]; dim[i] = Di[i]; sig2[i] = Sg[i];
-  }
+  cells[0] = reinterpret_cast<const Cell*>(b.gu) + off;
+  cells[1] = reinterpret_cast<const Cell*>(b.gv) + off;
+  cells[2] = reinterpret_cast<const Cell*>(b.dre) + off;
+  cells[3] = reinterpret_cast<const Cell*>(b.dim) + off;
+  cells[4] = reinterpret_cast<const Cell*>(b.sig2) + off;
   for (int i = threadIdx.x; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[(size_t)g * kMaxNodes + i]);
-  return n;
+  return b.count[g];
 }
 
 // Helper side of the sampling board, run by a CTA once the galaxy queue is empty: warp 0 scans
 // the slots of the launch for a chunk with unclaimed points and claims one; the CTA evaluates it
-// with the galaxy's cells staged in its own shared memory.  Returns when every galaxy of the
-// launch is finished, or after kBoardWaitNs without finding work.
+// with the galaxy's cells and prior.  Returns when every galaxy of the launch is finished, or after
+// kBoardWaitNs without finding work.
 template <class P>
-__device__ void board_help(const FacetBatch& b, FitShared<typename P::S>& sh, NodeCache& nc,
-                           typename P::Cell* gu, typename P::Cell* gv, typename P::Cell* dre,
-                           typename P::Cell* dim, typename P::Cell* sig2) {
+__device__ void board_help(const FacetBatch& b, FitShared<typename P::S>& sh, NodeCache& nc) {
   const SampleBoard& bd = b.board;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int staged = -1, n = 0;
+  const typename P::Cell* cp[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   unsigned long long idle0 = global_ns();
   while (true) {
     if (warp == 0) {
@@ -1643,14 +1659,14 @@ __device__ void board_help(const FacetBatch& b, FitShared<typename P::S>& sh, No
     if (sh.claim_state < 0) return;
     const int gg = sh.claim_g;
     if (gg != staged) {
-      n = stage_galaxy<P>(b, gg, gu, gv, dre, dim, sig2, sh);
+      n = bind_galaxy<P>(b, gg, cp, sh);
       staged = gg;
     }
     const SampleSlot prm = sh.claim_prm;
     const int seq = sh.claim_seq, idx = sh.claim_idx;
     const int before = sh.newton;
     __syncthreads();
-    board_point<P>(sh, nc, gu, gv, dre, dim, sig2, n, bd, gg, seq, idx, prm, before);
+    board_point<P>(sh, nc, cp[0], cp[1], cp[2], cp[3], cp[4], n, bd, gg, seq, idx, prm, before);
     idle0 = global_ns();
     __syncthreads();
   }
@@ -1661,12 +1677,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
   using Cell = typename P::Cell;
   __shared__ FitShared<typename P::S> sh;
   extern __shared__ __align__(16) unsigned char dyn[];
-  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
-  Cell* gu = reinterpret_cast<Cell*>(dyn + sizeof(NodeCache));
-  Cell* gv = gu + b.max_cells;
-  Cell* dre = gv + b.max_cells;
-  Cell* dim = dre + b.max_cells;
-  Cell* sig2 = dim + b.max_cells;
+  NodeCache nc = node_cache_view(dyn, c_fit.numr);
   const int tid = threadIdx.x;
   if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
   while (true) {
@@ -1679,12 +1690,13 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
       __syncthreads();
       continue;
     }
-    const int n = stage_galaxy<P>(b, g, gu, gv, dre, dim, sig2, sh);
+    const Cell* cp[5];
+    const int n = bind_galaxy<P>(b, g, cp, sh);
     if (tid == 0) { sh.newton = 0; sh.status = 0; }
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
-    FitCtx<P> c{&sh, &nc, gu, gv, dre, dim, sig2, n, 0,
+    FitCtx<P> c{&sh, &nc, cp[0], cp[1], cp[2], cp[3], cp[4], n, 0,
                 b.trace ? b.trace + (size_t)g * b.trace_cap * 4 : nullptr, b.trace_cap, b.board, g, 0};
     FitOut o = fit_galaxy<P>(c, se1, se2, step, c_fit.np_max);
     __syncthreads();
@@ -1700,7 +1712,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
     }
     __syncthreads();
   }
-  if (b.board.slot) board_help<P>(b, sh, nc, gu, gv, dre, dim, sig2);
+  if (b.board.slot) board_help<P>(b, sh, nc);
 }
 
 // one loglikelihood evaluation of galaxy 0 of the batch (C entry point loglikelihood)
@@ -1711,7 +1723,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_loglike_once(FacetBatch b, d
   using S = typename P::S;
   __shared__ FitShared<S> sh;
   extern __shared__ __align__(16) unsigned char dyn[];
-  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
+  NodeCache nc = node_cache_view(dyn, c_fit.numr);
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
@@ -1732,7 +1744,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, 
   using S = typename P::S;
   __shared__ FitShared<S> sh;
   extern __shared__ __align__(16) unsigned char dyn[];
-  NodeCache& nc = *reinterpret_cast<NodeCache*>(dyn);
+  NodeCache nc = node_cache_view(dyn, c_fit.numr);
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
@@ -1805,10 +1817,13 @@ static int check(const char* what) {
   return 0;
 }
 
+static int g_fit_numr = kMaxNodes;  // host copy of c_fit.numr (sizes the node caches)
+
 int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
   FitConst h;
   memset(&h, 0, sizeof(h));
   h.numr = cfg.numr;
+  g_fit_numr = cfg.numr;
   h.gaussian = cfg.gaussian;
   h.np_max = cfg.np_max;
   for (int i = 0; i < kMaxNodes; ++i) {
@@ -1848,14 +1863,14 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
 
 template <class P>
 static int fit_launch_t(const FacetBatch& b, int grid, cudaStream_t st) {
-  const size_t dyn = sizeof(NodeCache) + (size_t)5 * (b.max_cells > 0 ? b.max_cells : 1) * sizeof(typename P::Cell);
+  const size_t dyn = node_cache_bytes(g_fit_numr);
   constexpr size_t kDynMax = 190 * 1024;
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_fit<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDynMax);
     attr_set = true;
   }
-  if (dyn > kDynMax) { fprintf(stderr, "rlf: facet too large for the fit kernel\n"); return 1; }
+  if (dyn > kDynMax) { fprintf(stderr, "rlf: too many scalelength nodes for the fit kernel\n"); return 1; }
   // persistent CTAs: as many as fit on the GPU with this batch's facet staging
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
@@ -1897,19 +1912,19 @@ int launch_cross_correlation(int n, const double* gu, const double* gv, const do
 // default 48 KB together with their static state
 template <class K>
 static void allow_node_cache(K kernel) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(NodeCache));
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)node_cache_bytes(g_fit_numr));
 }
 int launch_loglikelihood(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
                          cudaStream_t st) {
   allow_node_cache(k_loglike_once<PolicyF64>);
-  k_loglike_once<PolicyF64><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, out2, node_L);
+  k_loglike_once<PolicyF64><<<1, kFitThreads, node_cache_bytes(g_fit_numr), st>>>(b, e1, e2, out2, node_L);
   return check("k_loglike_once");
 }
 int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double* out2, double* node_L,
                               Precision prec, cudaStream_t st) {
   if (prec == kMixed) {
     allow_node_cache(k_loglike_once<PolicyMixed>);
-    k_loglike_once<PolicyMixed><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, out2, node_L);
+    k_loglike_once<PolicyMixed><<<1, kFitThreads, node_cache_bytes(g_fit_numr), st>>>(b, e1, e2, out2, node_L);
     return check("k_loglike_once<mixed>");
   }
   return launch_loglikelihood(b, e1, e2, out2, node_L, st);
@@ -1917,7 +1932,7 @@ int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double*
 int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
                                double* out5, cudaStream_t st) {
   allow_node_cache(k_sampling_once<PolicyF64>);
-  k_sampling_once<PolicyF64><<<1, kFitThreads, sizeof(NodeCache), st>>>(b, e1, e2, maxL, np_max, out5);
+  k_sampling_once<PolicyF64><<<1, kFitThreads, node_cache_bytes(g_fit_numr), st>>>(b, e1, e2, maxL, np_max, out5);
   return check("k_sampling_once");
 }
 int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st) {
