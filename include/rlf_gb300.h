@@ -81,6 +81,38 @@ void rlf_obs_destroy(rlf_observation *obs);
 int rlf_obs_set_vis(rlf_observation *obs, const double *data_c128, const double *sky_c128);
 /* data from host complex64 [n_ch*n_rows] */
 int rlf_obs_set_data_c64(rlf_observation *obs, const float *data_c64);
+/* No counterpart in the reference: data straight from a Measurement Set DATA block
+ * [n_rows][n_ch][num_pols] complex64 in Jy (num_pols 1 or 4), converted on the GPU as
+ * ms_read_vis does (measurement_set.cpp:345-400): Stokes I, uJy, channel-major. */
+int rlf_obs_set_data_ms(rlf_observation *obs, const float *data_block, unsigned int num_pols);
+
+/* -------- Measurement Set columns (measurement_set.cpp:203-453) --------
+ * The reference's readers take a casacore table; these take the column blocks the caller read
+ * from it, row-major ([row][channel][correlation], complex64 interleaved), and produce the same
+ * arrays on the GPU.  No counterpart names in the reference (its ms_* functions need casacore). */
+/* ms_read_coords (measurement_set.cpp:203-241): UVW [num_coords][3] -> uu, vv, ww; returns
+ * ceil(max(max|u|, max|v|)) */
+double rlf_ms_read_coords(const double *uvw_block, unsigned int num_coords, double *uu, double *vv,
+                          double *ww);
+/* ms_read_Flag (measurement_set.cpp:280-334): FLAG [num_coords][num_channels][num_pols] (bytes)
+ * -> flag [num_channels * num_coords], correlation 0, or 0 || 3 with four; returns the number
+ * flagged */
+unsigned long rlf_ms_read_flag(const uint8_t *flag_block, unsigned int num_coords,
+                               unsigned int num_channels, unsigned int num_pols, uint8_t *flag);
+/* ms_read_vis (measurement_set.cpp:345-400): DATA -> vis complex128 [num_channels * num_coords],
+ * Stokes I ((0 + 3) / 2 with four correlations) in uJy */
+int rlf_ms_read_vis(const float *data_block, unsigned int num_coords, unsigned int num_channels,
+                    unsigned int num_pols, double *vis_c128);
+/* ms_read_sigma (measurement_set.cpp:246-274) and the driver's fallback (RadioLensfit2.cpp:257-270):
+ * sigma2_vis[num_channels * num_coords] = sigma[i]^2 for i < num_coords (the column read flat, as the
+ * reference does), every entry <= 0 or not set by the reader = sigma2_theory; sigma_block NULL: all
+ * entries sigma2_theory */
+int rlf_ms_read_sigma2(const float *sigma_block, unsigned int num_coords, unsigned int num_channels,
+                       float sigma2_theory, float *sigma2_vis);
+/* ms_write_vis (measurement_set.cpp:409-453): vis complex128 [num_channels * num_coords] in uJy ->
+ * DATA block [num_coords][num_channels] complex64 in Jy (one correlation) */
+int rlf_ms_write_vis(const double *vis_c128, unsigned int num_coords, unsigned int num_channels,
+                     float *data_block);
 int rlf_obs_get_vis(rlf_observation *obs, double *data_c128, double *sky_c128);
 /* data = sum of sheared galaxy models + complex Gaussian noise (sigma per component), on the GPU */
 int rlf_obs_simulate(rlf_observation *obs, int n_gal, const double *flux, const double *scale,

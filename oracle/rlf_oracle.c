@@ -688,3 +688,81 @@ void orc_data_processing(int re_fitting, unsigned int *bad_list, int nsources, d
   *bad = nbad;
   free(fvis); free(fs2); free(fu); free(fv); free(mod);
 }
+
+/* ------------------------------------------------------------------ Measurement Set columns
+ * The readers of measurement_set.cpp applied to column blocks already read from the table
+ * (casacore is not available): block layout [row][channel][correlation], row slowest. */
+
+/* ms_read_coords (measurement_set.cpp:224-240): UVW [rows][3] -> uu, vv, ww */
+double orc_ms_read_coords(const double *uvw, unsigned int num_coords, double *uu, double *vv, double *ww) {
+  double umax = 0., vmax = 0.;
+  for (unsigned int i = 0; i < num_coords; ++i) {
+    uu[i] = uvw[3 * (size_t)i];
+    vv[i] = uvw[3 * (size_t)i + 1];
+    ww[i] = uvw[3 * (size_t)i + 2];
+    double ua = fabs(uu[i]), va = fabs(vv[i]);
+    if (ua > umax) umax = ua;
+    if (va > vmax) vmax = va;
+  }
+  return ceil(fmax(umax, vmax));
+}
+
+/* ms_read_Flag (measurement_set.cpp:318-332): the first correlation, or first || last of four */
+unsigned long orc_ms_read_flag(const unsigned char *in, unsigned int num_coords, unsigned int num_channels,
+                               unsigned int num_pols, unsigned char *flag) {
+  unsigned long count = 0;
+  for (unsigned int c = 0; c < num_channels; ++c)
+    for (unsigned int b = 0; b < num_coords; ++b) {
+      unsigned long i = (unsigned long)num_pols * ((unsigned long)b * num_channels + c);
+      unsigned long j = (unsigned long)c * num_coords + b;
+      flag[j] = in[i];
+      if (num_pols == 4) flag[j] = (flag[j] || in[i + 3]);
+      if (flag[j]) count++;
+    }
+  return count;
+}
+
+/* ms_read_vis (measurement_set.cpp:384-400): Stokes I in uJy, channel-major */
+void orc_ms_read_vis(const float *in, unsigned int num_coords, unsigned int num_channels, unsigned int num_pols,
+                     orc_complex *vis) {
+  for (unsigned int c = 0; c < num_channels; ++c)
+    for (unsigned int b = 0; b < num_coords; ++b) {
+      unsigned long i = ((unsigned long)num_pols * ((unsigned long)b * num_channels + c)) << 1;
+      unsigned long j = (unsigned long)c * num_coords + b;
+      vis[j].real = in[i];
+      vis[j].imag = in[i + 1];
+      if (num_pols == 4) {
+        i += 6;
+        vis[j].real += in[i];
+        vis[j].imag += in[i + 1];
+        vis[j].real *= 0.5;
+        vis[j].imag *= 0.5;
+      }
+      vis[j].real *= 1e+6;
+      vis[j].imag *= 1e+6;
+    }
+}
+
+/* ms_read_sigma (measurement_set.cpp:266-273) into a [num_channels * num_coords] array, then the
+ * driver's replacement of non-positive values (RadioLensfit2.cpp:257-270).  The reader sets only the
+ * first num_coords entries; the rest are taken as unset (0) and so receive the theoretical value. */
+void orc_ms_read_sigma2(const float *in, unsigned int num_coords, unsigned int num_channels, float sigma2,
+                        float *sigma2_vis) {
+  unsigned long num_vis = (unsigned long)num_channels * num_coords;
+  for (unsigned long i = 0; i < num_vis; ++i) sigma2_vis[i] = 0.f;
+  if (in)
+    for (unsigned int i = 0; i < num_coords; ++i) sigma2_vis[i] = in[i] * in[i];
+  for (unsigned long i = 0; i < num_vis; ++i)
+    if (sigma2_vis[i] <= 0.) sigma2_vis[i] = sigma2;
+}
+
+/* ms_write_vis (measurement_set.cpp:423-433): one correlation, Jy, row-major */
+void orc_ms_write_vis(const orc_complex *vis, unsigned int num_coords, unsigned int num_channels, float *out) {
+  for (unsigned int c = 0; c < num_channels; ++c)
+    for (unsigned int b = 0; b < num_coords; ++b) {
+      unsigned long i = (unsigned long)c * num_coords + b;
+      unsigned long j = ((unsigned long)b * num_channels + c) << 1;
+      out[j] = vis[i].real * 1e-6;
+      out[j + 1] = vis[i].imag * 1e-6;
+    }
+}

@@ -113,6 +113,16 @@ void orc_data_processing(int re_fitting, unsigned int *bad_list, int nsources, d
                          const unsigned char *flag, const double *uu, const double *vv,
                          const double *ww, int gaussian, orc_fit_result *out, int *bad);
 
+/* Measurement Set column blocks (measurement_set.cpp) */
+double orc_ms_read_coords(const double *uvw, unsigned int num_coords, double *uu, double *vv, double *ww);
+unsigned long orc_ms_read_flag(const unsigned char *in, unsigned int num_coords, unsigned int num_channels,
+                               unsigned int num_pols, unsigned char *flag);
+void orc_ms_read_vis(const float *in, unsigned int num_coords, unsigned int num_channels, unsigned int num_pols,
+                     orc_complex *vis);
+void orc_ms_read_sigma2(const float *in, unsigned int num_coords, unsigned int num_channels, float sigma2,
+                        float *sigma2_vis);
+void orc_ms_write_vis(const orc_complex *vis, unsigned int num_coords, unsigned int num_channels, float *out);
+
 #ifdef __cplusplus
 }
 #endif

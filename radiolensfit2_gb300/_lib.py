@@ -54,6 +54,12 @@ def load():
         "rlf_device_count": (C.c_int, []),
         "rlf_launch_count": (C.c_longlong, []),
         "rlf_release": (None, []),
+        "rlf_obs_set_data_ms": (C.c_int, [C.c_void_p, PF, C.c_uint]),
+        "rlf_ms_read_coords": (D, [PD, C.c_uint, PD, PD, PD]),
+        "rlf_ms_read_flag": (C.c_ulong, [PU8, C.c_uint, C.c_uint, C.c_uint, PU8]),
+        "rlf_ms_read_vis": (C.c_int, [PF, C.c_uint, C.c_uint, C.c_uint, PD]),
+        "rlf_ms_read_sigma2": (C.c_int, [PF, C.c_uint, C.c_uint, C.c_float, PF]),
+        "rlf_ms_write_vis": (C.c_int, [PD, C.c_uint, C.c_uint, PF]),
         "rlf_transfer_bytes": (None, [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
         "rlf_fp32_peak_gflops": (D, []),
         "rlf_configure": (C.c_int, [C.POINTER(Options)]),
@@ -117,7 +123,8 @@ def load():
 
 EXPORTED = [
     "rlf_version", "rlf_device_count", "rlf_launch_count", "rlf_fp32_peak_gflops", "rlf_configure", "rlf_release",
-    "rlf_transfer_bytes", "rlf_obs_create", "rlf_obs_destroy",
+    "rlf_transfer_bytes", "rlf_obs_create", "rlf_obs_destroy", "rlf_obs_set_data_ms", "rlf_ms_read_coords",
+    "rlf_ms_read_flag", "rlf_ms_read_vis", "rlf_ms_read_sigma2", "rlf_ms_write_vis",
     "rlf_obs_set_vis", "rlf_obs_set_data_c64", "rlf_obs_get_vis", "rlf_obs_simulate",
     "rlf_obs_sky_model", "rlf_obs_snapshot", "rlf_obs_restore", "rlf_obs_process",
     "rlf_obs_last_timing", "rlf_obs_last_stats", "rlf_obs_extract", "rlf_debug_fit_trace", "rlf_debug_loglike_nodes", "rlf_gridding_visibilities_noalloc", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",

@@ -1,6 +1,6 @@
 """Build librlf_gb300.so for sm_103a (in-tree, no CMake).
 
-The three CUDA translation units compile in parallel and link into
+The CUDA translation units compile in parallel and link into
 radiolensfit2_gb300/_build/librlf_gb300.so.  Set RLF_NVCC to override the compiler path.
 """
 from __future__ import annotations
@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "librlf_gb300.so")
-SOURCES = ["rlf_fit.cu", "rlf_vis.cu", "rlf_batch.cu", "rlf_capi.cu", "rlf_noalloc.cu"]
+SOURCES = ["rlf_fit.cu", "rlf_vis.cu", "rlf_batch.cu", "rlf_capi.cu", "rlf_noalloc.cu", "rlf_ms.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -19,6 +19,7 @@
 #include "rlf_fit.cuh"
 #include "rlf_vis.cuh"
 #include "rlf_batch.cuh"
+#include "rlf_ms.cuh"
 #include "../../include/rlf_gb300.h"
 
 typedef struct {
@@ -828,6 +829,17 @@ __attribute__((constructor)) static void install_segv_trace() {
 using namespace rlf;
 
 // =========================================================== batched / device API
+// an input block on the device: page-locked host memory is read in place, other memory copied
+template <class T>
+static const T* device_in(const T* h, size_t n, DevBuf<T>& buf, cudaStream_t st) {
+  if (const void* d = mapped_host(h)) {
+    __atomic_add_fetch(&g_h2d_bytes, (unsigned long long)n * sizeof(T), __ATOMIC_RELAXED);
+    return static_cast<const T*>(d);
+  }
+  if (buf.upload(h, n, st)) return nullptr;
+  return buf.p;
+}
+
 extern "C" {
 
 const char* rlf_version(void) { return "rlf-gb300 0.1 (sm_103a)"; }
@@ -888,6 +900,119 @@ int rlf_obs_set_data_c64(rlf_observation* obs, const float* data_c64) {
     RLF_CUDA(copy_async(obs->data32.p, data_c64, n * sizeof(float2), cudaMemcpyHostToDevice, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   }
+  return 0;
+}
+
+// DATA block of the Measurement Set straight into the observation's data (measurement_set.cpp:345-400)
+int rlf_obs_set_data_ms(rlf_observation* obs, const float* data_block, unsigned int num_pols) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const long long n = obs->n_vis * (long long)num_pols;
+  DevBuf<float2> in;
+  const float2* src = static_cast<const float2*>(mapped_host(data_block));
+  if (src) {
+    __atomic_add_fetch(&g_h2d_bytes, (unsigned long long)n * sizeof(float2), __ATOMIC_RELAXED);
+  } else {
+    RLF_OK(in.upload(reinterpret_cast<const float2*>(data_block), (size_t)n, st));
+    src = in.p;
+  }
+  if (obs->precision == RLF_F64) RLF_OK(launch_ms_vis_c128(src, obs->n_rows, obs->n_ch, (int)num_pols, obs->data64.p, st));
+  else RLF_OK(launch_ms_vis_f32(src, obs->n_rows, obs->n_ch, (int)num_pols, obs->data32.p, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+// ---- Measurement Set readers and writer on column blocks the caller read from the table
+
+double rlf_ms_read_coords(const double* uvw_block, unsigned int num_coords, double* uu, double* vv, double* ww) {
+  cudaStream_t st;
+  if (lib_stream(&st) || num_coords == 0) return 0.;
+  DevBuf<double> in, u, v, w;
+  DevBuf<unsigned long long> mx;
+  const double* d = device_in(uvw_block, (size_t)3 * num_coords, in, st);
+  if (!d || u.ensure(num_coords) || v.ensure(num_coords) || w.ensure(num_coords) || mx.ensure(1)) return 0.;
+  cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), st);
+  if (launch_ms_coords(d, num_coords, u.p, v.p, w.p, mx.p, st)) return 0.;
+  unsigned long long bits = 0;
+  u.download(uu, num_coords, st);
+  v.download(vv, num_coords, st);
+  w.download(ww, num_coords, st);
+  copy_async(&bits, mx.p, sizeof(bits), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  double m;
+  memcpy(&m, &bits, sizeof(m));
+  return ceil(m);
+}
+
+unsigned long rlf_ms_read_flag(const uint8_t* flag_block, unsigned int num_coords, unsigned int num_channels,
+                               unsigned int num_pols, uint8_t* flag) {
+  cudaStream_t st;
+  if (lib_stream(&st) || num_coords == 0 || num_channels == 0) return 0;
+  const size_t nv = (size_t)num_coords * num_channels;
+  DevBuf<uint8_t> in, out;
+  DevBuf<unsigned long long> cnt;
+  const uint8_t* d = device_in(flag_block, nv * num_pols, in, st);
+  if (!d || out.ensure(nv) || cnt.ensure(1)) return 0;
+  cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), st);
+  if (launch_ms_flags(d, num_coords, (int)num_channels, (int)num_pols, out.p, cnt.p, st)) return 0;
+  unsigned long long c = 0;
+  out.download(flag, nv, st);
+  copy_async(&c, cnt.p, sizeof(c), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return (unsigned long)c;
+}
+
+int rlf_ms_read_vis(const float* data_block, unsigned int num_coords, unsigned int num_channels, unsigned int num_pols,
+                    double* vis_c128) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  if (num_coords == 0 || num_channels == 0) return 0;
+  const size_t nv = (size_t)num_coords * num_channels;
+  DevBuf<float2> in;
+  DevBuf<double2> out;
+  const float2* d = device_in(reinterpret_cast<const float2*>(data_block), nv * num_pols, in, st);
+  if (!d) return 1;
+  double2* o = static_cast<double2*>(mapped_host(vis_c128));
+  if (o) __atomic_add_fetch(&g_d2h_bytes, (unsigned long long)nv * sizeof(double2), __ATOMIC_RELAXED);
+  else { RLF_OK(out.ensure(nv)); o = out.p; }
+  RLF_OK(launch_ms_vis_c128(d, num_coords, (int)num_channels, (int)num_pols, o, st));
+  if (o == out.p) RLF_OK(out.download(reinterpret_cast<double2*>(vis_c128), nv, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_ms_read_sigma2(const float* sigma_block, unsigned int num_coords, unsigned int num_channels,
+                       float sigma2_theory, float* sigma2_vis) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const size_t nv = (size_t)num_coords * num_channels;
+  if (nv == 0) return 0;
+  DevBuf<float> in, out;
+  const float* d = sigma_block ? device_in(sigma_block, num_coords, in, st) : nullptr;
+  if (sigma_block && !d) return 1;
+  RLF_OK(out.ensure(nv));
+  // without a SIGMA column every entry takes the theoretical variance (RadioLensfit2.cpp:258-263)
+  RLF_OK(launch_ms_sigma2(d, d ? num_coords : 0, (long long)nv, sigma2_theory, out.p, st));
+  RLF_OK(out.download(sigma2_vis, nv, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int rlf_ms_write_vis(const double* vis_c128, unsigned int num_coords, unsigned int num_channels, float* data_block) {
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const size_t nv = (size_t)num_coords * num_channels;
+  if (nv == 0) return 0;
+  DevBuf<double2> in;
+  DevBuf<float2> out;
+  const double2* d = device_in(reinterpret_cast<const double2*>(vis_c128), nv, in, st);
+  if (!d) return 1;
+  float2* o = static_cast<float2*>(mapped_host(data_block));
+  if (o) __atomic_add_fetch(&g_d2h_bytes, (unsigned long long)nv * sizeof(float2), __ATOMIC_RELAXED);
+  else { RLF_OK(out.ensure(nv)); o = out.p; }
+  RLF_OK(launch_ms_write(d, num_coords, (int)num_channels, o, st));
+  if (o == out.p) RLF_OK(out.download(reinterpret_cast<float2*>(data_block), nv, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
   return 0;
 }
 

@@ -57,6 +57,15 @@ class DeviceObservation:
             raise RuntimeError("rlf_obs_create failed")
         self.h = C.c_void_p(h)
 
+    def set_data_ms(self, data_block, num_pols: int):
+        """Data from a Measurement Set DATA block [n_rows][n_ch][num_pols] complex64 in Jy, converted
+        on the GPU as ms_read_vis does (measurement_set.cpp:345-400): Stokes I in uJy, channel-major."""
+        b = np.ascontiguousarray(data_block, dtype=np.complex64).reshape(-1)
+        if b.size != self.obs.n_vis * num_pols:
+            raise ValueError("DATA block size does not match the observation")
+        if self.lib.rlf_obs_set_data_ms(self.h, b.view(np.float32).ctypes.data_as(_lib.PF), num_pols):
+            raise RuntimeError("rlf_obs_set_data_ms failed")
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.rlf_obs_destroy(self.h)

@@ -64,6 +64,16 @@ def load_oracle():
     lib.orc_gridding.argtypes = [PD, C.c_uint, C.c_uint, PD, PD, PC, PF, D, C.c_uint, PC, PD, PU8, PD]
     lib.orc_average_facets.restype = None
     lib.orc_average_facets.argtypes = [C.c_ulong, PC, PD, PD]
+    lib.orc_ms_read_coords.restype = D
+    lib.orc_ms_read_coords.argtypes = [PD, C.c_uint, PD, PD, PD]
+    lib.orc_ms_read_flag.restype = C.c_ulong
+    lib.orc_ms_read_flag.argtypes = [PU8, C.c_uint, C.c_uint, C.c_uint, PU8]
+    lib.orc_ms_read_vis.restype = None
+    lib.orc_ms_read_vis.argtypes = [PF, C.c_uint, C.c_uint, C.c_uint, PC]
+    lib.orc_ms_read_sigma2.restype = None
+    lib.orc_ms_read_sigma2.argtypes = [PF, C.c_uint, C.c_uint, C.c_float, PF]
+    lib.orc_ms_write_vis.restype = None
+    lib.orc_ms_write_vis.argtypes = [PC, C.c_uint, C.c_uint, PF]
     for nm in ("orc_sersic_shape", "orc_gaussian_shape"):
         getattr(lib, nm).restype = D
         getattr(lib, nm).argtypes = [D, D, D, D]
