@@ -123,3 +123,19 @@ def test_sky_model_and_simulator(orc, gaussian):
         ed = np.max(np.abs(d - data_ref)) / np.max(np.abs(data_ref))
         print(f"precision {prec} gaussian {gaussian}: sky model {es:.2e}, simulated data {ed:.2e}")
         assert es < tol and ed < tol
+
+
+@pytest.mark.parametrize("n_ch,gaussian", [(16, 0), (32, 0), (16, 1)])
+def test_batched_full_chunks(orc, n_ch, gaussian):
+    """The batched path on 16 and 32 channels, where most work items are single-run 16-channel
+    chunks (the kernels' fast path; 16 channels: the single-chunk variant with compile-time channel
+    constants) and the galaxy profiles come from the chunk polynomials, against the oracle's
+    one-galaxy-at-a-time data_processing."""
+    case = Case(n_ant=40, ha_hours=2.0, dt_s=600.0, n_ch=n_ch, n_gal=12, fmin=30.0, fmax=200.0, noise=1500.0,
+                flag_frac=0.01, gaussian=bool(gaussian))
+    sky = oracle_sky_model(orc, case)
+    _, _, _, _, ref = oracle_data_processing(orc, case, case.data, sky)
+    dev = _dev(case, sky, _lib.RLF_MIXED)
+    pr = dev.process(case.cat, batch=12, refit=False, gaussian=gaussian, rounds=3)
+    dev.close()
+    _compare(pr.results, ref, 1e-4, f"{n_ch} channels, gaussian {gaussian}")
