@@ -672,16 +672,20 @@ int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, cons
 
 // ---------------------------------------------------------------- removal
 // grid-stride over (row, chunk of kRemCh channels); galaxies staged through shared memory in
-// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  POLY: the profiles of a chunk from
-// its cubic in dl (profile_poly), one profile evaluation per model, galaxy and chunk.
+// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  MODE as k_extract_seq: 0 exact
+// per-channel profiles; 1 the profiles of a chunk from its cubic in dl (profile_poly), one profile
+// evaluation per model, galaxy and chunk; 2 as 1 with exactly one 16-channel chunk (compile-time
+// channel constants).
 static_assert(kRemCh == kChunk, "removal chunks must be the chunks of the channel polynomials");
-template <int GAUSS, bool POLY>
+template <int GAUSS, int MODE>
 __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __restrict__ rows, float2* data,
                                                       float2* sky, const GalaxyParams* __restrict__ gals,
                                                       const FitOut* __restrict__ fit, int n_gal) {
+  constexpr bool POLY = MODE > 0;
+  constexpr bool ONE = MODE == 2;
   __shared__ GalF sg[kRemTile];
-  const int nch = c_bnch;
-  const int nchunk = (nch + kRemCh - 1) / kRemCh;
+  const int nch = ONE ? kChunk : c_bnch;
+  const int nchunk = ONE ? 1 : (nch + kRemCh - 1) / kRemCh;
   const long long total = (long long)n_rows * nchunk;
   const long long stride = (long long)gridDim.x * blockDim.x;
   // all threads of the block iterate the same number of times so that the tiles can be shared
@@ -689,8 +693,8 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
   for (long long it = 0; it < iters; ++it) {
     const long long t = it * stride + blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const bool live = t < total;
-    const int r = live ? (int)(t % n_rows) : 0;
-    const int ch0 = live ? (int)(t / n_rows) * kRemCh : 0;
+    const int r = live ? (ONE ? (int)t : (int)(t % n_rows)) : 0;
+    const int ch0 = ONE ? 0 : (live ? (int)(t / n_rows) * kRemCh : 0);
     RowF rw = rows[r];
     float ar[kRemCh], ai[kRemCh], br[kRemCh], bi[kRemCh];
 #pragma unroll
@@ -774,14 +778,15 @@ int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = sms * 4;
-  const int poly = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
-  if (gaussian) {
-    if (poly) k_remove_batch<1, true><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
-    else k_remove_batch<1, false><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
-  } else {
-    if (poly) k_remove_batch<0, true><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
-    else k_remove_batch<0, false><<<blocks, 256, 0, st>>>(n_rows, rows, data, sky, gals, fit, n_gal);
-  }
+  const bool known = dev >= 0 && dev < 64;
+  const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+  const void* kernels[2][3] = {{(const void*)k_remove_batch<0, 0>, (const void*)k_remove_batch<0, 1>,
+                                (const void*)k_remove_batch<0, 2>},
+                               {(const void*)k_remove_batch<1, 0>, (const void*)k_remove_batch<1, 1>,
+                                (const void*)k_remove_batch<1, 2>}};
+  void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&data, (void*)&sky, (void*)&gals, (void*)&fit, (void*)&n_gal};
+  const cudaError_t le = cudaLaunchKernel(kernels[gaussian ? 1 : 0][mode], dim3(blocks), dim3(256), args, 0, st);
+  if (le != cudaSuccess) { fprintf(stderr, "rlf: k_remove_batch: %s\n", cudaGetErrorString(le)); return (int)le; }
   return check("k_remove_batch");
 }
 
