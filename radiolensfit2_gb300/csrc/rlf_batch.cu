@@ -795,13 +795,16 @@ int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
 // (data_simulation.c:131-165, sky_model) or the sheared models for the simulator
 // (data_simulation.c:41-127 with galaxy_visibilities.c:154-190).  Thread per (row, 16-channel
 // chunk), galaxies staged in shared memory; per (row, galaxy) the double-float delay and two
-// sin/cos of the phase, per channel a phase recurrence and the profile.
-template <int GAUSS, int SHEARED>
+// sin/cos of the phase, per channel a phase recurrence and the profile (MODE as k_extract_seq: 0
+// exact profiles, 1 chunk polynomials, 2 chunk polynomials with one 16-channel chunk).
+template <int GAUSS, int SHEARED, int MODE>
 __global__ void __launch_bounds__(256) k_model_sum_batch(int n_rows, const RowF* __restrict__ rows, float2* vis,
                                                          const GalaxyParams* __restrict__ gals, int n_gal) {
+  constexpr bool POLY = MODE > 0;
+  constexpr bool ONE = MODE == 2;
   __shared__ GalF sg[kRemTile];
-  const int nch = c_bnch;
-  const int nchunk = (nch + kRemCh - 1) / kRemCh;
+  const int nch = ONE ? kChunk : c_bnch;
+  const int nchunk = ONE ? 1 : (nch + kRemCh - 1) / kRemCh;
   const long long total = (long long)n_rows * nchunk;
   const long long stride = (long long)gridDim.x * blockDim.x;
   // all threads of the block iterate the same number of times so that the tiles can be shared
@@ -809,8 +812,8 @@ __global__ void __launch_bounds__(256) k_model_sum_batch(int n_rows, const RowF*
   for (long long it = 0; it < iters; ++it) {
     const long long t = it * stride + blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const bool live = t < total;
-    const int r = live ? (int)(t % n_rows) : 0;
-    const int ch0 = live ? (int)(t / n_rows) * kRemCh : 0;
+    const int r = live ? (ONE ? (int)t : (int)(t % n_rows)) : 0;
+    const int ch0 = ONE ? 0 : (live ? (int)(t / n_rows) * kRemCh : 0);
     const RowF rw = rows[r];
     const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
     float ar[kRemCh], ai[kRemCh];
@@ -828,17 +831,28 @@ __global__ void __launch_bounds__(256) k_model_sum_batch(int n_rows, const RowF*
         const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
         const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
         float zr, zi, ws, wc;
-        sincos_turn(turns_at(T0, dT, ch0), &zi, &zr);  // exp(+2 pi i T): the model phase
+        sincos_turn(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zi, &zr);  // exp(+2 pi i T)
         sincos_turn(dT.hi + dT.lo, &ws, &wc);
         const float q = SHEARED ? g.A * uu + g.B * rw.uv + g.Cc * vv : rw.q;
         const float sf = SHEARED ? g.sf1 : g.sf0;
+        float cp[4];
+        if (POLY) {
+          profile_poly<GAUSS>(sf * c_chunk[ch0 / kChunk].wn2c * q, cp);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) cp[j] *= g.flux;
+        }
 #pragma unroll
         for (int k = 0; k < kRemCh; ++k) {
           const int ch = ch0 + k;
           if (ch < nch) {
             const BatchChan bc = c_bch[ch];
-            const float x = sf * bc.wn2 * q;
-            const float a = (GAUSS ? __expf(-0.5f * x) : round_shape(x)) * bc.spec * g.flux;
+            float a;
+            if (POLY) {
+              a = bc.spec * poly3(cp, bc.dl);
+            } else {
+              const float x = sf * bc.wn2 * q;
+              a = (GAUSS ? __expf(-0.5f * x) : round_shape(x)) * bc.spec * g.flux;
+            }
             ar[k] = fmaf(a, zr, ar[k]);
             ai[k] = fmaf(a, zi, ai[k]);
             const float nzr = fmaf(zr, wc, -zi * ws);
@@ -871,13 +885,16 @@ int launch_model_sum_batch(int n_rows, const RowF* rows, float2* vis, const Gala
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = sms * 4;
-  if (gaussian) {
-    if (sheared) k_model_sum_batch<1, 1><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
-    else k_model_sum_batch<1, 0><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
-  } else {
-    if (sheared) k_model_sum_batch<0, 1><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
-    else k_model_sum_batch<0, 0><<<blocks, 256, 0, st>>>(n_rows, rows, vis, gals, n_gal);
-  }
+  const bool known = dev >= 0 && dev < 64;
+  const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+#define RLF_MS_K(G, S) {(const void*)k_model_sum_batch<G, S, 0>, (const void*)k_model_sum_batch<G, S, 1>, \
+                        (const void*)k_model_sum_batch<G, S, 2>}
+  const void* kernels[2][2][3] = {{RLF_MS_K(0, 0), RLF_MS_K(0, 1)}, {RLF_MS_K(1, 0), RLF_MS_K(1, 1)}};
+#undef RLF_MS_K
+  void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&vis, (void*)&gals, (void*)&n_gal};
+  const cudaError_t le = cudaLaunchKernel(kernels[gaussian ? 1 : 0][sheared ? 1 : 0][mode], dim3(blocks), dim3(256),
+                                          args, 0, st);
+  if (le != cudaSuccess) { fprintf(stderr, "rlf: k_model_sum_batch: %s\n", cudaGetErrorString(le)); return (int)le; }
   return check("k_model_sum_batch");
 }
 

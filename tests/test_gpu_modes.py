@@ -93,12 +93,12 @@ def test_batched_two_passes(orc):
     assert np.max(np.abs(s - s2)) < 1e-5 * np.max(np.abs(sky))
 
 
-@pytest.mark.parametrize("gaussian", [0, 1])
-def test_sky_model_and_simulator(orc, gaussian):
+@pytest.mark.parametrize("gaussian,n_ch", [(0, 8), (1, 8), (0, 16), (1, 16)])
+def test_sky_model_and_simulator(orc, gaussian, n_ch):
     """rlf_obs_sky_model (round models, data_simulation.c:131-165) and the noise-free
     rlf_obs_simulate (sheared models) against the oracle's per-galaxy, per-channel model
-    visibilities (galaxy_visibilities.c:154-190)."""
-    case = Case(n_ant=48, ha_hours=2.0, dt_s=600.0, n_ch=8, n_gal=12, fmin=30.0, fmax=200.0, noise=0.0,
+    visibilities (galaxy_visibilities.c:154-190); 16 channels take the single-chunk kernels."""
+    case = Case(n_ant=48, ha_hours=2.0, dt_s=600.0, n_ch=n_ch, n_gal=12, fmin=30.0, fmax=200.0, noise=0.0,
                 gaussian=bool(gaussian))
     o, c = case.obs, case.cat
     sky_ref = oracle_sky_model(orc, case)
