@@ -177,13 +177,29 @@ __global__ void k_grid_weights(Observation o, const uint16_t* cell, const float*
   double* ws = sm + nc;
   for (int i = threadIdx.x; i < 2 * nc; i += blockDim.x) sm[i] = 0.0;
   __syncthreads();
+  // a row's consecutive channels mostly fall in one cell: sum each run locally, one atomic pair per run
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < o.n_rows; row += gridDim.x * blockDim.x) {
+    uint16_t cur = kNoCell;
+    double s_run = 0.0, w_run = 0.0;
     for (int ch = 0; ch < c_nch; ++ch) {
       const long long idx = row * o.lay.s_row + ch * o.lay.s_ch;
       const uint16_t c = cell[idx];
       if (c == kNoCell) continue;
-      atomicAdd(&ss[c], (double)sigma2[idx]);
-      atomicAdd(&ws[c], 1.0);
+      if (c != cur) {
+        if (cur != kNoCell) {
+          atomicAdd(&ss[cur], s_run);
+          atomicAdd(&ws[cur], w_run);
+        }
+        cur = c;
+        s_run = 0.0;
+        w_run = 0.0;
+      }
+      s_run += (double)sigma2[idx];
+      w_run += 1.0;
+    }
+    if (cur != kNoCell) {
+      atomicAdd(&ss[cur], s_run);
+      atomicAdd(&ws[cur], w_run);
     }
   }
   __syncthreads();
