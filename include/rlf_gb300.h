@@ -160,7 +160,10 @@ int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
  * stats[RLF_STAT_CHANGED]         galaxies whose fit still changed in the last round of their
  *                                 sub-batch (ellipticity by more than 1e-9 or the error flag),
  * stats[RLF_STAT_EXTRACT_GAL_FIRST] the part of RLF_STAT_EXTRACT_GAL in first rounds (no model
- *                                 differences removed). */
+ *                                 differences removed),
+ * stats[RLF_STAT_SKIPPED_GAL]     galaxy rounds not run because they could not change: the galaxies
+ *                                 of a sub-batch up to the first good fit of the round before, and
+ *                                 every later round of a sub-batch without good fits. */
 enum {
   RLF_STAT_EXTRACT_PASSES = 0,
   RLF_STAT_EXTRACT_SINGLE = 1,
@@ -170,7 +173,8 @@ enum {
   RLF_STAT_EXTRACT_GAL = 5,
   RLF_STAT_CHANGED = 6,
   RLF_STAT_EXTRACT_GAL_FIRST = 7,
-  RLF_NSTATS = 8
+  RLF_STAT_SKIPPED_GAL = 8,
+  RLF_NSTATS = 9
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
 

@@ -517,16 +517,41 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
+    // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the
+    // fitted - round model differences of round r's good fits among the galaxies before k, round r
+    // with those of round r-1 (none before round 1); a good fit's difference moves between rounds,
+    // a bad fit's is zero.  So galaxy k keeps its facet and fit unless a galaxy before it was good
+    // in round r or r-1: the next round starts at the first such galaxy (it is extracted again for
+    // its model difference), and none means the unit has converged.
+    int j0 = 0;
+    std::vector<char> good_prev(u.seq ? bn : 0, 0);
     for (int rd = 0; rd < nr; ++rd) {
+      const int bj = b0 + j0, bk = bn - j0;
+      SeqBatch sr = sb;
+      FacetBatch fr = fb;
+      FacetOut fq = fo;
+      fq.offset = doff.p + j0;
+      fq.ncoords = dnc.p + bj;
+      fr.n_gal = bk;
+      fr.offset = doff.p + j0;
+      fr.count = dnc.p + bj;
+      fr.rprior = dprior.p + (size_t)bj * kMaxNodes;
+      fr.start = opt.start ? dstart.p + (size_t)3 * bj : nullptr;
+      fr.out = dout.p + bj;
       // ---- extraction
       if (u.seq) {
-        sb.fit = rd == 0 ? nullptr : dout.p + b0;
+        sr.n_gal = bk;
+        sr.gals = dg.p + bj;
+        sr.fidx = dfidx.p + bj;
+        sr.foff = dfoff.p + bj;
+        sr.facet = dfac.p + bj;
+        sr.fit = rd == 0 ? nullptr : dout.p + bj;
         ob->stats[RLF_STAT_EXTRACT_PASSES] += 1;
-        ob->stats[RLF_STAT_EXTRACT_GAL] += bn;
-        if (rd == 0) ob->stats[RLF_STAT_EXTRACT_GAL_FIRST] += bn;
-        RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sb, opt.gaussian, seq_ctas,
+        ob->stats[RLF_STAT_EXTRACT_GAL] += bk;
+        if (rd == 0) ob->stats[RLF_STAT_EXTRACT_GAL_FIRST] += bk;
+        RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sr, opt.gaussian, seq_ctas,
                                   ob->bpartial.p, st));
-        RLF_OK(launch_finalize_seq(sb, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, ob->len, fo, st));
+        RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + bj, dsw.p + bj, ob->len, fq, st));
       } else {
         const int i = b0;
         const unsigned F = (unsigned)facets[i];
@@ -544,24 +569,42 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       RLF_OK(pt.mark(kPhaseExtract, st));
       if (facets_out) break;
       // ---- fit
-      if (u.seq && rd == nr - 1 && nr > 1)
+      const bool last = rd == nr - 1;
+      if (u.seq && last && nr > 1)
         RLF_CUDA(copy_async(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
       RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
-      if (fb.board.slot) {
-        RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bn * sizeof(SampleSlot), st));
-        RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)bn * 2 * kBoardCap * sizeof(int), st));
-        RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)bn * sizeof(int), st));
+      if (fr.board.slot) {
+        RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bk * sizeof(SampleSlot), st));
+        RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)bk * 2 * kBoardCap * sizeof(int), st));
+        RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)bk * sizeof(int), st));
         RLF_CUDA(cudaMemsetAsync(bdone.p, 0, sizeof(int), st));
       }
-      ob->stats[RLF_STAT_FITTED] += bn;
+      ob->stats[RLF_STAT_FITTED] += bk;
       // with the board, CTAs beyond the galaxy count start as helpers of the sampling grids
-      RLF_OK(fit_launch(fb, fprec, fb.board.slot ? grid_fit : std::min(grid_fit, bn), st));
-      if (u.seq && rd == nr - 1 && nr > 1) {
+      RLF_OK(fit_launch(fr, fprec, fr.board.slot ? grid_fit : std::min(grid_fit, bk), st));
+      if (u.seq && last && nr > 1) {
         k_count_changed<<<(bn + 127) / 128, 128, 0, st>>>(bn, dprev.p, dout.p + b0, 1e-9, dchanged.p);
         count_launch();
         RLF_CUDA(cudaGetLastError());
       }
       RLF_OK(pt.mark(kPhaseFit, st));
+      if (u.seq && !last) {
+        std::vector<FitOut> h(bk);
+        RLF_CUDA(copy_async(h.data(), dout.p + bj, bk * sizeof(FitOut), cudaMemcpyDeviceToHost, st));
+        RLF_CUDA(cudaStreamSynchronize(st));
+        int first = bn;
+        for (int k = 0; k < bk; ++k) {
+          const char good = h[k].error == 0;
+          if (first == bn && (good || good_prev[j0 + k])) first = j0 + k;
+          good_prev[j0 + k] = good;
+        }
+        if (first == bn) {
+          ob->stats[RLF_STAT_SKIPPED_GAL] += (long long)bn * (nr - 1 - rd);
+          break;
+        }
+        j0 = first;
+        ob->stats[RLF_STAT_SKIPPED_GAL] += j0;
+      }
     }
     if (facets_out) {
       // extraction only: hand the packed facets of this unit back as doubles

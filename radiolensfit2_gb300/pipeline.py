@@ -139,10 +139,11 @@ class DeviceObservation:
         res = np.frombuffer(out, dtype=RESULT_DTYPE, count=cat.n).copy()
         ms = (C.c_double * 4)()
         self.lib.rlf_obs_last_timing(self.h, ms)
-        sv = (C.c_longlong * 8)()
+        names = ("extract_passes", "extract_single", "remove_batches", "remove_single", "fitted",
+                 "extract_gal", "changed", "extract_gal_first", "skipped_gal")  # RLF_NSTATS entries
+        sv = (C.c_longlong * len(names))()
         self.lib.rlf_obs_last_stats(self.h, sv)
-        stats = dict(zip(("extract_passes", "extract_single", "remove_batches", "remove_single", "fitted",
-                          "extract_gal", "changed", "extract_gal_first"), (int(x) for x in sv[:8])))
+        stats = dict(zip(names, (int(x) for x in sv)))
         return ProcessResult(res, nbad.value, tuple(ms), stats)
 
     def extract(self, cat: Catalogue, *, batch: int = 1):
