@@ -22,7 +22,7 @@ int launch_row_table(int n_rows, const double* uu, const double* vv, const doubl
                      cudaStream_t st);
 // ---- sequential batch extraction (exact in-batch removal order)
 #ifndef RLF_SEQ_THREADS
-#define RLF_SEQ_THREADS 768
+#define RLF_SEQ_THREADS 1024
 #endif
 #ifndef RLF_SEQ_CTAS_PER_SM
 #define RLF_SEQ_CTAS_PER_SM 1
