@@ -474,6 +474,7 @@ struct FitShared {
   // sampling board: a claimed grid point and its chunk (owner and helper CTAs)
   SampleSlot claim_prm;
   int claim_g, claim_seq, claim_idx, claim_state;
+  int bcast_np;
   int status;
 };
 
@@ -1459,6 +1460,9 @@ __device__ __noinline__ void likelihood_sampling(FitCtx<P>& c, typename P::S* me
         c.seq++;
         board_chunk<P>(c, c.seq, prm);
         const size_t row = board_row(c.g, c.seq);
+        // the accumulation runs on thread 0 alone: only it writes the galaxy's result, and the
+        // replicated FP64 arithmetic (an exp per point) would cost every warp of the CTA
+        if (threadIdx.x == 0)
         for (int k = 0; k < prm.npts; ++k) {
           const int e = c.board.err[row + k];
           if (e < 0) continue;
@@ -1486,6 +1490,11 @@ __device__ __noinline__ void likelihood_sampling(FitCtx<P>& c, typename P::S* me
           }
         }
       }
+      // the level's point count decides the next level for every thread
+      if (threadIdx.x == 0) c.sh->bcast_np = np;
+      __syncthreads();
+      np = c.sh->bcast_np;
+      __syncthreads();
     } else {
       for (ie1 = lo1; (float)ie1 <= q1; ie1 += 2) {
         for (ie2 = lo2; (float)ie2 <= q2; ie2 += 2) {
