@@ -38,6 +38,9 @@ struct BatchChunk {
 constexpr int kChunks = kMaxCh / 16;
 __constant__ BatchChan c_bch[kMaxCh];
 __constant__ BatchChunk c_chunk[kChunks];
+// moments of the channels before and from channel s of a chunk: [chunk][s][0..3] = sum_{k<s},
+// [4..7] = sum_{k>=s} of spec_k dl_k^j (the two runs of a chunk crossing a cell boundary at s)
+__constant__ float c_chunk_split[kChunks][17][8];
 __constant__ int c_chunk_poly;
 static int g_chunk_poly[64];  // host copy of c_chunk_poly per device (selects the kernel variant)
 static int g_nch[64];         // host copy of c_bnch per device
@@ -70,6 +73,7 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   if (worst * max_delay_m > 1e-9) return -1;
   static BatchChan h[kMaxCh];
   static BatchChunk hc[kChunks];
+  static float hs[kChunks][17][8];
   double dmax = 0.0;
   for (int c0 = 0; c0 < n_ch; c0 += 16) {
     const int c1 = std::min(n_ch, c0 + 16);
@@ -94,6 +98,19 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
     BatchChunk& k = hc[c0 / 16];
     k.wn2c = (float)wc;
     for (int j = 0; j < 4; ++j) k.mom[j] = (float)mom[j];
+    for (int sp = 0; sp <= 16; ++sp) {
+      double pre[4] = {0, 0, 0, 0}, suf[4] = {0, 0, 0, 0};
+      for (int c = c0; c < c1; ++c) {
+        const double d = wavenumbers[c] * wavenumbers[c] / wc - 1.0;
+        double dp = 1.0;
+        for (int j = 0; j < 4; ++j) {
+          if (c - c0 < sp) pre[j] += spec[c] * dp;
+          else suf[j] += spec[c] * dp;
+          dp *= d;
+        }
+      }
+      for (int j = 0; j < 4; ++j) { hs[c0 / 16][sp][j] = (float)pre[j]; hs[c0 / 16][sp][4 + j] = (float)suf[j]; }
+    }
     k.pad[0] = k.pad[1] = k.pad[2] = 0.f;
   }
   // truncation of the cubic: below 2.5 dl^4 of the peak (exponential profile; less for the
@@ -110,6 +127,8 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk, hc, sizeof(BatchChunk) * ((n_ch + 15) / 16), 0,
                                                      cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_poly, &poly, 4, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_split, hs, sizeof(float) * 17 * 8 * ((n_ch + 15) / 16), 0,
+                                                     cudaMemcpyHostToDevice, st);
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
     g_chunk_poly[dev] = poly;
@@ -242,10 +261,11 @@ __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(siz
 
 size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes) {
   return align16((size_t)total_cells * sizeof(float2)) + align16((size_t)n_gal * sizeof(SeqGal)) +
-         (size_t)n_sizes * kSeqThreads * sizeof(uint32_t);
+         (size_t)n_sizes * kSeqThreads * (sizeof(uint32_t) + sizeof(uint16_t));
 }
 
-__global__ void k_cell_desc(int n_rows, int nch, const uint16_t* __restrict__ cell, uint32_t* __restrict__ desc) {
+__global__ void k_cell_desc(int n_rows, int nch, const uint16_t* __restrict__ cell, uint32_t* __restrict__ desc,
+                            uint16_t* __restrict__ desc1) {
   const int nchunk = (nch + kChunk - 1) / kChunk;
   const long long total = (long long)n_rows * nchunk;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -260,50 +280,80 @@ __global__ void k_cell_desc(int n_rows, int nch, const uint16_t* __restrict__ ce
       if (ch >= nch || c == kNoCell || cell[(size_t)ch * n_rows + r] != c) mask |= 1u << k;
     }
     desc[t] = (uint32_t)c | (mask << 16);
+    // two runs: the first cell valid, the other channels a suffix s..15 inside the observation,
+    // all in one cell
+    uint16_t c1 = kNotTwoRun;
+    if (mask && c != kNoCell) {
+      const int sp = __ffs(mask) - 1;
+      const uint32_t suffix = (0xFFFFu << sp) & 0xFFFFu;
+      if (mask == suffix && c0 + kChunk <= nch) {
+        const uint16_t cs = cell[(size_t)(c0 + sp) * n_rows + r];
+        bool same = true;
+        for (int k = sp + 1; k < kChunk; ++k) same = same && cell[(size_t)(c0 + k) * n_rows + r] == cs;
+        if (same) c1 = cs;
+      }
+    }
+    desc1[t] = c1;
   }
 }
 
-int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, cudaStream_t st) {
+int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, uint16_t* desc1, cudaStream_t st) {
   const long long total = (long long)n_rows * ((n_ch + kChunk - 1) / kChunk);
   const int blocks = (int)std::min<long long>((total + 255) / 256, 8192);
-  k_cell_desc<<<blocks, 256, 0, st>>>(n_rows, n_ch, cell, desc);
+  k_cell_desc<<<blocks, 256, 0, st>>>(n_rows, n_ch, cell, desc, desc1);
   return check("k_cell_desc");
 }
 
 // Work items (row, chunk) of a batch split into "simple" ones, one run of 16 valid channels for
-// every facet size of the batch (front of items, count in *n_simple), and the others (back), so
-// that the extraction runs each kind without divergence between the lanes of a warp.
-__global__ void k_classify_items(long long total, SeqBatch b, int* __restrict__ items, int* __restrict__ n_simple,
-                                 int* __restrict__ n_complex) {
+// every facet size of the batch (front of items, count in counters[0]), "two-run" ones, at most
+// two runs for every facet size (items2, counters[2]; only when two_run), and the general others
+// (back of items, counters[1]), so that the extraction runs each kind without divergence between
+// the lanes of a warp.
+__global__ void k_classify_items(long long total, SeqBatch b, int two_run, int* __restrict__ items,
+                                 int* __restrict__ items2, int* __restrict__ counters) {
   const int lane = threadIdx.x & 31;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   // whole warps walk 32 consecutive items per step (the ballots below need every lane)
   for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < total; w += nwarps) {
     const long long t = w * 32 + lane;
     const bool live = t < total;
-    bool simple = live;
+    bool simple = live, two = live && two_run;
     if (live)
-      for (int f = 0; f < b.n_sizes; ++f) simple = simple && (b.desc[f][t] >> 16) == 0;
+      for (int f = 0; f < b.n_sizes; ++f) {
+        const bool one = (b.desc[f][t] >> 16) == 0;
+        simple = simple && one;
+        two = two && (one || b.desc1[f][t] != kNotTwoRun);
+      }
+    two = two && !simple;
+    const bool general = live && !simple && !two;
     const unsigned ms = __ballot_sync(0xffffffffu, simple);
-    const unsigned mc = __ballot_sync(0xffffffffu, live && !simple);
-    int s0 = 0, c0 = 0;
+    const unsigned mt = __ballot_sync(0xffffffffu, two);
+    const unsigned mg = __ballot_sync(0xffffffffu, general);
+    int s0 = 0, t0 = 0, g0 = 0;
     if (lane == 0) {
-      if (ms) s0 = atomicAdd(n_simple, __popc(ms));
-      if (mc) c0 = atomicAdd(n_complex, __popc(mc));
+      if (ms) s0 = atomicAdd(&counters[0], __popc(ms));
+      if (mg) g0 = atomicAdd(&counters[1], __popc(mg));
+      if (mt) t0 = atomicAdd(&counters[2], __popc(mt));
     }
     s0 = __shfl_sync(0xffffffffu, s0, 0);
-    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    g0 = __shfl_sync(0xffffffffu, g0, 0);
+    t0 = __shfl_sync(0xffffffffu, t0, 0);
     const unsigned below = (1u << lane) - 1u;
     if (simple) items[s0 + __popc(ms & below)] = (int)t;
-    else if (live) items[total - 1 - (c0 + __popc(mc & below))] = (int)t;
+    else if (two) items2[t0 + __popc(mt & below)] = (int)t;
+    else if (general) items[total - 1 - (g0 + __popc(mg & below))] = (int)t;
   }
 }
 
-int launch_classify_items(long long total, const SeqBatch& b, int* items, int* counters, cudaStream_t st) {
-  const cudaError_t e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), st);
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
+                          cudaStream_t st) {
+  const cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(int), st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: classify: %s\n", cudaGetErrorString(e)); return (int)e; }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int two_run = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
   const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
-  k_classify_items<<<blocks, 256, 0, st>>>(total, b, items, counters, counters + 1);
+  k_classify_items<<<blocks, 256, 0, st>>>(total, b, two_run, items, items2, counters);
   return check("k_classify_items");
 }
 
@@ -517,6 +567,115 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
 #undef XB
 }
 
+// one work item whose chunk is, for every facet size of the batch, one run or two runs: channels
+// 0..s-1 in the chunk's first cell, s..15 in a second cell (a row's uv point crossing a cell
+// boundary within the chunk).  As the single-run path with a deposit per run: in the first round
+// two Horner sums split at s, the second one rotated by the phase at channel s; in the correction
+// rounds the phase recurrence with the rotated residual summed per run; the round model of each
+// run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).
+template <int GAUSS, int MODE>
+__device__ __forceinline__ void seq_item2(int t, int n_rows, const RowF* __restrict__ rows,
+                                          const float2* __restrict__ data, const float2* __restrict__ sky,
+                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, uint16_t* d1cache,
+                                          float2* acc) {
+  constexpr bool ONE = MODE == 2;
+  const int tid = threadIdx.x;
+  const int r = ONE ? t : t % n_rows;
+  const int c0 = ONE ? 0 : (t / n_rows) * kChunk;
+  const int ci = c0 / kChunk;
+  const RowF rw = rows[r];
+  float pr[kChunk], pi[kChunk];
+#pragma unroll
+  for (int k = 0; k < kChunk; ++k) {
+    const size_t idx = (size_t)(c0 + k) * n_rows + r;
+    const float2 d = data[idx], sk = sky[idx];
+    pr[k] = d.x - sk.x;
+    pi[k] = d.y - sk.y;
+  }
+  for (int f = 0; f < b.n_sizes; ++f) {
+    dcache[f * kSeqThreads + tid] = b.desc[f][t];
+    d1cache[f * kSeqThreads + tid] = b.desc1[f][t];
+  }
+  const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
+  const float invq = rw.q > 0.f ? 1.f / rw.q : 0.f;
+  const float xq = c_chunk[ci].wn2c * rw.q;
+  for (int j = 0; j < b.n_gal; ++j) {
+    const SeqGal s = sg[j];
+    const GalF& g = s.g;
+    const f2 p = delay_df(rw, g);
+    const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
+    const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
+    float ws, wc, zs, zc;
+    sincos_turn(dT.hi + dT.lo, &ws, &wc);
+    sincos_turn(c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0), &zs, &zc);
+    const float wr = wc, wi = -ws;    // w = exp(-2 pi i dT)
+    const float zr0 = zc, zi0 = -zs;  // exp(-2 pi i T(c0))
+    const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
+    const uint32_t mask = d >> 16;
+    const int split = mask ? __ffs(mask) - 1 : kChunk;
+    const int cell_a = (int)(d & 0xffffu);
+    const uint16_t cell_b = d1cache[s.fidx * kSeqThreads + tid];
+    float2* fac = acc + s.off;
+    const float f1 = s.apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
+    float c0p[4], dfp[4];
+    profile_poly<GAUSS>(g.sf0 * xq, c0p);
+    if (s.apply) {
+      float c1p[4];
+      profile_poly<GAUSS>(f1 * xq, c1p);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dfp[q] = g.flux * (c1p[q] - c0p[q]);
+    }
+    const float* ms = c_chunk_split[ci][split];
+    const float rs_a = fmaf(c0p[3], ms[3], fmaf(c0p[2], ms[2], fmaf(c0p[1], ms[1], c0p[0] * ms[0])));
+    const float rs_b = fmaf(c0p[3], ms[7], fmaf(c0p[2], ms[6], fmaf(c0p[1], ms[5], c0p[0] * ms[4])));
+    float ar, ai, br, bi;  // the rotated residual of each run
+    if (!s.apply) {
+      // Horner from channel 15 down: run B (from s) relative to channel s, then run A from channel 0
+      float sr = 0.f, si = 0.f, hr = 0.f, hi = 0.f;
+#pragma unroll
+      for (int k = kChunk - 1; k >= 0; --k) {
+        if (k == split - 1) { hr = sr; hi = si; sr = 0.f; si = 0.f; }
+        const float nr_ = fmaf(sr, wr, fmaf(-si, wi, pr[k]));
+        const float ni_ = fmaf(sr, wi, fmaf(si, wr, pi[k]));
+        sr = nr_;
+        si = ni_;
+      }
+      ar = fmaf(sr, zr0, -si * zi0);
+      ai = fmaf(sr, zi0, si * zr0);
+      br = bi = 0.f;
+      if (split < kChunk) {
+        float ys, yc;
+        sincos_turn(turns_at(T0, dT, c0 + split), &ys, &yc);  // exp(-2 pi i T(c0 + s)) = yc - i ys
+        br = fmaf(hr, yc, hi * ys);
+        bi = fmaf(hi, yc, -hr * ys);
+      }
+    } else {
+      float zr = zr0, zi = zi0;
+      ar = ai = br = bi = 0.f;
+#pragma unroll
+      for (int k = 0; k < kChunk; ++k) {
+        const float tr = fmaf(pr[k], zr, -pi[k] * zi);
+        const float ti = fmaf(pr[k], zi, pi[k] * zr);
+        if (k < split) { ar += tr; ai += ti; }
+        else { br += tr; bi += ti; }
+        const float a = c_bch[c0 + k].spec * poly3(dfp, c_bch[c0 + k].dl);
+        pr[k] = fmaf(-a, zr, pr[k]);
+        pi[k] = fmaf(a, zi, pi[k]);
+        const float nzr = fmaf(zr, wr, -zi * wi);
+        const float nzi = fmaf(zr, wi, zi * wr);
+        zr = nzr;
+        zi = nzi;
+      }
+    }
+    atomicAdd(&fac[cell_a].x, fmaf(rs_a, g.flux, ar));
+    atomicAdd(&fac[cell_a].y, ai);
+    if (split < kChunk && cell_b != kNoCell) {
+      atomicAdd(&fac[cell_b].x, fmaf(rs_b, g.flux, br));
+      atomicAdd(&fac[cell_b].y, bi);
+    }
+  }
+}
+
 template <int GAUSS, int MODE>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
@@ -527,6 +686,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
   SeqGal* sg = reinterpret_cast<SeqGal*>(smem_raw + align16((size_t)b.total_cells * sizeof(float2)));
   uint32_t* dcache = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sg) +
                                                  align16((size_t)b.n_gal * sizeof(SeqGal)));
+  uint16_t* d1cache = reinterpret_cast<uint16_t*>(dcache + (size_t)b.n_sizes * kSeqThreads);
   const int tid = threadIdx.x;
   for (int i = tid; i < b.total_cells; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
   for (int i = tid; i < b.n_gal; i += blockDim.x) {
@@ -554,13 +714,26 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     const int q = base + lane;
     if (q < ns) seq_item<GAUSS, true, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
+  if (MODE > 0) {
+    const int nt = *b.n_two;
+    while (true) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&b.queue[2], 32);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= nt) break;
+      const int q = base + lane;
+      if (q < nt) seq_item2<GAUSS, MODE>(b.items2[q], n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
+    }
+  }
+  // the general items fill the back of the list
+  const int ng = b.n_simple[1];
   while (true) {
     int base = 0;
     if (lane == 0) base = atomicAdd(&b.queue[1], 32);
     base = __shfl_sync(0xffffffffu, base, 0);
-    const int q = ns + base + lane;
-    if (ns + base >= total) break;
-    if (q < total) seq_item<GAUSS, false, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (base >= ng) break;
+    const int q = total - ng + base + lane;
+    if (base + lane < ng) seq_item<GAUSS, false, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;
@@ -576,7 +749,7 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   }
   const size_t smem = seq_smem_bytes(b.n_gal, b.total_cells, b.n_sizes);
   if (smem > 227 * 1024) { fprintf(stderr, "rlf: sequential extraction batch too large (%zu B)\n", smem); return 1; }
-  const cudaError_t qe = cudaMemsetAsync(b.queue, 0, 2 * sizeof(int), st);
+  const cudaError_t qe = cudaMemsetAsync(b.queue, 0, 3 * sizeof(int), st);
   if (qe != cudaSuccess) { fprintf(stderr, "rlf: extraction queue: %s\n", cudaGetErrorString(qe)); return (int)qe; }
   int dev = 0;
   cudaGetDevice(&dev);

@@ -40,7 +40,11 @@ constexpr size_t kSeqFacetBudget = (size_t)RLF_SEQ_FACET_KB * 1024;  // shared f
 // first channel in bits 0-15, bit 16+k set when channel k of the chunk is flagged, beyond the last
 // channel or in another cell (so 0 in the high half = one run over all 16 channels).
 // desc: [chunk][row]; cell: [ch][row] (launch_cell_index).
-int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, cudaStream_t st);
+// desc1: [chunk][row] the cell of channels s..15 when the chunk is two runs, channels 0..s-1 in the
+// first cell and s..15 (all within the observation) in one second cell (kNoCell: flagged), with
+// s the first set mask bit; kNotTwoRun otherwise.
+constexpr uint16_t kNotTwoRun = 0xFFFE;
+int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, uint16_t* desc1, cudaStream_t st);
 
 struct SeqBatch {
   int n_gal;
@@ -54,16 +58,21 @@ struct SeqBatch {
   int total_cells;            // sum of facet^2 over the batch
   int n_sizes;
   const uint32_t* desc[kSeqMaxSizes];
+  const uint16_t* desc1[kSeqMaxSizes];
   const uint16_t* cells[kSeqMaxSizes];
   const int* items;           // work items (row, 16-channel chunk) = chunk * n_rows + row: the
-  const int* n_simple;        // *n_simple single-run ones first, then the others
-  int* queue;                 // [2] work counters of the extraction (single-run, other items),
-                              // zeroed by launch_extract_seq
+  const int* n_simple;        // *n_simple single-run ones first, then the general ones
+  const int* items2;          // work items of at most two runs per facet size, count *n_two
+  const int* n_two;
+  int* queue;                 // [3] work counters of the extraction (single-run, general, two-run
+                              // items), zeroed by launch_extract_seq
 };
 size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes);
-// split the batch's work items into single-run ones (front) and the others (back) for
-// launch_extract_seq; items: [n_rows * chunks], counters: [2] (simple, other)
-int launch_classify_items(long long total, const SeqBatch& b, int* items, int* counters, cudaStream_t st);
+// split the batch's work items into single-run ones (front of items), general ones (back of items)
+// and ones of at most two runs for every facet size (items2; only with chunk polynomials), for
+// launch_extract_seq; items, items2: [n_rows * chunks], counters: [3] (simple, general, two-run)
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
+                          cudaStream_t st);
 // partial: [ctas][total_cells] float2
 int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
                        int gaussian, int ctas, float2* partial, cudaStream_t st);

@@ -146,6 +146,7 @@ struct FacetCache {
   DevBuf<uint16_t> cell;
   DevBuf<double> ss, sw;
   DevBuf<uint32_t> desc;   // run descriptors of the sequential batch extraction (built on first use)
+  DevBuf<uint16_t> desc1;  // second-run cells of the two-run chunks
 };
 
 struct Timing {
@@ -172,7 +173,8 @@ struct rlf_observation {
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
   rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
   rlf::DevBuf<int> items;           // work items of the sequential batch extraction
-  rlf::DevBuf<int> item_count;      // [4] simple / other work items, then the extraction's work counters
+  rlf::DevBuf<int> items2;          // its two-run work items
+  rlf::DevBuf<int> item_count;      // [6] simple / general / two-run work items, then the extraction's work counters
   double max_delay_m = 0;
   int n_part = 0;
   double ms[4] = {0, 0, 0, 0};
@@ -501,20 +503,25 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         RLF_OK(obs_facet(ob, (unsigned)unit_sizes[ui][f], &fcF, st));
         if (!fcF->desc.p) {
           RLF_OK(fcF->desc.ensure((size_t)ob->n_rows * ((ob->n_ch + 15) / 16)));
-          RLF_OK(launch_cell_desc(ob->n_rows, ob->n_ch, fcF->cell.p, fcF->desc.p, st));
+          RLF_OK(fcF->desc1.ensure((size_t)ob->n_rows * ((ob->n_ch + 15) / 16)));
+          RLF_OK(launch_cell_desc(ob->n_rows, ob->n_ch, fcF->cell.p, fcF->desc.p, fcF->desc1.p, st));
         }
         sb.desc[f] = fcF->desc.p;
+        sb.desc1[f] = fcF->desc1.p;
         sb.cells[f] = fcF->cell.p;
       }
       RLF_OK(ob->bpartial.ensure((size_t)seq_ctas * sb.total_cells));
       const long long n_items = (long long)ob->n_rows * ((ob->n_ch + 15) / 16);
       if (n_items > 0x7fffffffLL - (1LL << 24)) { fprintf(stderr, "rlf: %lld row-chunks exceed the batched extraction\n", n_items); return 1; }
       RLF_OK(ob->items.ensure((size_t)n_items));
-      RLF_OK(ob->item_count.ensure(4));
+      RLF_OK(ob->items2.ensure((size_t)n_items));
+      RLF_OK(ob->item_count.ensure(6));
       sb.items = ob->items.p;
+      sb.items2 = ob->items2.p;
       sb.n_simple = ob->item_count.p;
-      sb.queue = ob->item_count.p + 2;
-      RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->item_count.p, st));
+      sb.n_two = ob->item_count.p + 2;
+      sb.queue = ob->item_count.p + 3;
+      RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->items2.p, ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
     // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the
