@@ -269,6 +269,13 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
     return sub.n / dt, dt, res
 
 
+# DRAM bytes of one k_extract_seq launch per row of the observation, from the ncu capture of
+# profiles/k_extract_seq_mid_128ant_16ch.md (dram__bytes_read.sum + dram__bytes_write.sum =
+# 403.2 MB + 6.7 MB over 975,360 rows); a launch reads data, sky model, the row table, the work-item
+# list and the run descriptors once per row, so the traffic of a launch grows with the rows
+EXTRACT_DRAM_BYTES_PER_ROW = (403.183104e6 + 6.673152e6) / 975360
+
+
 def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak):
     """Roofline of the dominant stage of a step.
 
@@ -299,6 +306,13 @@ def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_p
          "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
          "traffic": None, "time_ms_per_step": stage_ms[dominant], "passes": st}
     r["frac"] = r["achieved"] / hbm_peak if r["achieved"] else None
+    if dominant == "extract":
+        # per launch, from the mid-size capture scaled by rows (this workload is too large for a
+        # multi-pass capture); algorithmic bytes per launch beside it
+        r["traffic"] = EXTRACT_DRAM_BYTES_PER_ROW * n_rows
+        r["traffic_algorithmic"] = 16.0 * n_vis + 32.0 * n_rows
+        r["traffic_source"] = ("ncu DRAM bytes of one k_extract_seq launch on mid_128ant_16ch "
+                               "(profiles/k_extract_seq_mid_128ant_16ch.md), scaled by rows")
     if flops:
         # the batched passes are FP32-pipe bound (profiles, phase recurrences), not HBM bound
         r["compute"] = {"bound": "fp32", "unit": "TFLOP/s", "achieved": flops / t / 1e12,
