@@ -304,19 +304,87 @@ int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc,
   return check("k_cell_desc");
 }
 
+__device__ __forceinline__ int order_bin(double u, double v, double il0, double scale, double len) {
+  int bu = (int)floor((u * il0 + len) * scale), bv = (int)floor((v * il0 + len) * scale);
+  bu = min(max(bu, 0), kOrderBins - 1);
+  bv = min(max(bv, 0), kOrderBins - 1);
+  return bv * kOrderBins + bu;
+}
+__global__ void k_order_count(int n_rows, const double* __restrict__ uu, const double* __restrict__ vv, double il0,
+                              double scale, double len, int* __restrict__ bins) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x)
+    atomicAdd(&bins[order_bin(uu[r], vv[r], il0, scale, len)], 1);
+}
+// exclusive prefix sum of the kOrderBins^2 bin counts in place: one block of kOrderBins threads, each
+// over kOrderBins consecutive bins
+__global__ void __launch_bounds__(kOrderBins) k_order_scan(int* __restrict__ bins) {
+  __shared__ int sums[kOrderBins];
+  int* mine = bins + (size_t)threadIdx.x * kOrderBins;
+  int s = 0;
+  for (int k = 0; k < kOrderBins; ++k) s += mine[k];
+  sums[threadIdx.x] = s;
+  __syncthreads();
+  // Hillis-Steele inclusive scan of the per-thread sums
+  for (int o = 1; o < kOrderBins; o <<= 1) {
+    const int x = threadIdx.x >= o ? sums[threadIdx.x - o] : 0;
+    __syncthreads();
+    sums[threadIdx.x] += x;
+    __syncthreads();
+  }
+  int run = sums[threadIdx.x] - s;
+  for (int k = 0; k < kOrderBins; ++k) {
+    const int c = mine[k];
+    mine[k] = run;
+    run += c;
+  }
+}
+__global__ void k_order_place(int n_rows, const double* __restrict__ uu, const double* __restrict__ vv, double il0,
+                              double scale, double len, int* __restrict__ bins, int* __restrict__ order) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x)
+    order[atomicAdd(&bins[order_bin(uu[r], vv[r], il0, scale, len)], 1)] = r;
+}
+
+int launch_row_order(int n_rows, const double* uu, const double* vv, double inv_lambda0, double len, int* order,
+                     int* bins, cudaStream_t st) {
+  if (n_rows <= 0) return 0;
+  const double scale = len > 0 ? kOrderBins / (2 * len) : 0.0;
+  const cudaError_t e = cudaMemsetAsync(bins, 0, sizeof(int) * kOrderBins * kOrderBins, st);
+  if (e != cudaSuccess) { fprintf(stderr, "rlf: row order: %s\n", cudaGetErrorString(e)); return (int)e; }
+  const int blocks = std::min((n_rows + 255) / 256, 4096);
+  k_order_count<<<blocks, 256, 0, st>>>(n_rows, uu, vv, inv_lambda0, scale, len, bins);
+  int r = check("k_order_count");
+  if (r) return r;
+  k_order_scan<<<1, kOrderBins, 0, st>>>(bins);
+  r = check("k_order_scan");
+  if (r) return r;
+  k_order_place<<<blocks, 256, 0, st>>>(n_rows, uu, vv, inv_lambda0, scale, len, bins, order);
+  return check("k_order_place");
+}
+
 // Work items (row, chunk) of a batch split into "simple" ones, one run of 16 valid channels for
 // every facet size of the batch (front of items, count in counters[0]), "two-run" ones, at most
 // two runs for every facet size (items2, counters[2]; only when two_run), and the general others
 // (back of items, counters[1]), so that the extraction runs each kind without divergence between
-// the lanes of a warp.
-__global__ void k_classify_items(long long total, SeqBatch b, int two_run, int* __restrict__ items,
-                                 int* __restrict__ items2, int* __restrict__ counters) {
-  const int lane = threadIdx.x & 31;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  // whole warps walk 32 consecutive items per step (the ballots below need every lane)
-  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < total; w += nwarps) {
-    const long long t = w * 32 + lane;
-    const bool live = t < total;
+// the lanes of a warp.  A block takes 256 consecutive positions of the row order and places each
+// class's items contiguously, in that order, with one counter update per class.
+constexpr int kClassifyThreads = 256;
+__global__ void __launch_bounds__(kClassifyThreads) k_classify_items(long long total, int n_rows,
+                                                                     const int* __restrict__ order, SeqBatch b,
+                                                                     int two_run, int* __restrict__ items,
+                                                                     int* __restrict__ items2,
+                                                                     int* __restrict__ counters) {
+  constexpr int kWarps = kClassifyThreads / 32;
+  __shared__ int wcount[3][kWarps];
+  __shared__ int bbase[3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long p0 = (long long)blockIdx.x * kClassifyThreads; p0 < total; p0 += (long long)gridDim.x * kClassifyThreads) {
+    const long long tp = p0 + threadIdx.x;
+    const bool live = tp < total;
+    long long t = 0;
+    if (live) {
+      const long long ch = tp / n_rows, i = tp - ch * n_rows;
+      t = ch * n_rows + (order ? order[i] : i);
+    }
     bool simple = live, two = live && two_run;
     if (live)
       for (int f = 0; f < b.n_sizes; ++f) {
@@ -326,35 +394,70 @@ __global__ void k_classify_items(long long total, SeqBatch b, int two_run, int* 
       }
     two = two && !simple;
     const bool general = live && !simple && !two;
-    const unsigned ms = __ballot_sync(0xffffffffu, simple);
-    const unsigned mt = __ballot_sync(0xffffffffu, two);
-    const unsigned mg = __ballot_sync(0xffffffffu, general);
-    int s0 = 0, t0 = 0, g0 = 0;
-    if (lane == 0) {
-      if (ms) s0 = atomicAdd(&counters[0], __popc(ms));
-      if (mg) g0 = atomicAdd(&counters[1], __popc(mg));
-      if (mt) t0 = atomicAdd(&counters[2], __popc(mt));
+    const unsigned m[3] = {__ballot_sync(0xffffffffu, simple), __ballot_sync(0xffffffffu, general),
+                           __ballot_sync(0xffffffffu, two)};
+    if (lane == 0)
+      for (int k = 0; k < 3; ++k) wcount[k][warp] = __popc(m[k]);
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      int n = 0;
+      for (int w = 0; w < kWarps; ++w) n += wcount[threadIdx.x][w];
+      bbase[threadIdx.x] = n ? atomicAdd(&counters[threadIdx.x], n) : 0;
     }
-    s0 = __shfl_sync(0xffffffffu, s0, 0);
-    g0 = __shfl_sync(0xffffffffu, g0, 0);
-    t0 = __shfl_sync(0xffffffffu, t0, 0);
-    const unsigned below = (1u << lane) - 1u;
-    if (simple) items[s0 + __popc(ms & below)] = (int)t;
-    else if (two) items2[t0 + __popc(mt & below)] = (int)t;
-    else if (general) items[total - 1 - (g0 + __popc(mg & below))] = (int)t;
+    __syncthreads();
+    const int k = simple ? 0 : (general ? 1 : 2);
+    if (live) {
+      int pos = bbase[k] + __popc(m[k] & ((1u << lane) - 1u));
+      for (int w = 0; w < warp; ++w) pos += wcount[k][w];
+      if (k == 0) items[pos] = (int)t;
+      else if (k == 2) items2[pos] = (int)t;
+      else items[total - 1 - pos] = (int)t;
+    }
+    __syncthreads();
   }
 }
 
-int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
-                          cudaStream_t st) {
+int launch_classify_items(long long total, int n_rows, const int* order, const SeqBatch& b, int* items,
+                          int* items2, int* counters, cudaStream_t st) {
   const cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(int), st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: classify: %s\n", cudaGetErrorString(e)); return (int)e; }
   int dev = 0;
   cudaGetDevice(&dev);
   const int two_run = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
-  const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
-  k_classify_items<<<blocks, 256, 0, st>>>(total, b, two_run, items, items2, counters);
+  const int blocks = (int)std::min<long long>((total + kClassifyThreads - 1) / kClassifyThreads, 4096);
+  k_classify_items<<<blocks, kClassifyThreads, 0, st>>>(total, n_rows, order, b, two_run, items, items2, counters);
   return check("k_classify_items");
+}
+
+// The deposits of a warp's lanes into one galaxy's facet (key: the lane's cell, negative for none).
+// Float atomic adds to shared memory from several lanes of an instruction to one address are
+// retried lane by lane, and with the rows in uv order most warps have all their lanes in one cell
+// of the small facets.  So when every lane has the same cell the 32 values are summed exactly as
+// integers (redux.sync) on the fixed-point grid of 2^-24 .. 2^-25 of the largest magnitude (a
+// power of two, so the scaling is exact; the sum stays below 2^30) and one lane adds the sum;
+// otherwise, or for non-finite values, each lane adds its own.  All 32 lanes must call it.
+__device__ __forceinline__ void warp_deposit(float2* fac, int key, float vr, float vi, int lane) {
+  const int k0 = __shfl_sync(0xffffffffu, key, 0);
+  if (__all_sync(0xffffffffu, key == k0) && k0 >= 0) {
+    // non-negative floats order as their bit patterns; NaN patterns are above infinity
+    const unsigned mb = __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(vr)), __float_as_uint(fabsf(vi))));
+    const int e = (int)(mb >> 23);  // biased exponent of the largest magnitude
+    if (e >= 24 && e < 255) {
+      const float sc = __uint_as_float((unsigned)(278 - e) << 23);  // 2^(151 - e)
+      const float inv = __uint_as_float((unsigned)(e - 24) << 23);  // 2^(e - 151)
+      const int sr = __reduce_add_sync(0xffffffffu, __float2int_rn(vr * sc));
+      const int si = __reduce_add_sync(0xffffffffu, __float2int_rn(vi * sc));
+      if (lane == 0) {
+        atomicAdd(&fac[k0].x, (float)sr * inv);
+        atomicAdd(&fac[k0].y, (float)si * inv);
+      }
+      return;
+    }
+  }
+  if (key >= 0) {
+    atomicAdd(&fac[key].x, vr);
+    atomicAdd(&fac[key].y, vi);
+  }
 }
 
 // sin(2 pi t) and cos(2 pi t) for a phase in turns: quadrant q = rint(4t), remainder
@@ -412,9 +515,10 @@ __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(
 // one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order.
 // MODE 0: exact per-channel profiles; 1: the profiles from the chunk polynomial, one profile
 // evaluation per galaxy and chunk; 2: as 1 for an observation of exactly one 16-channel chunk, so
-// that the channel constants are compile-time operands.
+// that the channel constants are compile-time operands.  Single-run items (SIMPLE) are called by
+// all lanes of a warp (run_deposit), a lane without an item with live = false and any valid t.
 template <int GAUSS, bool SIMPLE, int MODE>
-__device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF* __restrict__ rows,
+__device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
   constexpr bool POLY = MODE > 0;
@@ -528,27 +632,38 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
         cr = fmaf(rs, g.flux, ar);
         ci = ai;
       }
-      const int c = (int)(d & 0xffffu);
-      atomicAdd(&fac[c].x, cr);
-      atomicAdd(&fac[c].y, ci);
+      warp_deposit(fac, live ? (int)(d & 0xffffu) : -1, cr, ci, tid & 31);
     } else {
-      // flagged channels, several cells or a short chunk: channel by channel
+      // flagged channels, several cells or a short chunk: channel by channel, each run of
+      // channels in one cell summed before its deposit
       const uint16_t* cl = b.cells[s.fidx];
       const uint16_t cell0 = (uint16_t)(d & 0xffffu);
       const uint32_t mask = d >> 16;
       float zr = zr0, zi = zi0;
+      int cur = kNoCell;
+      float ur = 0.f, ui = 0.f;
 #pragma unroll
       for (int k = 0; k < kChunk; ++k) {
         if (k < nk) {
           const float spec = c_bch[c0 + k].spec;
           const float xbk = XB(k);
           const float s0 = POLY ? poly3(c0p, c_bch[c0 + k].dl) : profile(g.sf0 * xbk, GAUSS);
-          const uint16_t c = (mask & (1u << k)) ? cl[(size_t)(c0 + k) * n_rows + r] : cell0;
+          const int c = (mask & (1u << k)) ? (int)cl[(size_t)(c0 + k) * n_rows + r] : (int)cell0;
           if (c != kNoCell) {
             const float cr = fmaf(pr[k], zr, fmaf(-pi[k], zi, s0 * spec * g.flux));
             const float ci = fmaf(pr[k], zi, pi[k] * zr);
-            atomicAdd(&fac[c].x, cr);
-            atomicAdd(&fac[c].y, ci);
+            if (c != cur) {
+              if (cur != kNoCell) {
+                atomicAdd(&fac[cur].x, ur);
+                atomicAdd(&fac[cur].y, ui);
+              }
+              cur = c;
+              ur = cr;
+              ui = ci;
+            } else {
+              ur += cr;
+              ui += ci;
+            }
           }
           if (s.apply) {
             const float a = POLY ? spec * poly3(dfp, c_bch[c0 + k].dl)
@@ -562,6 +677,10 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
           zi = nzi;
         }
       }
+      if (cur != kNoCell) {
+        atomicAdd(&fac[cur].x, ur);
+        atomicAdd(&fac[cur].y, ui);
+      }
     }
   }
 #undef XB
@@ -572,9 +691,10 @@ __device__ __forceinline__ void seq_item(int t, int n_rows, int nch, const RowF*
 // boundary within the chunk).  As the single-run path with a deposit per run: in the first round
 // two Horner sums split at s, the second one rotated by the phase at channel s; in the correction
 // rounds the phase recurrence with the rotated residual summed per run; the round model of each
-// run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).
+// run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).  Called by all
+// lanes of a warp, as seq_item's single-run items.
 template <int GAUSS, int MODE>
-__device__ __forceinline__ void seq_item2(int t, int n_rows, const RowF* __restrict__ rows,
+__device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const RowF* __restrict__ rows,
                                           const float2* __restrict__ data, const float2* __restrict__ sky,
                                           const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, uint16_t* d1cache,
                                           float2* acc) {
@@ -667,12 +787,10 @@ __device__ __forceinline__ void seq_item2(int t, int n_rows, const RowF* __restr
         zi = nzi;
       }
     }
-    atomicAdd(&fac[cell_a].x, fmaf(rs_a, g.flux, ar));
-    atomicAdd(&fac[cell_a].y, ai);
-    if (split < kChunk && cell_b != kNoCell) {
-      atomicAdd(&fac[cell_b].x, fmaf(rs_b, g.flux, br));
-      atomicAdd(&fac[cell_b].y, bi);
-    }
+    const int lane = tid & 31;
+    warp_deposit(fac, live ? cell_a : -1, fmaf(rs_a, g.flux, ar), ai, lane);
+    warp_deposit(fac, live && split < kChunk && cell_b != kNoCell ? (int)cell_b : -1, fmaf(rs_b, g.flux, br), bi,
+                 lane);
   }
 }
 
@@ -703,17 +821,21 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
   const int total = (int)((long long)n_rows * ((nch + kChunk - 1) / kChunk));
   const int ns = *b.n_simple;
   const int lane = tid & 31;
-  // each warp takes 32 consecutive items at a time from a device counter, the single-run items
-  // first: the other items cost several times more and a static split would leave their tail to a
-  // few CTAs
+  // Work comes from device counters, the costliest items first so that the cheap single-run ones
+  // even out the end of the launch.  The general items (rare; a deposit per run of channels each)
+  // come in chunks of 32 whose lane l takes item l * chunks + c of the list, so that the rows of a
+  // warp lie far apart in uv and their deposits rarely meet in a cell.
+  const int ng = b.n_simple[1];
+  const int gch = (ng + 31) / 32;
   while (true) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&b.queue[0], 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= ns) break;
-    const int q = base + lane;
-    if (q < ns) seq_item<GAUSS, true, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    int c = 0;
+    if (lane == 0) c = atomicAdd(&b.queue[1], 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= gch) break;
+    const int k = lane * gch + c;
+    if (k < ng) seq_item<GAUSS, false, MODE>(b.items[total - ng + k], true, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
+  // the two-run and single-run items: 32 consecutive items of the list (neighbours in uv) at a time
   if (MODE > 0) {
     const int nt = *b.n_two;
     while (true) {
@@ -722,18 +844,16 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base >= nt) break;
       const int q = base + lane;
-      if (q < nt) seq_item2<GAUSS, MODE>(b.items2[q], n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
+      seq_item2<GAUSS, MODE>(b.items2[min(q, nt - 1)], q < nt, n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
     }
   }
-  // the general items fill the back of the list
-  const int ng = b.n_simple[1];
   while (true) {
     int base = 0;
-    if (lane == 0) base = atomicAdd(&b.queue[1], 32);
+    if (lane == 0) base = atomicAdd(&b.queue[0], 32);
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= ng) break;
-    const int q = total - ng + base + lane;
-    if (base + lane < ng) seq_item<GAUSS, false, MODE>(b.items[q], n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (base >= ns) break;
+    const int q = base + lane;
+    seq_item<GAUSS, true, MODE>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;

@@ -172,6 +172,8 @@ struct rlf_observation {
   rlf::DevBuf<double> partial;
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
   rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
+  rlf::DevBuf<int> order;           // rows in uv order (launch_row_order), built on first use
+  rlf::DevBuf<int> order_bins;      // its bin counts
   rlf::DevBuf<int> items;           // work items of the sequential batch extraction
   rlf::DevBuf<int> items2;          // its two-run work items
   rlf::DevBuf<int> item_count;      // [6] simple / general / two-run work items, then the extraction's work counters
@@ -457,6 +459,12 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     RLF_OK(ob->rows.ensure(ob->n_rows));
     RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
   }
+  if (batched && !ob->order.p) {
+    RLF_OK(ob->order_bins.ensure((size_t)kOrderBins * kOrderBins));
+    RLF_OK(ob->order.ensure(ob->n_rows));
+    RLF_OK(launch_row_order(ob->n_rows, ob->uu.p, ob->vv.p, ob->wavenumbers[0] / (2 * kPi), ob->len, ob->order.p,
+                            ob->order_bins.p, st));
+  }
   PhaseTimer pt;
   RLF_OK(pt.mark(-1, st));
   for (size_t ui = 0; ui < units.size(); ++ui) {
@@ -521,7 +529,8 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       sb.n_simple = ob->item_count.p;
       sb.n_two = ob->item_count.p + 2;
       sb.queue = ob->item_count.p + 3;
-      RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->items2.p, ob->item_count.p, st));
+      RLF_OK(launch_classify_items(n_items, ob->n_rows, ob->order.p, sb, ob->items.p, ob->items2.p,
+                                   ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
     // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the
