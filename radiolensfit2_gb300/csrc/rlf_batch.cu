@@ -517,7 +517,7 @@ __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(
 // evaluation per galaxy and chunk; 2: as 1 for an observation of exactly one 16-channel chunk, so
 // that the channel constants are compile-time operands.  Single-run items (SIMPLE) are called by
 // all lanes of a warp (run_deposit), a lane without an item with live = false and any valid t.
-template <int GAUSS, bool SIMPLE, int MODE>
+template <int GAUSS, bool SIMPLE, int MODE, bool FIT>
 __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
@@ -547,6 +547,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
   for (int j = 0; j < b.n_gal; ++j) {
     const SeqGal s = sg[j];
     const GalF& g = s.g;
+    const bool apply = FIT && s.apply;
     const f2 p = delay_df(rw, g);
     const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
     const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
@@ -559,13 +560,13 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
     const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
     float2* fac = acc + s.off;
     // fitted model: |k'|^2 = A u^2 + B uv + C v^2 (sheared), as a factor on wn^2 (u^2 + v^2)
-    const float f1 = s.apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
+    const float f1 = apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
     // chunk polynomials of the round model (c0p) and of flux * (fitted - round) (dfp)
     float c0p[4], dfp[4];
     if (POLY) {
       const float xq = c_chunk[c0 / kChunk].wn2c * rw.q;
       profile_poly<GAUSS>(g.sf0 * xq, c0p);
-      if (s.apply) {
+      if (apply) {
         float c1p[4];
         profile_poly<GAUSS>(f1 * xq, c1p);
 #pragma unroll
@@ -575,7 +576,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
     if (SIMPLE) {
       // one run: all 16 channels valid and in the cell d & 0xffff
       float cr, ci;
-      if (!s.apply) {
+      if (!apply) {
         float sr = 0.f, si = 0.f, rs = 0.f;
 #pragma unroll
         for (int k = kChunk - 1; k >= 0; --k) {
@@ -665,7 +666,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
               ui += ci;
             }
           }
-          if (s.apply) {
+          if (apply) {
             const float a = POLY ? spec * poly3(dfp, c_bch[c0 + k].dl)
                                  : g.flux * spec * (profile(f1 * xbk, GAUSS) - s0);
             pr[k] = fmaf(-a, zr, pr[k]);
@@ -693,7 +694,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
 // rounds the phase recurrence with the rotated residual summed per run; the round model of each
 // run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).  Called by all
 // lanes of a warp, as seq_item's single-run items.
-template <int GAUSS, int MODE>
+template <int GAUSS, int MODE, bool FIT>
 __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const RowF* __restrict__ rows,
                                           const float2* __restrict__ data, const float2* __restrict__ sky,
                                           const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, uint16_t* d1cache,
@@ -722,6 +723,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
   for (int j = 0; j < b.n_gal; ++j) {
     const SeqGal s = sg[j];
     const GalF& g = s.g;
+    const bool apply = FIT && s.apply;
     const f2 p = delay_df(rw, g);
     const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
     const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
@@ -736,10 +738,10 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
     const int cell_a = (int)(d & 0xffffu);
     const uint16_t cell_b = d1cache[s.fidx * kSeqThreads + tid];
     float2* fac = acc + s.off;
-    const float f1 = s.apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
+    const float f1 = apply ? g.sf1 * (g.A * uu + g.B * rw.uv + g.Cc * vv) * invq : 0.f;
     float c0p[4], dfp[4];
     profile_poly<GAUSS>(g.sf0 * xq, c0p);
-    if (s.apply) {
+    if (apply) {
       float c1p[4];
       profile_poly<GAUSS>(f1 * xq, c1p);
 #pragma unroll
@@ -749,7 +751,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
     const float rs_a = fmaf(c0p[3], ms[3], fmaf(c0p[2], ms[2], fmaf(c0p[1], ms[1], c0p[0] * ms[0])));
     const float rs_b = fmaf(c0p[3], ms[7], fmaf(c0p[2], ms[6], fmaf(c0p[1], ms[5], c0p[0] * ms[4])));
     float ar, ai, br, bi;  // the rotated residual of each run
-    if (!s.apply) {
+    if (!apply) {
       // Horner from channel 15 down: run B (from s) relative to channel s, then run A from channel 0
       float sr = 0.f, si = 0.f, hr = 0.f, hi = 0.f;
 #pragma unroll
@@ -794,7 +796,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
   }
 }
 
-template <int GAUSS, int MODE>
+template <int GAUSS, int MODE, bool FIT>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
                                                                 const float2* __restrict__ sky, SeqBatch b,
@@ -833,7 +835,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= gch) break;
     const int k = lane * gch + c;
-    if (k < ng) seq_item<GAUSS, false, MODE>(b.items[total - ng + k], true, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (k < ng) seq_item<GAUSS, false, MODE, FIT>(b.items[total - ng + k], true, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   // the two-run and single-run items: 32 consecutive items of the list (neighbours in uv) at a time
   if (MODE > 0) {
@@ -844,7 +846,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base >= nt) break;
       const int q = base + lane;
-      seq_item2<GAUSS, MODE>(b.items2[min(q, nt - 1)], q < nt, n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
+      seq_item2<GAUSS, MODE, FIT>(b.items2[min(q, nt - 1)], q < nt, n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
     }
   }
   while (true) {
@@ -853,7 +855,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= ns) break;
     const int q = base + lane;
-    seq_item<GAUSS, true, MODE>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    seq_item<GAUSS, true, MODE, FIT>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
   float2* out = partial + (size_t)blockIdx.x * b.total_cells;
@@ -875,11 +877,18 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   cudaGetDevice(&dev);
   const bool known = dev >= 0 && dev < 64;
   const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
-  const void* kernels[2][3] = {{(const void*)k_extract_seq<0, 0>, (const void*)k_extract_seq<0, 1>,
-                                (const void*)k_extract_seq<0, 2>},
-                               {(const void*)k_extract_seq<1, 0>, (const void*)k_extract_seq<1, 1>,
-                                (const void*)k_extract_seq<1, 2>}};
-  const void* kern = kernels[gaussian ? 1 : 0][mode];
+  // FIT: a correction round (fitted - round model differences to remove); the first round's kernel
+  // leaves that path out
+  const void* kernels[2][2][3] = {
+      {{(const void*)k_extract_seq<0, 0, false>, (const void*)k_extract_seq<0, 1, false>,
+        (const void*)k_extract_seq<0, 2, false>},
+       {(const void*)k_extract_seq<1, 0, false>, (const void*)k_extract_seq<1, 1, false>,
+        (const void*)k_extract_seq<1, 2, false>}},
+      {{(const void*)k_extract_seq<0, 0, true>, (const void*)k_extract_seq<0, 1, true>,
+        (const void*)k_extract_seq<0, 2, true>},
+       {(const void*)k_extract_seq<1, 0, true>, (const void*)k_extract_seq<1, 1, true>,
+        (const void*)k_extract_seq<1, 2, true>}}};
+  const void* kern = kernels[b.fit ? 1 : 0][gaussian ? 1 : 0][mode];
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&data, (void*)&sky, (void*)&b, (void*)&partial};
   const cudaError_t le = cudaLaunchKernel(kern, dim3(ctas), dim3(kSeqThreads), args, smem, st);
