@@ -431,30 +431,37 @@ int launch_classify_items(long long total, int n_rows, const int* order, const S
 
 // The deposits of a warp's lanes into one galaxy's facet (key: the lane's cell, negative for none).
 // Float atomic adds to shared memory from several lanes of an instruction to one address are
-// retried lane by lane, and with the rows in uv order most warps have all their lanes in one cell
-// of the small facets.  So when every lane has the same cell the 32 values are summed exactly as
-// integers (redux.sync) on the fixed-point grid of 2^-24 .. 2^-25 of the largest magnitude (a
-// power of two, so the scaling is exact; the sum stays below 2^30) and one lane adds the sum;
-// otherwise, or for non-finite values, each lane adds its own.  All 32 lanes must call it.
+// retried lane by lane, and with the rows in uv order a warp's lanes mostly fall in one cell of
+// the small facets, or in two at a cell boundary.  So the lanes of each cell (up to four cells)
+// are summed exactly as integers (redux.sync) on the fixed-point grid of 2^-24 .. 2^-25 of the
+// group's largest magnitude (a power of two, so the scaling is exact; the sum stays below 2^30)
+// and the group's first lane adds the sum; lanes of further cells, or of groups with non-finite or
+// tiny values, add their own.  All 32 lanes must call it.
 __device__ __forceinline__ void warp_deposit(float2* fac, int key, float vr, float vi, int lane) {
-  const int k0 = __shfl_sync(0xffffffffu, key, 0);
-  if (__all_sync(0xffffffffu, key == k0) && k0 >= 0) {
-    // non-negative floats order as their bit patterns; NaN patterns are above infinity
-    const unsigned mb = __reduce_max_sync(0xffffffffu, max(__float_as_uint(fabsf(vr)), __float_as_uint(fabsf(vi))));
-    const int e = (int)(mb >> 23);  // biased exponent of the largest magnitude
+  const unsigned mag = max(__float_as_uint(fabsf(vr)), __float_as_uint(fabsf(vi)));  // NaN above inf
+  unsigned todo = __ballot_sync(0xffffffffu, key >= 0), rest = 0;
+#pragma unroll 1
+  for (int it = 0; it < 4 && todo; ++it) {
+    const int src = __ffs(todo) - 1;
+    const int k = __shfl_sync(0xffffffffu, key, src);
+    const bool in = key == k;
+    const unsigned m = __ballot_sync(0xffffffffu, in);
+    const int e = (int)(__reduce_max_sync(0xffffffffu, in ? mag : 0u) >> 23);  // biased exponent
     if (e >= 24 && e < 255) {
       const float sc = __uint_as_float((unsigned)(278 - e) << 23);  // 2^(151 - e)
       const float inv = __uint_as_float((unsigned)(e - 24) << 23);  // 2^(e - 151)
-      const int sr = __reduce_add_sync(0xffffffffu, __float2int_rn(vr * sc));
-      const int si = __reduce_add_sync(0xffffffffu, __float2int_rn(vi * sc));
-      if (lane == 0) {
-        atomicAdd(&fac[k0].x, (float)sr * inv);
-        atomicAdd(&fac[k0].y, (float)si * inv);
+      const int sr = __reduce_add_sync(0xffffffffu, in ? __float2int_rn(vr * sc) : 0);
+      const int si = __reduce_add_sync(0xffffffffu, in ? __float2int_rn(vi * sc) : 0);
+      if (lane == src) {
+        atomicAdd(&fac[k].x, (float)sr * inv);
+        atomicAdd(&fac[k].y, (float)si * inv);
       }
-      return;
+    } else {
+      rest |= m;
     }
+    todo &= ~m;
   }
-  if (key >= 0) {
+  if (((todo | rest) >> lane) & 1u) {
     atomicAdd(&fac[key].x, vr);
     atomicAdd(&fac[key].y, vi);
   }
