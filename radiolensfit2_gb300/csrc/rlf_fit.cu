@@ -466,6 +466,7 @@ struct FitShared {
   S Lr[kMaxNodes];
   S rprior[kMaxNodes];
   S xs[kMaxNodes], ys[kMaxNodes], cs[kMaxNodes];
+  S sb[kMaxNodes], sd[kMaxNodes];         // linear and cubic spline coefficients of each interval
   S qa[kQagCap], qb[kQagCap], qr[kQagCap], qe[kQagCap];
   S bcast_L;
   int bcast_err;
@@ -491,13 +492,23 @@ __device__ __forceinline__ S spline_eval(const FitShared<S>& sh, int n, bool cub
   const S y_lo = sh.ys[lo], y_hi = sh.ys[lo + 1];
   const S dx = x_hi - x_lo, dy = y_hi - y_lo, delx = x - x_lo;
   *ok = true;
-  if (cubic) {
-    const S c_i = sh.cs[lo], c_ip1 = sh.cs[lo + 1];
-    const S b_i = (dy / dx) - dx * (c_ip1 + S(2) * c_i) / S(3);
-    const S d_i = (c_ip1 - c_i) / (S(3) * dx);
-    return y_lo + delx * (b_i + delx * (c_i + delx * d_i));
-  }
+  // cubic: the coefficients of gsl_interp_cspline's evaluation, made once per spline (spline_coeffs)
+  if (cubic) return y_lo + delx * (sh.sb[lo] + delx * (sh.cs[lo] + delx * sh.sd[lo]));
   return y_lo + delx / dx * dy;
+}
+
+// b_i and d_i of every interval of the natural cubic spline (xs, ys, cs), lane i: as the
+// reference's interpolation evaluates them per point (gsl_interp_cspline), once per spline
+template <class S>
+__device__ __forceinline__ void spline_coeffs(FitShared<S>& sh, int n) {
+  const int i = threadIdx.x & 31;
+  if (i < n - 1) {
+    const S dx = sh.xs[i + 1] - sh.xs[i], dy = sh.ys[i + 1] - sh.ys[i];
+    const S c_i = sh.cs[i], c_ip1 = sh.cs[i + 1];
+    sh.sb[i] = (dy / dx) - dx * (c_ip1 + S(2) * c_i) / S(3);
+    sh.sd[i] = (c_ip1 - c_i) / (S(3) * dx);
+  }
+  __syncwarp();
 }
 
 // integrand of marginalise_r.c:231-238: exp(spline(x)), 0 outside the nodes
@@ -708,6 +719,7 @@ __device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
     }
   }
   __syncwarp();
+  spline_coeffs<S>(sh, n);
   if (xmax <= xmin) return S(kBad);  // the reference exits the process here
   S sump;
   int status = qag_warp<S>(sh, n, true, xmin, xmax, &sump);
