@@ -493,6 +493,14 @@ __device__ __forceinline__ void sincos_turn(float t, float* s, float* c) {
   *c = (qi & 2) ? -c1 : c1;
 }
 
+// sin and cos of 2 pi t for |t| <= 1/2 from the SFU (__sincosf: absolute error below 2^-21.4 on
+// [-pi, pi]), for a phase that no recurrence amplifies: the first channel of a chunk, or of a
+// chunk's second run.  The channel step exp(-2 pi i dT), raised to the 15th power by the
+// recurrence, keeps sincos_turn.
+__device__ __forceinline__ void sincos_turn_sfu(float t, float* s, float* c) {
+  __sincosf(6.28318530717958647692f * t, s, c);
+}
+
 __device__ __forceinline__ float profile(float x, int gauss) {
   return gauss ? __expf(-0.5f * x) : round_shape(x);
 }
@@ -561,7 +569,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
     float ws, wc, zs, zc;
     sincos_turn(dT.hi + dT.lo, &ws, &wc);
     const float ta = c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0);
-    sincos_turn(ta, &zs, &zc);
+    sincos_turn_sfu(ta, &zs, &zc);
     const float wr = wc, wi = -ws;    // w = exp(-2 pi i dT)
     const float zr0 = zc, zi0 = -zs;  // exp(-2 pi i T(c0))
     const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
@@ -736,7 +744,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
     const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
     float ws, wc, zs, zc;
     sincos_turn(dT.hi + dT.lo, &ws, &wc);
-    sincos_turn(c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0), &zs, &zc);
+    sincos_turn_sfu(c0 == 0 ? (T0.hi + T0.lo) : turns_at(T0, dT, c0), &zs, &zc);
     const float wr = wc, wi = -ws;    // w = exp(-2 pi i dT)
     const float zr0 = zc, zi0 = -zs;  // exp(-2 pi i T(c0))
     const uint32_t d = dcache[s.fidx * kSeqThreads + tid];
@@ -774,7 +782,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
       br = bi = 0.f;
       if (split < kChunk) {
         float ys, yc;
-        sincos_turn(turns_at(T0, dT, c0 + split), &ys, &yc);  // exp(-2 pi i T(c0 + s)) = yc - i ys
+        sincos_turn_sfu(turns_at(T0, dT, c0 + split), &ys, &yc);  // exp(-2 pi i T(c0 + s)) = yc - i ys
         br = fmaf(hr, yc, hi * ys);
         bi = fmaf(hi, yc, -hr * ys);
       }
@@ -1022,7 +1030,7 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
         const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
         const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
         float zs, zc, ws, wc;
-        sincos_turn(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
+        sincos_turn_sfu(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
         sincos_turn(dT.hi + dT.lo, &ws, &wc);
         float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
         const float k1q = g.A * (rw.u_hi * rw.u_hi) + g.B * rw.uv + g.Cc * (rw.v_hi * rw.v_hi);
