@@ -50,6 +50,8 @@ __constant__ double c_invk[kInvTab];       // 1 / k
 __constant__ double c_invfact[kEiTerms];   // 1 / k!
 __constant__ double c_ei_tab[kEiTab];      // Ei(k), computed on the host in extended precision
 __constant__ double c_exp_tab[kEiTab];     // e^k
+__constant__ float2 c_invk2[kInvTab];       // 1 / k as a float pair (hi, lo)
+__constant__ float2 c_invfact2[kEiTerms];   // 1 / k! as a float pair
 
 struct FitConst {
   int numr;
@@ -771,16 +773,6 @@ __device__ __forceinline__ void ei_pair_lane(double x1, double x2, double* e1, d
   *e2 = ser2 ? kEulerGamma + log(x2) + a2 : c_ei_tab[k2] + c_exp_tab[k2] * a2;
 }
 
-// likelihood.c:376-421 for one lane's own x
-__device__ double pos_marg_lane(double x) {
-  const double Delta = 0.5 * 5.991;
-  if (x <= Delta) return kBad;
-  if (x > 100.) return x - log(Delta) - exp(-Delta);
-  if ((x - Delta) < 0.0001) x = Delta + 0.0001;
-  double yc, ys;
-  ei_pair_lane(x, x - Delta, &yc, &ys);
-  return log((yc - ys) / log(x / (x - Delta)));
-}
 
 // ---- double-float (unevaluated sum of two floats) arithmetic for sin/cos on the FP32 pipes
 __device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
@@ -799,6 +791,138 @@ __device__ __forceinline__ double df_to_double(f2 a) { return (double)a.hi + (do
 // P * y + c
 __device__ __forceinline__ f2 df_horner(f2 P, f2 y, float c_hi, float c_lo) {
   return df_add(df_mul(P, y), f2{c_hi, c_lo});
+}
+
+// ---- double-float division, square root, exp and log for the fit's serial phases.  Dependent
+// FP64 operations on this GPU take 64 cycles (fma) to ~550 (division), ~700 (square root), ~1150
+// (exp) and ~2100 (log); an FP32 fma ~5 and a double-float multiply ~22.  Each function works to
+// the pair's precision (~2^-47 relative).
+__device__ __forceinline__ f2 df_sqr(f2 a) {
+  f2 p = two_prod(a.hi, a.hi);
+  p.lo = fmaf(2.f * a.hi, a.lo, p.lo);
+  return quick_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ f2 df_scale(f2 a, float s) { return f2{a.hi * s, a.lo * s}; }  // s a power of 2
+// a / b: the quotient of the high parts from an approximate reciprocal, refined twice by the
+// double-float remainder a - q b
+__device__ __forceinline__ f2 df_div(f2 a, f2 b) {
+  const float r = __fdividef(1.f, b.hi);
+  const float q1 = a.hi * r;
+  f2 rem = df_sub(a, df_mul(f2{q1, 0.f}, b));
+  const float q2 = rem.hi * r;
+  f2 q = quick_two_sum(q1, q2);
+  rem = df_sub(a, df_mul(q, b));
+  return df_add(q, f2{rem.hi * r, 0.f});
+}
+// sqrt(a), a > 0: s = a rsqrt(a) refined twice by s + (a - s^2) / (2 s)
+__device__ __forceinline__ f2 df_sqrt(f2 a) {
+  const float y = rsqrtf(a.hi);
+  f2 s{a.hi * y, 0.f};
+  f2 e = df_sub(a, df_sqr(s));
+  s = df_add(s, f2{e.hi * 0.5f * y, 0.f});
+  e = df_sub(a, df_sqr(s));
+  return df_add(s, f2{e.hi * 0.5f * y, 0.f});
+}
+// exp(a): a = k ln2 + r, |r| <= ln2 / 2, with ln2 split in three so that k * (first part) is exact
+// and k * (second part) exact as a pair; exp(r) = exp(r / 8)^8 with exp(r / 8) from its Taylor
+// series to degree 10 (remainder below 1e-23); 0 below the float range, inf above it
+__constant__ float2 c_df_invfact[11] = {
+    {1.0f, 0.f}, {1.0f, 0.f}, {0.5f, 0.f}, {0.1666666716337204f, -4.967053879312289e-09f},
+    {0.0416666679084301f, -1.2417634698280722e-09f}, {0.008333333767950535f, -4.34617203337595e-10f},
+    {0.0013888889225199819f, -3.3631094437103215e-11f}, {0.00019841270113829523f, -2.725596874933456e-12f},
+    {2.4801587642286904e-05f, -3.40699609366682e-13f}, {2.7557318844628753e-06f, 3.793571224297229e-14f},
+    {2.755731998149713e-07f, -7.575112209051195e-15f}};
+__device__ __forceinline__ f2 df_exp(f2 a) {
+  if (a.hi < -87.f) return f2{0.f, 0.f};
+  if (a.hi > 88.f) return f2{__int_as_float(0x7f800000), 0.f};
+  const float k = rintf(a.hi * 1.4426950216293335f);
+  f2 r = df_add(a, f2{-k * 0.693115234375f, 0.f});      // 2839 / 4096: 12 significant bits
+  r = df_sub(r, two_prod(k, 3.194618329871446e-05f));
+  r = df_add(r, f2{-k * 1.6465949697480609e-12f, 0.f});
+  const f2 t = df_scale(r, 0.125f);
+  f2 p{c_df_invfact[10].x, c_df_invfact[10].y};
+#pragma unroll
+  for (int n = 9; n >= 0; --n) p = df_add(df_mul(p, t), f2{c_df_invfact[n].x, c_df_invfact[n].y});
+  p = df_sqr(df_sqr(df_sqr(p)));
+  // 2^k in two factors, each inside the float exponent range
+  const int ki = (int)k, k1 = ki / 2, k2 = ki - k1;
+  const float s1 = __int_as_float((k1 + 127) << 23), s2 = __int_as_float((k2 + 127) << 23);
+  return df_scale(df_scale(p, s1), s2);
+}
+// e ln2 as a pair (|e| < 2^11: the first product is exact)
+__device__ __forceinline__ f2 df_ln2_times(float e) {
+  f2 l = df_add(two_prod(e, 3.194618329871446e-05f), f2{e * 1.6465949697480609e-12f, 0.f});
+  return df_add(f2{e * 0.693115234375f, 0.f}, l);
+}
+// log(a), a > 0 within the float range: y0 = log(a.hi) from the SFU, then
+// log(a) = y0 + log(1 + d), d = a exp(-y0) - 1 (|d| ~1e-6): y0 + d - d^2 / 2
+__device__ __forceinline__ f2 df_log(f2 a) {
+  const float y0 = __logf(a.hi);
+  const f2 d = df_sub(df_mul(a, df_exp(f2{-y0, 0.f})), f2{1.f, 0.f});
+  return df_add(f2{y0, 0.f}, df_add(d, f2{-0.5f * d.hi * d.hi, 0.f}));
+}
+// log(x) of a positive normal double of any magnitude: x = m 2^e with m in [1, 2) split into a
+// float pair from its bits (the low part's 29 bits rounded to 24), log m + e ln2
+__device__ __forceinline__ f2 df_log_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  const unsigned long long frac = b & 0x000fffffffffffffull;
+  const float hi = __uint_as_float(0x3f800000u | (unsigned)(frac >> 29));
+  const float lo = (float)(unsigned)(frac & 0x1fffffffull) * 2.220446049250313e-16f;  // 2^-52
+  return df_add(df_log(quick_two_sum(hi, lo)), df_ln2_times((float)e));
+}
+
+// Ei(x1) and Ei(x2) as ei_pair_lane, the expansions' recurrences in double-float on the FP32 pipes
+// (this GPU's FP64 pipe is 1/64 of FP32 and shared by the SM's CTAs; the lane chains were bound
+// by its latency); each expansion stops at its first term below 2^-53 of its sum, under the
+// pair's ~2^-48 precision.  The closing sums and the tables stay in double.
+__device__ __forceinline__ f2 df_c(float2 v) { return f2{v.x, v.y}; }
+__device__ __forceinline__ void ei_pair_df(double x1, double x2, double* e1, double* e2) {
+  const bool ser1 = x1 <= 2.5, ser2 = x2 <= 2.5;
+  const int k1 = ser1 ? 0 : (int)(x1 + 0.5), k2 = ser2 ? 0 : (int)(x2 + 0.5);
+  const f2 s1 = df_from_double(ser1 ? x1 : x1 - k1), s2 = df_from_double(ser2 ? x2 : x2 - k2);
+  const f2 i1 = df_c(c_invk2[k1]), i2 = df_c(c_invk2[k2]);
+  // series: c = s^k / k!, term c / k;  Taylor: c = c_k, p = s^(k+1), term c p / (k+1)
+  f2 c1 = ser1 ? f2{1.f, 0.f} : i1, c2 = ser2 ? f2{1.f, 0.f} : i2;
+  f2 p1 = s1, p2 = s2;
+  f2 a1 = ser1 ? f2{0.f, 0.f} : df_mul(i1, s1), a2 = ser2 ? f2{0.f, 0.f} : df_mul(i2, s2);
+  bool run1 = true, run2 = true;
+  for (int k = 1; k < kEiTerms - 1 && (run1 || run2); ++k) {
+    const f2 ik = df_c(c_invk2[k]), ik1 = df_c(c_invk2[k + 1]), ifk = df_c(c_invfact2[k]);
+    if (run1) {
+      f2 t;
+      if (ser1) { c1 = df_mul(df_mul(c1, s1), ik); t = df_mul(c1, ik); }
+      else { c1 = df_mul(df_sub(ifk, c1), i1); p1 = df_mul(p1, s1); t = df_mul(df_mul(c1, p1), ik1); }
+      a1 = df_add(a1, t);
+      if (fabsf(t.hi) < 1.1102230246251565e-16f * fabsf(a1.hi)) run1 = false;
+    }
+    if (run2) {
+      f2 t;
+      if (ser2) { c2 = df_mul(df_mul(c2, s2), ik); t = df_mul(c2, ik); }
+      else { c2 = df_mul(df_sub(ifk, c2), i2); p2 = df_mul(p2, s2); t = df_mul(df_mul(c2, p2), ik1); }
+      a2 = df_add(a2, t);
+      if (fabsf(t.hi) < 1.1102230246251565e-16f * fabsf(a2.hi)) run2 = false;
+    }
+  }
+  const double d1 = df_to_double(a1), d2 = df_to_double(a2);
+  *e1 = ser1 ? kEulerGamma + log(x1) + d1 : c_ei_tab[k1] + c_exp_tab[k1] * d1;
+  *e2 = ser2 ? kEulerGamma + log(x2) + d2 : c_ei_tab[k2] + c_exp_tab[k2] * d2;
+}
+
+// likelihood.c:376-421 for one lane's own x = S^2 / 2, with - log(det) / 2 of likelihood.c:171
+// added (det > 0): the logs and quotients in double-float.  log(Delta) and exp(-Delta) are the
+// double values of the reference's expressions.
+__device__ double pos_marg_lane(double x, double det) {
+  const double Delta = 0.5 * 5.991;
+  if (x <= Delta) return kBad;
+  const f2 ld = df_log_double(det);
+  if (x > 100.) return x - 1.0971111625418426 - 0.05001161502657909 - 0.5 * df_to_double(ld);
+  if ((x - Delta) < 0.0001) x = Delta + 0.0001;
+  double yc, ys;
+  ei_pair_df(x, x - Delta, &yc, &ys);
+  // log((yc - ys) / log(x / (x - Delta))) - log(det) / 2
+  const f2 lr = df_log(df_div(df_from_double(x), df_from_double(x - Delta)));
+  return df_to_double(df_sub(df_sub(df_log_double(yc - ys), df_log(lr)), df_scale(ld, 0.5f)));
 }
 
 // sin and cos of a double |a| <= pi/4 from their Taylor series (coefficients 1/n!, split into
@@ -1083,9 +1207,8 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
   if (mine) {
     double L = kBad;
     if (det > 0) {
-      L = pos_marg_lane((Sval * Sval) * 0.5);
+      L = pos_marg_lane((Sval * Sval) * 0.5, det);
       if (isnan(L)) L = kBad;
-      else if (L != kBad) L = L - 0.5 * log(det);
     }
     sh.Lr[lane] = typename P::S(L);
   }
@@ -1877,6 +2000,17 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invfact, invfact, sizeof(invfact), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_ei_tab, eitab, sizeof(eitab), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_exp_tab, exptab, sizeof(exptab), 0, cudaMemcpyHostToDevice, st);
+  static float2 invk2[kInvTab], invfact2[kEiTerms];
+  for (int k = 0; k < kInvTab; ++k) {
+    invk2[k].x = (float)invk[k];
+    invk2[k].y = (float)(invk[k] - (double)invk2[k].x);
+  }
+  for (int k = 0; k < kEiTerms; ++k) {
+    invfact2[k].x = (float)invfact[k];
+    invfact2[k].y = (float)(invfact[k] - (double)invfact2[k].x);
+  }
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invk2, invk2, sizeof(invk2), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invfact2, invfact2, sizeof(invfact2), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // h is released on return
   if (e != cudaSuccess) { fprintf(stderr, "rlf: fit config: %s\n", cudaGetErrorString(e)); return (int)e; }
   return 0;
