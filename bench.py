@@ -271,10 +271,10 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
 
 # DRAM bytes of one k_extract_seq launch per row of the observation, from the ncu capture of
 # profiles/k_extract_seq_mid_128ant_16ch.md (dram__bytes_read.sum + dram__bytes_write.sum =
-# 2637.9 MB + 24.1 MB over 975,360 rows); a launch reads data, sky model, the row table, the
-# work-item list and the run descriptors once per row (the rows in uv order, so each visibility
-# read takes its own 32-byte sector), so the traffic of a launch grows with the rows
-EXTRACT_DRAM_BYTES_PER_ROW = (2637.867520e6 + 24.093184e6) / 975360
+# 335.9 MB + 7.7 MB over 975,360 rows); a launch reads data, sky model, the row table, the
+# work-item list and the run descriptors once per row, so the traffic of a launch grows with the
+# rows
+EXTRACT_DRAM_BYTES_PER_ROW = (335.856384e6 + 7.741184e6) / 975360
 
 
 def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak):

@@ -172,8 +172,10 @@ struct rlf_observation {
   rlf::DevBuf<double> partial;
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
   rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
-  rlf::DevBuf<int> order;           // rows in uv order (launch_row_order), built on first use
-  rlf::DevBuf<int> order_bins;      // its bin counts
+  // mixed-precision observations store their rows in uv order (launch_row_order), so that the
+  // batched extraction's consecutive work items are neighbours in uv and in memory: perm[p] is the
+  // caller's row at position p, inv its inverse; empty for FP64 observations (caller's order)
+  rlf::DevBuf<int> perm, inv;
   rlf::DevBuf<int> items;           // work items of the sequential batch extraction
   rlf::DevBuf<int> items2;          // its two-run work items
   rlf::DevBuf<int> item_count;      // [6] simple / general / two-run work items, then the extraction's work counters
@@ -236,10 +238,17 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
   return c;
 }
 
+// Gaussian noise keyed by the visibility's index in the caller's order (perm: the caller's row of
+// each stored row of a permuted observation, or nullptr)
 template <class C>
-__global__ void k_add_noise(long long n, C* vis, double sigma, uint64_t seed) {
+__global__ void k_add_noise(long long n, C* vis, double sigma, uint64_t seed, const int* perm, int n_rows) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const uint4 r = philox(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 0u, 0u),
+    long long key = i;
+    if (perm) {
+      const long long ch = i / n_rows;
+      key = ch * n_rows + perm[i - ch * n_rows];
+    }
+    const uint4 r = philox(make_uint4((uint32_t)key, (uint32_t)(key >> 32), 0u, 0u),
                            make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
     const double u1 = ((double)r.x + 1.0) * (1.0 / 4294967296.0);
     const double u2 = (double)r.y * (1.0 / 4294967296.0);
@@ -459,12 +468,6 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     RLF_OK(ob->rows.ensure(ob->n_rows));
     RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
   }
-  if (batched && !ob->order.p) {
-    RLF_OK(ob->order_bins.ensure((size_t)kOrderBins * kOrderBins));
-    RLF_OK(ob->order.ensure(ob->n_rows));
-    RLF_OK(launch_row_order(ob->n_rows, ob->uu.p, ob->vv.p, ob->wavenumbers[0] / (2 * kPi), ob->len, ob->order.p,
-                            ob->order_bins.p, st));
-  }
   PhaseTimer pt;
   RLF_OK(pt.mark(-1, st));
   for (size_t ui = 0; ui < units.size(); ++ui) {
@@ -529,7 +532,8 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       sb.n_simple = ob->item_count.p;
       sb.n_two = ob->item_count.p + 2;
       sb.queue = ob->item_count.p + 3;
-      RLF_OK(launch_classify_items(n_items, ob->n_rows, ob->order.p, sb, ob->items.p, ob->items2.p,
+      // the rows are stored in uv order: the items in storage order are already neighbours in uv
+      RLF_OK(launch_classify_items(n_items, ob->n_rows, nullptr, sb, ob->items.p, ob->items2.p,
                                    ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
@@ -713,6 +717,41 @@ static int process(rlf_observation* ob, int n_gal, const double* flux, const dou
   return 0;
 }
 
+// Rows of a new mixed-precision observation into uv order: perm, inv, and uvw, variances and flags
+// (in the caller's order on entry) gathered to their positions.
+static int obs_permute_rows(rlf_observation* ob, cudaStream_t st) {
+  const int n = ob->n_rows;
+  DevBuf<int> bins;
+  RLF_OK(bins.ensure((size_t)kOrderBins * kOrderBins));
+  RLF_OK(ob->perm.ensure(n));
+  RLF_OK(ob->inv.ensure(n));
+  RLF_OK(launch_row_order(n, ob->uu.p, ob->vv.p, ob->wavenumbers[0] / (2 * kPi), ob->len, ob->perm.p, bins.p, st));
+  RLF_OK(launch_invert_perm(n, ob->perm.p, ob->inv.p, st));
+  for (DevBuf<double>* a : {&ob->uu, &ob->vv, &ob->ww}) {
+    DevBuf<double> t;
+    RLF_OK(t.ensure(n));
+    RLF_OK(launch_gather_rows_f64(n, a->p, ob->perm.p, t.p, st));
+    std::swap(a->p, t.p);
+    std::swap(a->n, t.n);
+  }
+  {
+    DevBuf<float> t;
+    RLF_OK(t.ensure((size_t)ob->n_vis));
+    RLF_OK(launch_scatter_rows<float>(0, ob->n_vis, n, ob->sigma2.p, ob->inv.p, t.p, st));
+    std::swap(ob->sigma2.p, t.p);
+    std::swap(ob->sigma2.n, t.n);
+  }
+  if (ob->flag.p) {
+    DevBuf<uint8_t> t;
+    RLF_OK(t.ensure((size_t)ob->n_vis));
+    RLF_OK(launch_scatter_rows<uint8_t>(0, ob->n_vis, n, ob->flag.p, ob->inv.p, t.p, st));
+    std::swap(ob->flag.p, t.p);
+    std::swap(ob->flag.n, t.n);
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));  // the swapped-out buffers are freed on return
+  return 0;
+}
+
 static rlf_observation* obs_create(int n_rows, int n_ch, const double* uu, const double* vv, const double* ww,
                                    const double* wavenumbers, const double* spec, double len, const float* sigma2,
                                    const uint8_t* flag, int precision, cudaStream_t st) {
@@ -733,6 +772,7 @@ static rlf_observation* obs_create(int n_rows, int n_ch, const double* uu, const
   if (!r) r = ob->ww.upload(ww, n_rows, st);
   if (!r) r = ob->sigma2.upload(sigma2, (size_t)ob->n_vis, st);
   if (!r && flag) r = ob->flag.upload(flag, (size_t)ob->n_vis, st);
+  if (!r && precision != RLF_F64) r = obs_permute_rows(ob, st);
   if (!r && precision == RLF_F64) {
     r = ob->data64.ensure(ob->n_vis);
     if (!r) r = ob->sky64.ensure(ob->n_vis);
@@ -773,9 +813,10 @@ static int obs_put_c128(rlf_observation* ob, const double* h, bool sky, cudaStre
   }
   float2* d = sky ? ob->sky32.p : ob->data32.p;
   if (!h) { RLF_CUDA(cudaMemsetAsync(d, 0, n * sizeof(float2), st)); return 0; }
+  // the caller's order read in sequence, each row scattered to its position (inv)
   if (const void* hd = mapped_host(h)) {
     __atomic_add_fetch(&g_h2d_bytes, (unsigned long long)n * sizeof(double2), __ATOMIC_RELAXED);
-    RLF_OK(launch_convert_c64_to_f32(n, static_cast<const double2*>(hd), d, st));
+    RLF_OK(launch_c64_to_f32_scatter(0, n, ob->n_rows, static_cast<const double2*>(hd), ob->inv.p, d, st));
     RLF_CUDA(cudaStreamSynchronize(st));
     return 0;
   }
@@ -786,7 +827,7 @@ static int obs_put_c128(rlf_observation* ob, const double* h, bool sky, cudaStre
   for (long long i = 0; i < n; i += chunk) {
     const long long c = std::min(chunk, n - i);
     RLF_CUDA(copy_async(tmp.p, h + 2 * i, c * sizeof(double2), cudaMemcpyHostToDevice, st));
-    RLF_OK(launch_convert_c64_to_f32(c, tmp.p, d + i, st));
+    RLF_OK(launch_c64_to_f32_scatter(i, c, ob->n_rows, tmp.p, ob->inv.p, d, st));
   }
   RLF_CUDA(cudaStreamSynchronize(st));
   return 0;
@@ -801,9 +842,10 @@ static int obs_get_c128(rlf_observation* ob, double* h, bool sky, cudaStream_t s
     return 0;
   }
   const float2* d = sky ? ob->sky32.p : ob->data32.p;
+  // each row gathered from its position (inv), the caller's order written in sequence
   if (void* hd = mapped_host(h)) {
     __atomic_add_fetch(&g_d2h_bytes, (unsigned long long)n * sizeof(double2), __ATOMIC_RELAXED);
-    RLF_OK(launch_convert_f32_to_c64(n, d, static_cast<double2*>(hd), st));
+    RLF_OK(launch_f32_to_c64_gather(0, n, ob->n_rows, d, ob->inv.p, static_cast<double2*>(hd), st));
     RLF_CUDA(cudaStreamSynchronize(st));
     return 0;
   }
@@ -812,7 +854,7 @@ static int obs_get_c128(rlf_observation* ob, double* h, bool sky, cudaStream_t s
   RLF_OK(tmp.ensure((size_t)std::min(chunk, n)));
   for (long long i = 0; i < n; i += chunk) {
     const long long c = std::min(chunk, n - i);
-    RLF_OK(launch_convert_f32_to_c64(c, d + i, tmp.p, st));
+    RLF_OK(launch_f32_to_c64_gather(i, c, ob->n_rows, d, ob->inv.p, tmp.p, st));
     RLF_CUDA(copy_async(h + 2 * i, tmp.p, c * sizeof(double2), cudaMemcpyDeviceToHost, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   }
@@ -956,7 +998,15 @@ int rlf_obs_set_data_c64(rlf_observation* obs, const float* data_c64) {
     RLF_OK(launch_convert_f32_to_c64(n, tmp.p, obs->data64.p, st));
     RLF_CUDA(cudaStreamSynchronize(st));
   } else {
-    RLF_CUDA(copy_async(obs->data32.p, data_c64, n * sizeof(float2), cudaMemcpyHostToDevice, st));
+    // staged in chunks, each row scattered to its position
+    const long long chunk = 1LL << 24;
+    DevBuf<float2> tmp;
+    RLF_OK(tmp.ensure((size_t)std::min(chunk, n)));
+    for (long long i = 0; i < n; i += chunk) {
+      const long long c = std::min(chunk, n - i);
+      RLF_CUDA(copy_async(tmp.p, data_c64 + 2 * i, c * sizeof(float2), cudaMemcpyHostToDevice, st));
+      RLF_OK(launch_scatter_rows<float2>(i, c, obs->n_rows, tmp.p, obs->inv.p, obs->data32.p, st));
+    }
     RLF_CUDA(cudaStreamSynchronize(st));
   }
   return 0;
@@ -976,7 +1026,7 @@ int rlf_obs_set_data_ms(rlf_observation* obs, const float* data_block, unsigned 
     src = in.p;
   }
   if (obs->precision == RLF_F64) RLF_OK(launch_ms_vis_c128(src, obs->n_rows, obs->n_ch, (int)num_pols, obs->data64.p, st));
-  else RLF_OK(launch_ms_vis_f32(src, obs->n_rows, obs->n_ch, (int)num_pols, obs->data32.p, st));
+  else RLF_OK(launch_ms_vis_f32(src, obs->n_rows, obs->n_ch, (int)num_pols, obs->inv.p, obs->data32.p, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   return 0;
 }
@@ -1130,8 +1180,10 @@ int rlf_obs_simulate(rlf_observation* obs, int n_gal, const double* flux, const 
   RLF_OK(dg.upload(g.data(), g.size(), st));
   RLF_OK(add_models(obs, dg.p, n_gal, 1, gaussian, st));
   if (noise_sigma > 0) {
-    if (obs->precision == RLF_F64) k_add_noise<double2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data64.p, noise_sigma, seed);
-    else k_add_noise<float2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data32.p, noise_sigma, seed);
+    if (obs->precision == RLF_F64)
+      k_add_noise<double2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data64.p, noise_sigma, seed, nullptr, obs->n_rows);
+    else
+      k_add_noise<float2><<<4096, 256, 0, st>>>(obs->n_vis, obs->data32.p, noise_sigma, seed, obs->perm.p, obs->n_rows);
     RLF_CUDA(cudaGetLastError());
   }
   RLF_CUDA(cudaStreamSynchronize(st));

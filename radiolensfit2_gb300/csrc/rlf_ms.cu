@@ -46,9 +46,11 @@ __device__ __forceinline__ void put_vis(float2* out, size_t i, double2 v) {
   out[i] = make_float2((float)v.x, (float)v.y);
 }
 
-// DATA block [rows][nch][npol] complex64 -> out [nch][rows]; grid (row tiles, channel tiles)
+// DATA block [rows][nch][npol] complex64 -> out [nch][rows] (row r at position inv[r] when the
+// observation stores its rows permuted); grid (row tiles, channel tiles)
 template <class OUT>
-__global__ void k_ms_vis(const float2* __restrict__ in, long long rows, int nch, int npol, OUT* __restrict__ out) {
+__global__ void k_ms_vis(const float2* __restrict__ in, long long rows, int nch, int npol, const int* __restrict__ inv,
+                         OUT* __restrict__ out) {
   __shared__ double2 tile[kTile][kTile + 1];
   const long long r0 = (long long)blockIdx.x * kTile;
   const int c0 = blockIdx.y * kTile;
@@ -64,7 +66,7 @@ __global__ void k_ms_vis(const float2* __restrict__ in, long long rows, int nch,
   for (int k = ty; k < kTile; k += blockDim.y) {
     const int c = c0 + k;
     const long long r = r0 + tx;
-    if (r < rows && c < nch) put_vis(out, (size_t)c * rows + r, tile[tx][k]);
+    if (r < rows && c < nch) put_vis(out, (size_t)c * rows + (inv ? inv[r] : r), tile[tx][k]);
   }
 }
 
@@ -160,13 +162,14 @@ static dim3 tiles(long long rows, int nch) {
 int launch_ms_vis_c128(const float2* in, long long rows, int nch, int npol, double2* out, cudaStream_t st) {
   if (rows <= 0 || nch <= 0) return 0;
   if (npol != 1 && npol != 4) { fprintf(stderr, "rlf: %d correlations unsupported (1 or 4)\n", npol); return 1; }
-  k_ms_vis<double2><<<tiles(rows, nch), dim3(kTile, 8), 0, st>>>(in, rows, nch, npol, out);
+  k_ms_vis<double2><<<tiles(rows, nch), dim3(kTile, 8), 0, st>>>(in, rows, nch, npol, nullptr, out);
   return check("k_ms_vis<double2>");
 }
-int launch_ms_vis_f32(const float2* in, long long rows, int nch, int npol, float2* out, cudaStream_t st) {
+int launch_ms_vis_f32(const float2* in, long long rows, int nch, int npol, const int* inv, float2* out,
+                      cudaStream_t st) {
   if (rows <= 0 || nch <= 0) return 0;
   if (npol != 1 && npol != 4) { fprintf(stderr, "rlf: %d correlations unsupported (1 or 4)\n", npol); return 1; }
-  k_ms_vis<float2><<<tiles(rows, nch), dim3(kTile, 8), 0, st>>>(in, rows, nch, npol, out);
+  k_ms_vis<float2><<<tiles(rows, nch), dim3(kTile, 8), 0, st>>>(in, rows, nch, npol, inv, out);
   return check("k_ms_vis<float2>");
 }
 int launch_ms_flags(const uint8_t* in, long long rows, int nch, int npol, uint8_t* out, unsigned long long* count,

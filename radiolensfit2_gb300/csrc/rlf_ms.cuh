@@ -8,7 +8,9 @@ namespace rlf {
 
 // DATA block [rows][nch][npol] complex64 (Jy) -> [nch][rows] Stokes I in uJy, complex128 / complex64
 int launch_ms_vis_c128(const float2* in, long long rows, int nch, int npol, double2* out, cudaStream_t st);
-int launch_ms_vis_f32(const float2* in, long long rows, int nch, int npol, float2* out, cudaStream_t st);
+// inv: position of each row in an observation stored with permuted rows, or nullptr
+int launch_ms_vis_f32(const float2* in, long long rows, int nch, int npol, const int* inv, float2* out,
+                      cudaStream_t st);
 // FLAG block [rows][nch][npol] -> [nch][rows]; *count (zeroed by the caller) += flagged
 int launch_ms_flags(const uint8_t* in, long long rows, int nch, int npol, uint8_t* out, unsigned long long* count,
                     cudaStream_t st);

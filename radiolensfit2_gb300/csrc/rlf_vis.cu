@@ -11,6 +11,7 @@
 // a double-float product per channel, range-reduced to [-1/2, 1/2] turn before the FP32 sincos.
 #include "rlf_vis.cuh"
 #include <stdio.h>
+#include <algorithm>
 
 namespace rlf {
 
@@ -831,6 +832,72 @@ __global__ void k_f32_to_c64(long long n, const float2* in, double2* out) {
     out[i] = make_double2((double)x.x, (double)x.y);
   }
 }
+// caller index -> position in a row-permuted observation
+__device__ __forceinline__ long long permuted(long long idx, int n_rows, const int* __restrict__ inv) {
+  const long long ch = idx / n_rows;
+  return ch * n_rows + inv[idx - ch * n_rows];
+}
+__global__ void k_c64_to_f32_scatter(long long i0, long long count, int n_rows, const double2* __restrict__ in,
+                                     const int* __restrict__ inv, float2* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    const double2 x = in[i];
+    out[permuted(i0 + i, n_rows, inv)] = make_float2((float)x.x, (float)x.y);
+  }
+}
+__global__ void k_f32_to_c64_gather(long long i0, long long count, int n_rows, const float2* __restrict__ in,
+                                    const int* __restrict__ inv, double2* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    const float2 x = in[permuted(i0 + i, n_rows, inv)];
+    out[i] = make_double2((double)x.x, (double)x.y);
+  }
+}
+template <class T>
+__global__ void k_scatter_rows(long long i0, long long count, int n_rows, const T* __restrict__ in,
+                               const int* __restrict__ inv, T* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    out[permuted(i0 + i, n_rows, inv)] = in[i];
+}
+__global__ void k_gather_rows_f64(int n, const double* __restrict__ in, const int* __restrict__ perm,
+                                  double* __restrict__ out) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) out[p] = in[perm[p]];
+}
+__global__ void k_invert_perm(int n, const int* __restrict__ perm, int* __restrict__ inv) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) inv[perm[p]] = p;
+}
+static int grid_of(long long n) { return (int)std::min<long long>((n + 255) / 256, 8192); }
+int launch_c64_to_f32_scatter(long long i0, long long count, int n_rows, const double2* in, const int* inv,
+                              float2* out, cudaStream_t st) {
+  if (count <= 0) return 0;
+  k_c64_to_f32_scatter<<<grid_of(count), 256, 0, st>>>(i0, count, n_rows, in, inv, out);
+  return check("k_c64_to_f32_scatter");
+}
+int launch_f32_to_c64_gather(long long i0, long long count, int n_rows, const float2* in, const int* inv,
+                             double2* out, cudaStream_t st) {
+  if (count <= 0) return 0;
+  k_f32_to_c64_gather<<<grid_of(count), 256, 0, st>>>(i0, count, n_rows, in, inv, out);
+  return check("k_f32_to_c64_gather");
+}
+template <class T>
+int launch_scatter_rows(long long i0, long long count, int n_rows, const T* in, const int* inv, T* out,
+                        cudaStream_t st) {
+  if (count <= 0) return 0;
+  k_scatter_rows<T><<<grid_of(count), 256, 0, st>>>(i0, count, n_rows, in, inv, out);
+  return check("k_scatter_rows");
+}
+template int launch_scatter_rows<float>(long long, long long, int, const float*, const int*, float*, cudaStream_t);
+template int launch_scatter_rows<uint8_t>(long long, long long, int, const uint8_t*, const int*, uint8_t*, cudaStream_t);
+template int launch_scatter_rows<float2>(long long, long long, int, const float2*, const int*, float2*, cudaStream_t);
+int launch_gather_rows_f64(int n, const double* in, const int* perm, double* out, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_gather_rows_f64<<<grid_of(n), 256, 0, st>>>(n, in, perm, out);
+  return check("k_gather_rows_f64");
+}
+int launch_invert_perm(int n, const int* perm, int* inv, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_invert_perm<<<grid_of(n), 256, 0, st>>>(n, perm, inv);
+  return check("k_invert_perm");
+}
+
 int launch_convert_c64_to_f32(long long n, const double2* in, float2* out, cudaStream_t st) {
   if (n <= 0) return 0;
   k_c64_to_f32<<<4096, 256, 0, st>>>(n, in, out);

@@ -118,5 +118,20 @@ int launch_average_facets(long long size, double2* vis, double* sigma2, const do
 // visibility layout conversion: complexd [ch][row] <-> float2 [ch][row] / double2
 int launch_convert_c64_to_f32(long long n, const double2* in, float2* out, cudaStream_t st);
 int launch_convert_f32_to_c64(long long n, const float2* in, double2* out, cudaStream_t st);
+// The same between the caller's visibility order ([ch][row], index ch * n_rows + row) and an
+// observation stored with its rows permuted (position inv[row]; launch_row_order): the caller's
+// elements [i0, i0 + count) from / to a buffer holding just those elements, so that the host side
+// is read or written in order and the device side is scattered or gathered.
+int launch_c64_to_f32_scatter(long long i0, long long count, int n_rows, const double2* in, const int* inv,
+                              float2* out, cudaStream_t st);
+int launch_f32_to_c64_gather(long long i0, long long count, int n_rows, const float2* in, const int* inv,
+                             double2* out, cudaStream_t st);
+template <class T>
+int launch_scatter_rows(long long i0, long long count, int n_rows, const T* in, const int* inv, T* out,
+                        cudaStream_t st);
+// out[p] = in[perm[p]] for p < n (the per-row arrays of a permuted observation)
+int launch_gather_rows_f64(int n, const double* in, const int* perm, double* out, cudaStream_t st);
+// inv[perm[p]] = p
+int launch_invert_perm(int n, const int* perm, int* inv, cudaStream_t st);
 
 }  // namespace rlf
