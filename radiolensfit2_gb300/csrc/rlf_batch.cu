@@ -365,11 +365,11 @@ int launch_row_order(int n_rows, const double* uu, const double* vv, double inv_
 // every facet size of the batch (front of items, count in counters[0]), "two-run" ones, at most
 // two runs for every facet size (items2, counters[2]; only when two_run), and the general others
 // (back of items, counters[1]), so that the extraction runs each kind without divergence between
-// the lanes of a warp.  A block takes 256 consecutive positions of the row order and places each
-// class's items contiguously, in that order, with one counter update per class.
+// the lanes of a warp.  A block takes 256 consecutive items and places each class's items
+// contiguously, in that order, with one counter update per class (the rows are stored in uv
+// order, so neighbouring items stay neighbours in uv).
 constexpr int kClassifyThreads = 256;
-__global__ void __launch_bounds__(kClassifyThreads) k_classify_items(long long total, int n_rows,
-                                                                     const int* __restrict__ order, SeqBatch b,
+__global__ void __launch_bounds__(kClassifyThreads) k_classify_items(long long total, SeqBatch b,
                                                                      int two_run, int* __restrict__ items,
                                                                      int* __restrict__ items2,
                                                                      int* __restrict__ counters) {
@@ -378,13 +378,8 @@ __global__ void __launch_bounds__(kClassifyThreads) k_classify_items(long long t
   __shared__ int bbase[3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (long long p0 = (long long)blockIdx.x * kClassifyThreads; p0 < total; p0 += (long long)gridDim.x * kClassifyThreads) {
-    const long long tp = p0 + threadIdx.x;
-    const bool live = tp < total;
-    long long t = 0;
-    if (live) {
-      const long long ch = tp / n_rows, i = tp - ch * n_rows;
-      t = ch * n_rows + (order ? order[i] : i);
-    }
+    const long long t = p0 + threadIdx.x;
+    const bool live = t < total;
     bool simple = live, two = live && two_run;
     if (live)
       for (int f = 0; f < b.n_sizes; ++f) {
@@ -417,15 +412,15 @@ __global__ void __launch_bounds__(kClassifyThreads) k_classify_items(long long t
   }
 }
 
-int launch_classify_items(long long total, int n_rows, const int* order, const SeqBatch& b, int* items,
-                          int* items2, int* counters, cudaStream_t st) {
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
+                          cudaStream_t st) {
   const cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(int), st);
   if (e != cudaSuccess) { fprintf(stderr, "rlf: classify: %s\n", cudaGetErrorString(e)); return (int)e; }
   int dev = 0;
   cudaGetDevice(&dev);
   const int two_run = (dev >= 0 && dev < 64) ? g_chunk_poly[dev] : 0;
   const int blocks = (int)std::min<long long>((total + kClassifyThreads - 1) / kClassifyThreads, 4096);
-  k_classify_items<<<blocks, kClassifyThreads, 0, st>>>(total, n_rows, order, b, two_run, items, items2, counters);
+  k_classify_items<<<blocks, kClassifyThreads, 0, st>>>(total, b, two_run, items, items2, counters);
   return check("k_classify_items");
 }
 

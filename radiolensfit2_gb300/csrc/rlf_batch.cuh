@@ -47,9 +47,10 @@ constexpr uint16_t kNotTwoRun = 0xFFFE;
 int launch_cell_desc(int n_rows, int n_ch, const uint16_t* cell, uint32_t* desc, uint16_t* desc1, cudaStream_t st);
 
 // Rows in the order of their uv points on a kOrderBins x kOrderBins grid over the facets' extent
-// (v bin major, u bin minor; rows of one bin in any order), so that consecutive work items of the
-// sequential extraction fall in the same facet cell for every facet size: a thin strip of constant
-// v bin crosses a facet row's cells in increasing u.  bins: [kOrderBins^2] scratch.
+// (v bin major, u bin minor; rows of one bin in any order): order[p] = the row at position p.
+// Mixed-precision observations store their rows in this order, so that consecutive work items of
+// the sequential extraction fall in the same facet cell for every facet size (a thin strip of
+// constant v bin crosses a facet row's cells in increasing u).  bins: [kOrderBins^2] scratch.
 constexpr int kOrderBins = 1024;
 int launch_row_order(int n_rows, const double* uu, const double* vv, double inv_lambda0, double len, int* order,
                      int* bins, cudaStream_t st);
@@ -79,10 +80,9 @@ size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes);
 // split the batch's work items into single-run ones (front of items), general ones (back of items)
 // and ones of at most two runs for every facet size (items2; only with chunk polynomials), for
 // launch_extract_seq; items, items2: [n_rows * chunks], counters: [3] (simple, general, two-run).
-// The items of every chunk are taken in the row order `order` (launch_row_order; nullptr: row
-// index order) and each class keeps that order within a block of 256 items.
-int launch_classify_items(long long total, int n_rows, const int* order, const SeqBatch& b, int* items,
-                          int* items2, int* counters, cudaStream_t st);
+// Each class keeps the items' order within a block of 256 items.
+int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
+                          cudaStream_t st);
 // partial: [ctas][total_cells] float2
 int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
                        int gaussian, int ctas, float2* partial, cudaStream_t st);

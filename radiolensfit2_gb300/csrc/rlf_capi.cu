@@ -532,9 +532,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       sb.n_simple = ob->item_count.p;
       sb.n_two = ob->item_count.p + 2;
       sb.queue = ob->item_count.p + 3;
-      // the rows are stored in uv order: the items in storage order are already neighbours in uv
-      RLF_OK(launch_classify_items(n_items, ob->n_rows, nullptr, sb, ob->items.p, ob->items2.p,
-                                   ob->item_count.p, st));
+      RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->items2.p, ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
     // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the

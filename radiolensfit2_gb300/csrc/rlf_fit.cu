@@ -46,8 +46,6 @@ constexpr int kEiTab = 101;        // Ei(k) and e^k for k = 0..100 (the position
 constexpr int kEiTerms = 48;       // terms of the per-lane Ei expansions (at most ~26 are used)
 constexpr int kInvTab = 128;       // 1/k for k < kInvTab
 
-__constant__ double c_invk[kInvTab];       // 1 / k
-__constant__ double c_invfact[kEiTerms];   // 1 / k!
 __constant__ double c_ei_tab[kEiTab];      // Ei(k), computed on the host in extended precision
 __constant__ double c_exp_tab[kEiTab];     // e^k
 __constant__ float2 c_invk2[kInvTab];       // 1 / k as a float pair (hi, lo)
@@ -731,49 +729,6 @@ __device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
 }
 
 // ------------------------------------------------------------ phased nodes
-// Ei(x1) and Ei(x2), 0 < x <= 100, evaluated by one lane (each lane its own x).
-//   x <= 2.5: the power series  gamma + ln x + sum_k x^k / (k k!)  (at most 26 terms);
-//   x > 2.5: the Taylor expansion about the nearest integer x0 of
-//       Ei(x) = Ei(x0) + e^x0 int_0^s e^t / (x0 + t) dt,   s = x - x0,  |s| <= 1/2,
-//     with e^t / (x0 + t) = sum_n c_n t^n,  c_0 = 1/x0,  c_n = (1/n! - c_(n-1)) / x0  (from
-//     (x0 + t) sum c_n t^n = e^t), so  Ei(x) = Ei(x0) + e^x0 sum_n c_n s^(n+1) / (n+1);  the terms
-//     shrink at least as (1/6)^n.  Ei(x0) and e^x0 come from a table made on the host in extended
-//     precision.
-// Each expansion stops at its first term below 1e-18 of its sum; relative error ~1e-15 against an
-// arbitrary-precision Ei over (0, 100], where the series alone needs up to ~100 terms.  The two
-// recurrences run in one loop (independent chains, so their latencies overlap).
-__device__ __forceinline__ void ei_pair_lane(double x1, double x2, double* e1, double* e2) {
-  const bool ser1 = x1 <= 2.5, ser2 = x2 <= 2.5;
-  const int k1 = ser1 ? 0 : (int)(x1 + 0.5), k2 = ser2 ? 0 : (int)(x2 + 0.5);
-  const double s1 = ser1 ? x1 : x1 - k1, s2 = ser2 ? x2 : x2 - k2;
-  const double i1 = c_invk[k1], i2 = c_invk[k2];
-  // series: c = s^k / k!, term c / k;  Taylor: c = c_k, p = s^(k+1), term c p / (k+1)
-  double c1 = ser1 ? 1.0 : i1, c2 = ser2 ? 1.0 : i2;
-  double p1 = s1, p2 = s2;
-  double a1 = ser1 ? 0.0 : i1 * s1, a2 = ser2 ? 0.0 : i2 * s2;
-  bool run1 = true, run2 = true;
-  for (int k = 1; k < kEiTerms - 1 && (run1 || run2); ++k) {
-    const double ik = c_invk[k], ik1 = c_invk[k + 1], ifk = c_invfact[k];
-    if (run1) {
-      double t;
-      if (ser1) { c1 = c1 * s1 * ik; t = c1 * ik; }
-      else { c1 = (ifk - c1) * i1; p1 = p1 * s1; t = c1 * p1 * ik1; }
-      a1 += t;
-      if (fabs(t) < 1e-18 * fabs(a1)) run1 = false;
-    }
-    if (run2) {
-      double t;
-      if (ser2) { c2 = c2 * s2 * ik; t = c2 * ik; }
-      else { c2 = (ifk - c2) * i2; p2 = p2 * s2; t = c2 * p2 * ik1; }
-      a2 += t;
-      if (fabs(t) < 1e-18 * fabs(a2)) run2 = false;
-    }
-  }
-  *e1 = ser1 ? kEulerGamma + log(x1) + a1 : c_ei_tab[k1] + c_exp_tab[k1] * a1;
-  *e2 = ser2 ? kEulerGamma + log(x2) + a2 : c_ei_tab[k2] + c_exp_tab[k2] * a2;
-}
-
-
 // ---- double-float (unevaluated sum of two floats) arithmetic for sin/cos on the FP32 pipes
 __device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
   f2 p = two_prod(a.hi, b.hi);
@@ -872,10 +827,18 @@ __device__ __forceinline__ f2 df_log_double(double x) {
   return df_add(df_log(quick_two_sum(hi, lo)), df_ln2_times((float)e));
 }
 
-// Ei(x1) and Ei(x2) as ei_pair_lane, the expansions' recurrences in double-float on the FP32 pipes
-// (this GPU's FP64 pipe is 1/64 of FP32 and shared by the SM's CTAs; the lane chains were bound
-// by its latency); each expansion stops at its first term below 2^-53 of its sum, under the
-// pair's ~2^-48 precision.  The closing sums and the tables stay in double.
+// Ei(x1) and Ei(x2), 0 < x <= 100, evaluated by one lane (each lane its own x).
+//   x <= 2.5: the power series  gamma + ln x + sum_k x^k / (k k!)  (at most 26 terms);
+//   x > 2.5: the Taylor expansion about the nearest integer x0 of
+//       Ei(x) = Ei(x0) + e^x0 int_0^s e^t / (x0 + t) dt,   s = x - x0,  |s| <= 1/2,
+//     with e^t / (x0 + t) = sum_n c_n t^n,  c_0 = 1/x0,  c_n = (1/n! - c_(n-1)) / x0  (from
+//     (x0 + t) sum c_n t^n = e^t), so  Ei(x) = Ei(x0) + e^x0 sum_n c_n s^(n+1) / (n+1);  the terms
+//     shrink at least as (1/6)^n.  Ei(x0) and e^x0 come from a table made on the host in extended
+//     precision.
+// The recurrences run in double-float on the FP32 pipes (dependent FP64 operations take 64 cycles
+// and more here), the two in one loop so that their latencies overlap; each expansion stops at its
+// first term below 2^-53 of its sum, under the pair's ~2^-47 precision (the series alone would
+// need up to ~100 terms over (0, 100]).  The closing sums and the tables stay in double.
 __device__ __forceinline__ f2 df_c(float2 v) { return f2{v.x, v.y}; }
 __device__ __forceinline__ void ei_pair_df(double x1, double x2, double* e1, double* e2) {
   const bool ser1 = x1 <= 2.5, ser2 = x2 <= 2.5;
@@ -1996,8 +1959,6 @@ int fit_set_config(const FitConfigHost& cfg, cudaStream_t st) {
     exptab[k] = (double)expl(x);
   }
   cudaError_t e = cudaMemcpyToSymbolAsync(c_fit, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invk, invk, sizeof(invk), 0, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_invfact, invfact, sizeof(invfact), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_ei_tab, eitab, sizeof(eitab), 0, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_exp_tab, exptab, sizeof(exptab), 0, cudaMemcpyHostToDevice, st);
   static float2 invk2[kInvTab], invfact2[kEiTerms];
