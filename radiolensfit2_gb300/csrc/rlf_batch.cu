@@ -984,7 +984,8 @@ int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, cons
 
 // ---------------------------------------------------------------- removal
 // grid-stride over (row, chunk of kRemCh channels); galaxies staged through shared memory in
-// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  MODE as k_extract_seq: 0 exact
+// tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  The channel's spectral factor
+// multiplies the sums over galaxies once, after the galaxy loop.  MODE as k_extract_seq: 0 exact
 // per-channel profiles; 1 the profiles of a chunk from its cubic in dl (profile_poly), one profile
 // evaluation per model, galaxy and chunk; 2 as 1 with exactly one 16-channel chunk (compile-time
 // channel constants).
@@ -1044,13 +1045,13 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
             const BatchChan bc = c_bch[ch];
             float a0, a1;
             if (POLY) {
-              a0 = bc.spec * poly3(c0p, bc.dl);
-              a1 = bc.spec * poly3(c1p, bc.dl);
+              a0 = poly3(c0p, bc.dl);
+              a1 = poly3(c1p, bc.dl);
             } else {
               const float x0 = g.sf0 * bc.wn2 * rw.q;
               const float x1 = g.sf1 * bc.wn2 * k1q;
-              a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * bc.spec * g.flux;
-              a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * bc.spec * g.flux;
+              a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * g.flux;
+              a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * g.flux;
             }
             ar[k] = fmaf(a0, zr, ar[k]);
             ai[k] = fmaf(a0, zi, ai[k]);
@@ -1070,13 +1071,14 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
       const int ch = ch0 + k;
       if (ch < nch) {
         const size_t idx = (size_t)ch * n_rows + r;
+        const float spec = c_bch[ch].spec;
         float2 s = sky[idx];
-        s.x -= ar[k];
-        s.y -= ai[k];
+        s.x = fmaf(-spec, ar[k], s.x);
+        s.y = fmaf(-spec, ai[k], s.y);
         sky[idx] = s;
         float2 d = data[idx];
-        d.x -= br[k];
-        d.y -= bi[k];
+        d.x = fmaf(-spec, br[k], d.x);
+        d.y = fmaf(-spec, bi[k], d.y);
         data[idx] = d;
       }
     }
