@@ -452,283 +452,6 @@ __device__ __forceinline__ NodeCache node_cache_view(unsigned char* base, int nr
   return c;
 }
 
-template <class S>
-struct FitShared {
-  // phased node evaluation (eval_nodes): per-node state
-  double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
-  double nnorm[kMaxNodes];                // 1 / the node's model normalisation
-  int alist[kMaxNodes];                   // nodes with a Newton pass pending
-  int nact;
-  // natural spline rows and the factorisation of its matrix for the abscissae fac_x[0..fac_n)
-  S soff[kMaxNodes], sdiag[kMaxNodes], sg[kMaxNodes], sz[kMaxNodes], salpha[kMaxNodes], sgamma[kMaxNodes];
-  S fac_x[kMaxNodes];
-  int fac_n;
-  S Lr[kMaxNodes];
-  S rprior[kMaxNodes];
-  S xs[kMaxNodes], ys[kMaxNodes], cs[kMaxNodes];
-  S sb[kMaxNodes], sd[kMaxNodes];         // linear and cubic spline coefficients of each interval
-  S qa[kQagCap], qb[kQagCap], qr[kQagCap], qe[kQagCap];
-  S bcast_L;
-  int bcast_err;
-  int g;
-  int newton;
-  // sampling board: a claimed grid point and its chunk (owner and helper CTAs)
-  SampleSlot claim_prm;
-  int claim_g, claim_seq, claim_idx, claim_state;
-  int bcast_np;
-  int status;
-};
-
-// ------------------------------------------------- scalelength marginalisation
-template <class S>
-__device__ __forceinline__ S spline_eval(const FitShared<S>& sh, int n, bool cubic, S x, bool* ok) {
-  if (x < sh.xs[0] || x > sh.xs[n - 1]) { *ok = false; return S(0); }
-  int lo = 0, hi = n - 1;
-  while (hi > lo + 1) {
-    int mid = (lo + hi) >> 1;
-    if (sh.xs[mid] > x) hi = mid; else lo = mid;
-  }
-  const S x_lo = sh.xs[lo], x_hi = sh.xs[lo + 1];
-  const S y_lo = sh.ys[lo], y_hi = sh.ys[lo + 1];
-  const S dx = x_hi - x_lo, dy = y_hi - y_lo, delx = x - x_lo;
-  *ok = true;
-  // cubic: the coefficients of gsl_interp_cspline's evaluation, made once per spline (spline_coeffs)
-  if (cubic) return y_lo + delx * (sh.sb[lo] + delx * (sh.cs[lo] + delx * sh.sd[lo]));
-  return y_lo + delx / dx * dy;
-}
-
-// b_i and d_i of every interval of the natural cubic spline (xs, ys, cs), lane i: as the
-// reference's interpolation evaluates them per point (gsl_interp_cspline), once per spline
-template <class S>
-__device__ __forceinline__ void spline_coeffs(FitShared<S>& sh, int n) {
-  const int i = threadIdx.x & 31;
-  if (i < n - 1) {
-    const S dx = sh.xs[i + 1] - sh.xs[i], dy = sh.ys[i + 1] - sh.ys[i];
-    const S c_i = sh.cs[i], c_ip1 = sh.cs[i + 1];
-    sh.sb[i] = (dy / dx) - dx * (c_ip1 + S(2) * c_i) / S(3);
-    sh.sd[i] = (c_ip1 - c_i) / (S(3) * dx);
-  }
-  __syncwarp();
-}
-
-// integrand of marginalise_r.c:231-238: exp(spline(x)), 0 outside the nodes
-template <class S>
-__device__ __forceinline__ S marf(const FitShared<S>& sh, int n, bool cubic, S x) {
-  bool ok;
-  S y = spline_eval(sh, n, cubic, x, &ok);
-  return ok ? s_exp(y) : S(0);
-}
-
-template <class S>
-__device__ __forceinline__ S rescale_error(S err, S result_abs, S result_asc) {
-  err = s_abs(err);
-  if (result_asc != S(0) && err != S(0)) {
-    S scale = s_pow15(S(200) * err / result_asc);
-    err = (scale < S(1)) ? result_asc * scale : result_asc;
-  }
-  if (result_abs > Consts<S>::dbl_min() / (S(50) * Consts<S>::dbl_eps())) {
-    S min_err = S(50) * Consts<S>::dbl_eps() * result_abs;
-    if (min_err > err) err = min_err;
-  }
-  return err;
-}
-
-// QUADPACK qk41 on one warp: lane j < 21 evaluates the integrand at centre -+ half*xgk[j].
-template <class S>
-__device__ __noinline__ void qk41_warp(const FitShared<S>& sh, int n, bool cubic, S a, S b, S* result, S* abserr,
-                          S* resabs, S* resasc) {
-  const int j = threadIdx.x & 31;
-  const S center = S(0.5) * (a + b);
-  const S half = S(0.5) * (b - a);
-  const S abs_half = s_abs(half);
-  S f1 = S(0), f2 = S(0);
-  if (j < 21) {
-    const S absc = half * S(c_xgk[j]);
-    f1 = marf(sh, n, cubic, center - absc);
-    f2 = (j == 20) ? f1 : marf(sh, n, cubic, center + absc);
-  }
-  const S fc = __shfl_sync(0xffffffffu, f1, 20);
-  const S wk = (j < 20) ? S(c_wgk[j]) : S(0);
-  const S wg = (j < 20 && (j & 1)) ? S(c_wg[j >> 1]) : S(0);
-  const S fsum = f1 + f2;
-  S rk = wsum<S>(wk * fsum) + fc * S(c_wgk[20]);
-  S rg = wsum<S>(wg * fsum);
-  S ra = wsum<S>(wk * (s_abs(f1) + s_abs(f2))) + s_abs(fc * S(c_wgk[20]));
-  const S mean = rk * S(0.5);
-  S rasc = wsum<S>(wk * (s_abs(f1 - mean) + s_abs(f2 - mean))) + S(c_wgk[20]) * s_abs(fc - mean);
-  const S err = (rk - rg) * half;
-  rk *= half;
-  ra *= abs_half;
-  rasc *= abs_half;
-  *result = rk;
-  *resabs = ra;
-  *resasc = rasc;
-  *abserr = rescale_error<S>(err, ra, rasc);
-}
-
-// QUADPACK qag (GSL gsl_integration_qag, key GSL_INTEG_GAUSS41, epsabs 0, epsrel 1e-3):
-// global adaptive bisection of the interval with the largest error.  Control is replicated in
-// the lanes of warp 0; interval lists live in shared memory (kQagCap entries).
-// Returns 0 on success, nonzero as GSL's status would be.
-template <class S>
-__device__ __noinline__ int qag_warp(FitShared<S>& sh, int n, bool cubic, S a, S b, S* out) {
-  const int lane = threadIdx.x & 31;
-  const S epsabs = S(0), epsrel = S(1.e-3);
-  S result0, abserr0, resabs0, resasc0;
-  qk41_warp<S>(sh, n, cubic, a, b, &result0, &abserr0, &resabs0, &resasc0);
-  S tolerance = fmax(epsabs, epsrel * s_abs(result0));
-  const S round_off = S(50) * Consts<S>::dbl_eps() * resabs0;
-  *out = result0;
-  if (abserr0 <= round_off && abserr0 > tolerance) return 18;        // GSL_EROUND
-  if ((abserr0 <= tolerance && abserr0 != resasc0) || abserr0 == S(0)) return 0;
-  if (lane == 0) { sh.qa[0] = a; sh.qb[0] = b; sh.qr[0] = result0; sh.qe[0] = abserr0; }
-  __syncwarp();
-  S area = result0, errsum = abserr0;
-  int nint = 1, iteration = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
-  const int limit = 1000;
-  do {
-    // interval with the largest error (lowest index on ties)
-    S best = S(-1);
-    int bi = 0x7fffffff;
-    for (int k = lane; k < nint; k += 32) {
-      S e = sh.qe[k];
-      if (e > best) { best = e; bi = k; }
-    }
-#pragma unroll
-    for (int m = 16; m > 0; m >>= 1) {
-      S ob = __shfl_xor_sync(0xffffffffu, best, m);
-      int oi = __shfl_xor_sync(0xffffffffu, bi, m);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    const int imax = bi;
-    const S a_i = sh.qa[imax], b_i = sh.qb[imax], r_i = sh.qr[imax], e_i = sh.qe[imax];
-    const S a1 = a_i, b1 = S(0.5) * (a_i + b_i), a2 = b1, b2 = b_i;
-    S area1, area2, error1, error2, resabs1, resabs2, resasc1, resasc2;
-    qk41_warp<S>(sh, n, cubic, a1, b1, &area1, &error1, &resabs1, &resasc1);
-    qk41_warp<S>(sh, n, cubic, a2, b2, &area2, &error2, &resabs2, &resasc2);
-    const S area12 = area1 + area2, error12 = error1 + error2;
-    errsum += (error12 - e_i);
-    area += area12 - r_i;
-    if (resasc1 != error1 && resasc2 != error2) {
-      const S delta = r_i - area12;
-      if (s_abs(delta) <= S(1.0e-5) * s_abs(area12) && error12 >= S(0.99) * e_i) roundoff1++;
-      if (iteration >= 10 && error12 > e_i) roundoff2++;
-    }
-    tolerance = fmax(epsabs, epsrel * s_abs(area));
-    if (errsum > tolerance) {
-      if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
-      const S tmp = (S(1) + S(100) * Consts<S>::dbl_eps()) * (s_abs(a2) + S(1000) * Consts<S>::dbl_min());
-      if (s_abs(a1) <= tmp && s_abs(b2) <= tmp) error_type = 3;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      sh.qa[imax] = a1; sh.qb[imax] = b1; sh.qr[imax] = area1; sh.qe[imax] = error1;
-      sh.qa[nint] = a2; sh.qb[nint] = b2; sh.qr[nint] = area2; sh.qe[nint] = error2;
-    }
-    __syncwarp();
-    nint++;
-    iteration++;
-    if (nint >= kQagCap && errsum > tolerance && !error_type) {
-      if (lane == 0) sh.status |= 2;
-      error_type = 4;  // device interval capacity: reported like GSL_EMAXITER
-    }
-  } while (iteration < limit && !error_type && errsum > tolerance);
-  S sum = S(0);
-  for (int k = lane; k < nint; k += 32) sum += sh.qr[k];
-  sum = wsum<S>(sum);
-  *out = sum;
-  if (errsum <= tolerance) return 0;
-  if (error_type == 2) return 18;
-  if (error_type == 3) return 21;
-  return 11;
-}
-
-// marginalise_r.c:81-223 on warp 0; (xs, ys, numvals) already in shared memory.
-template <class S>
-__device__ __noinline__ S marginalise_posterior_warp(FitShared<S>& sh, int n) {
-  const int lane = threadIdx.x & 31;
-  const bool in = lane < n;
-  const S y_l = in ? sh.ys[lane] : S(0);
-  const S x_l = in ? sh.xs[lane] : S(0);
-  // ymax: the first maximum above -10 (strict comparison from ymax = -10, marginalise_r.c:90-96)
-  S ymax = (in && y_l > S(-10.0)) ? y_l : S(-10.0);
-  int ypos = (in && y_l > S(-10.0)) ? lane : 0x7fffffff;
-  // xmin, xmax: the node range (it contains the maximum's neighbours, marginalise_r.c:97-106)
-  S xmin = in ? x_l : S(1e300), xmax = in ? x_l : S(-1e300);
-#pragma unroll
-  for (int m = 16; m > 0; m >>= 1) {
-    const S oy = __shfl_xor_sync(0xffffffffu, ymax, m);
-    const int op = __shfl_xor_sync(0xffffffffu, ypos, m);
-    if (oy > ymax || (oy == ymax && op < ypos)) { ymax = oy; ypos = op; }
-    xmin = fmin(xmin, __shfl_xor_sync(0xffffffffu, xmin, m));
-    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, m));
-  }
-  if (in) { sh.ys[lane] = y_l - ymax; sh.cs[lane] = S(0); }
-  // natural cubic spline: c_0 = c_{n-1} = 0, interior from the symmetric tridiagonal system
-  // solved by LDL^T (as gsl_interp_cspline).  The lanes form the rows; the factorisation
-  // (alpha, gamma) depends only on the abscissae and is kept while they do not change.
-  const int m = n - 2;
-  __syncwarp();
-  if (lane < m) {
-    const int i = lane;
-    const S h_i = sh.xs[i + 1] - sh.xs[i], h_ip1 = sh.xs[i + 2] - sh.xs[i + 1];
-    const S dy_i = sh.ys[i + 1] - sh.ys[i], dy_ip1 = sh.ys[i + 2] - sh.ys[i + 1];
-    const S g_i = (h_i != S(0)) ? S(1) / h_i : S(0);
-    const S g_ip1 = (h_ip1 != S(0)) ? S(1) / h_ip1 : S(0);
-    sh.soff[i] = h_ip1;
-    sh.sdiag[i] = S(2) * (h_ip1 + h_i);
-    sh.sg[i] = S(3) * (dy_ip1 * g_ip1 - dy_i * g_i);
-  }
-  const bool same = __all_sync(0xffffffffu, !in || sh.fac_x[lane] == x_l) && sh.fac_n == n;
-  __syncwarp();
-  if (m == 1) {
-    if (lane == 0) sh.cs[1] = sh.sg[0] / sh.sdiag[0];
-  } else if (m > 1) {
-    if (!same) {
-      if (lane == 0) {
-        sh.salpha[0] = sh.sdiag[0];
-        sh.sgamma[0] = sh.soff[0] / sh.salpha[0];
-        for (int i = 1; i < m - 1; i++) {
-          sh.salpha[i] = sh.sdiag[i] - sh.soff[i - 1] * sh.sgamma[i - 1];
-          sh.sgamma[i] = sh.soff[i] / sh.salpha[i];
-        }
-        sh.salpha[m - 1] = sh.sdiag[m - 1] - sh.soff[m - 2] * sh.sgamma[m - 2];
-        sh.fac_n = n;
-      }
-      if (in) sh.fac_x[lane] = x_l;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      S z = sh.sg[0];
-      sh.sz[0] = z;
-      for (int i = 1; i < m; i++) {
-        z = sh.sg[i] - sh.sgamma[i - 1] * z;
-        sh.sz[i] = z;
-      }
-    }
-    __syncwarp();
-    if (lane < m) sh.sz[lane] = sh.sz[lane] / sh.salpha[lane];
-    __syncwarp();
-    if (lane == 0) {
-      S c = sh.sz[m - 1];
-      sh.cs[m] = c;
-      for (int k = m - 1; k-- > 0;) {
-        c = sh.sz[k] - sh.sgamma[k] * c;
-        sh.cs[k + 1] = c;
-      }
-    }
-  }
-  __syncwarp();
-  spline_coeffs<S>(sh, n);
-  if (xmax <= xmin) return S(kBad);  // the reference exits the process here
-  S sump;
-  int status = qag_warp<S>(sh, n, true, xmin, xmax, &sump);
-  if (status) status = qag_warp<S>(sh, n, false, xmin, xmax, &sump);
-  if (status) return S(kBad);
-  return s_log(sump) + ymax;
-}
-
-// ------------------------------------------------------------ phased nodes
 // ---- double-float (unevaluated sum of two floats) arithmetic for sin/cos on the FP32 pipes
 __device__ __forceinline__ f2 df_mul(f2 a, f2 b) {
   f2 p = two_prod(a.hi, b.hi);
@@ -827,6 +550,387 @@ __device__ __forceinline__ f2 df_log_double(double x) {
   return df_add(df_log(quick_two_sum(hi, lo)), df_ln2_times((float)e));
 }
 
+
+// ---- a double-float number type for the F64 fit's marginalisation over the scalelength (the
+// natural spline, QUADPACK qag and its 41-point rule, exp and log): the FP64 code instantiated on
+// the FP32 pipes, where each of its dependent operations takes ~15-40 cycles instead of 64-2100
+struct DF {
+  float hi, lo;
+  DF() = default;
+  __device__ __forceinline__ DF(f2 a) : hi(a.hi), lo(a.lo) {}
+  __device__ __forceinline__ DF(double d) {
+    hi = (float)d;
+    lo = isfinite(hi) ? (float)(d - (double)hi) : 0.f;
+  }
+  __device__ __forceinline__ f2 p() const { return f2{hi, lo}; }
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ DF operator+(DF a, DF b) { return DF(df_add(a.p(), b.p())); }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return DF(df_sub(a.p(), b.p())); }
+__device__ __forceinline__ DF operator-(DF a) { return DF(f2{-a.hi, -a.lo}); }
+__device__ __forceinline__ DF operator*(DF a, DF b) { return DF(df_mul(a.p(), b.p())); }
+__device__ __forceinline__ DF operator/(DF a, DF b) { return DF(df_div(a.p(), b.p())); }
+__device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
+__device__ __forceinline__ DF& operator-=(DF& a, DF b) { return a = a - b; }
+__device__ __forceinline__ DF& operator*=(DF& a, DF b) { return a = a * b; }
+__device__ __forceinline__ bool operator<(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(DF a, DF b) { return b < a; }
+__device__ __forceinline__ bool operator<=(DF a, DF b) { return !(b < a); }
+__device__ __forceinline__ bool operator>=(DF a, DF b) { return !(a < b); }
+__device__ __forceinline__ bool operator==(DF a, DF b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(DF a, DF b) { return !(a == b); }
+__device__ __forceinline__ DF s_abs(DF a) { return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? -a : a; }
+__device__ __forceinline__ DF s_exp(DF a) { return DF(df_exp(a.p())); }
+__device__ __forceinline__ DF s_log(DF a) { return DF(df_log(a.p())); }
+__device__ __forceinline__ DF s_pow15(DF a) { return a * DF(df_sqrt(a.p())); }
+__device__ __forceinline__ double s_max(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ double s_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float s_max(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ float s_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ DF s_max(DF a, DF b) { return a < b ? b : a; }
+__device__ __forceinline__ DF s_min(DF a, DF b) { return b < a ? b : a; }
+template <> struct Consts<DF> {
+  static __device__ __forceinline__ DF dbl_eps() { return DF(2.2204460492503131e-16); }
+  static __device__ __forceinline__ DF dbl_min() { return DF(f2{0.f, 0.f}); }  // below the float range
+};
+// warp shuffles of the marginalisation's number types
+__device__ __forceinline__ double sshfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float sshfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ DF sshfl_xor(DF v, int m) {
+  return DF(f2{__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)});
+}
+__device__ __forceinline__ double sshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float sshfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ DF sshfl(DF v, int src) {
+  return DF(f2{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)});
+}
+template <> __device__ __forceinline__ DF wsum<DF>(DF v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v = v + sshfl_xor(v, m);
+  return v;
+}
+// the 41-point rule's abscissae and weights (c_xgk, c_wgk, c_wg) as float pairs
+__constant__ float2 c_xgk2[21] = {
+    {0.9988590478897095f, -1.6301431315923764e-08f}, {0.9931285977363586f, 1.4487362420823047e-09f},
+    {0.9815078973770142f, -1.9926764238675787e-08f}, {0.9639719128608704f, 1.4417043558978548e-08f},
+    {0.9408226609230042f, -2.709125013211633e-08f}, {0.9122344255447388f, 2.7065871766041028e-09f},
+    {0.8782768249511719f, -1.3698890022340038e-08f}, {0.8391169905662537f, -1.874403565693683e-08f},
+    {0.7950414419174194f, -1.3079867855481098e-08f}, {0.7463319301605225f, -2.3700371443169388e-08f},
+    {0.6932376623153687f, -5.9806173346999e-09f}, {0.6360536813735962f, -6.470811664271992e-10f},
+    {0.5751404762268066f, -2.9407097201783472e-08f}, {0.5108669996261597f, 2.324667569553185e-09f},
+    {0.44359317421913147f, 1.0195936317458631e-09f}, {0.3737061023712158f, -1.3655796493594607e-08f},
+    {0.30162787437438965f, -6.259476492687099e-09f}, {0.2277858555316925f, -4.390047436686473e-09f},
+    {0.15260545909404755f, 6.146875008994357e-09f}, {0.07652652263641357f, -1.502916235907037e-09f},
+    {0.0f, 0.0f}};
+__constant__ float2 c_wgk2[21] = {
+    {0.003073583822697401f, -1.0417686852060015e-10f}, {0.008600269444286823f, 4.113561158369805e-10f},
+    {0.014626169577240944f, -3.2026969964960017e-10f}, {0.020388374105095863f, -6.438293231880721e-10f},
+    {0.025882134214043617f, -6.090924431489952e-10f}, {0.0312873050570488f, 1.719984044079581e-09f},
+    {0.03660016879439354f, 9.638072562268007e-10f}, {0.04166887328028679f, 4.768689609857546e-11f},
+    {0.04643482342362404f, -1.5561263388974567e-09f}, {0.05094457417726517f, -2.535364695965825e-10f},
+    {0.05519510433077812f, 1.0175078557494999e-09f}, {0.059111401438713074f, -5.580734763199757e-10f},
+    {0.06265323609113693f, 1.4636442058346688e-09f}, {0.06583459675312042f, 3.80497994223461e-10f},
+    {0.06864867359399796f, -6.654763406999109e-10f}, {0.07105442136526108f, 2.188182968154706e-09f},
+    {0.07303068786859512f, 2.4641915175038775e-09f}, {0.07458287477493286f, 6.255663209664419e-10f},
+    {0.07570450007915497f, -2.3945982974282742e-09f}, {0.07637786865234375f, -9.802629818977948e-10f},
+    {0.07660071551799774f, -3.5999980774192863e-09f}};
+__constant__ float2 c_wg2[10] = {
+    {0.017614006996154785f, 1.429973361943837e-10f}, {0.04060142859816551f, 1.2022214335161152e-09f},
+    {0.06267204880714417f, -4.730351110815434e-10f}, {0.08327674120664597f, 3.7005878916751556e-10f},
+    {0.10193011909723282f, 7.200076090896346e-10f}, {0.11819453537464142f, -3.4131231174683307e-09f},
+    {0.13168863952159882f, -1.0724221510827192e-09f}, {0.14209610223770142f, 7.080680486382107e-09f},
+    {0.14917299151420593f, -5.041602246791399e-09f}, {0.15275338292121887f, 4.2095069652248185e-09f}};
+template <class S> __device__ __forceinline__ S kr(double d, float2 f) { return S(d); }
+template <> __device__ __forceinline__ DF kr<DF>(double d, float2 f) { return DF(f2{f.x, f.y}); }
+
+// state of the marginalisation over the scalelength (marginalise_posterior_warp)
+template <class T>
+struct MargShared {
+  // natural spline rows and the factorisation of its matrix for the abscissae fac_x[0..fac_n)
+  T soff[kMaxNodes], sdiag[kMaxNodes], sg[kMaxNodes], sz[kMaxNodes], salpha[kMaxNodes], sgamma[kMaxNodes];
+  T fac_x[kMaxNodes];
+  int fac_n;
+  T xs[kMaxNodes], ys[kMaxNodes], cs[kMaxNodes];
+  T sb[kMaxNodes], sd[kMaxNodes];         // linear and cubic spline coefficients of each interval
+  T qa[kQagCap], qb[kQagCap], qr[kQagCap], qe[kQagCap];
+  int status;
+};
+// the marginalisation's number type of a fit policy: double-float for the FP64 fit
+template <class S> struct MargNumT { using T = S; };
+template <> struct MargNumT<double> { using T = DF; };
+template <class S> using MargNum = typename MargNumT<S>::T;
+
+template <class S>
+struct FitShared {
+  // phased node evaluation (eval_nodes): per-node state
+  double nx[kMaxNodes], ny[kMaxNodes];    // position shift of each node's Newton search
+  double nnorm[kMaxNodes];                // 1 / the node's model normalisation
+  int alist[kMaxNodes];                   // nodes with a Newton pass pending
+  int nact;
+  S Lr[kMaxNodes];
+  S rprior[kMaxNodes];
+  MargShared<MargNum<S>> mg;              // the marginalisation over the scalelength
+  S bcast_L;
+  int bcast_err;
+  int g;
+  int newton;
+  // sampling board: a claimed grid point and its chunk (owner and helper CTAs)
+  SampleSlot claim_prm;
+  int claim_g, claim_seq, claim_idx, claim_state;
+  int bcast_np;
+  int status;
+};
+
+// ------------------------------------------------- scalelength marginalisation
+template <class S>
+__device__ __forceinline__ S spline_eval(const MargShared<S>& sh, int n, bool cubic, S x, bool* ok) {
+  if (x < sh.xs[0] || x > sh.xs[n - 1]) { *ok = false; return S(0); }
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    int mid = (lo + hi) >> 1;
+    if (sh.xs[mid] > x) hi = mid; else lo = mid;
+  }
+  const S x_lo = sh.xs[lo], x_hi = sh.xs[lo + 1];
+  const S y_lo = sh.ys[lo], y_hi = sh.ys[lo + 1];
+  const S dx = x_hi - x_lo, dy = y_hi - y_lo, delx = x - x_lo;
+  *ok = true;
+  // cubic: the coefficients of gsl_interp_cspline's evaluation, made once per spline (spline_coeffs)
+  if (cubic) return y_lo + delx * (sh.sb[lo] + delx * (sh.cs[lo] + delx * sh.sd[lo]));
+  return y_lo + delx / dx * dy;
+}
+
+// b_i and d_i of every interval of the natural cubic spline (xs, ys, cs), lane i: as the
+// reference's interpolation evaluates them per point (gsl_interp_cspline), once per spline
+template <class S>
+__device__ __forceinline__ void spline_coeffs(MargShared<S>& sh, int n) {
+  const int i = threadIdx.x & 31;
+  if (i < n - 1) {
+    const S dx = sh.xs[i + 1] - sh.xs[i], dy = sh.ys[i + 1] - sh.ys[i];
+    const S c_i = sh.cs[i], c_ip1 = sh.cs[i + 1];
+    sh.sb[i] = (dy / dx) - dx * (c_ip1 + S(2) * c_i) / S(3);
+    sh.sd[i] = (c_ip1 - c_i) / (S(3) * dx);
+  }
+  __syncwarp();
+}
+
+// integrand of marginalise_r.c:231-238: exp(spline(x)), 0 outside the nodes
+template <class S>
+__device__ __forceinline__ S marf(const MargShared<S>& sh, int n, bool cubic, S x) {
+  bool ok;
+  S y = spline_eval(sh, n, cubic, x, &ok);
+  return ok ? s_exp(y) : S(0);
+}
+
+template <class S>
+__device__ __forceinline__ S rescale_error(S err, S result_abs, S result_asc) {
+  err = s_abs(err);
+  if (result_asc != S(0) && err != S(0)) {
+    S scale = s_pow15(S(200) * err / result_asc);
+    err = (scale < S(1)) ? result_asc * scale : result_asc;
+  }
+  if (result_abs > Consts<S>::dbl_min() / (S(50) * Consts<S>::dbl_eps())) {
+    S min_err = S(50) * Consts<S>::dbl_eps() * result_abs;
+    if (min_err > err) err = min_err;
+  }
+  return err;
+}
+
+// QUADPACK qk41 on one warp: lane j < 21 evaluates the integrand at centre -+ half*xgk[j].
+template <class S>
+__device__ __noinline__ void qk41_warp(const MargShared<S>& sh, int n, bool cubic, S a, S b, S* result, S* abserr,
+                          S* resabs, S* resasc) {
+  const int j = threadIdx.x & 31;
+  const S center = S(0.5) * (a + b);
+  const S half = S(0.5) * (b - a);
+  const S abs_half = s_abs(half);
+  S f1 = S(0), f2 = S(0);
+  if (j < 21) {
+    const S absc = half * kr<S>(c_xgk[j], c_xgk2[j]);
+    f1 = marf(sh, n, cubic, center - absc);
+    f2 = (j == 20) ? f1 : marf(sh, n, cubic, center + absc);
+  }
+  const S fc = sshfl(f1, 20);
+  const S wk = (j < 20) ? kr<S>(c_wgk[j], c_wgk2[j]) : S(0);
+  const S wg = (j < 20 && (j & 1)) ? kr<S>(c_wg[j >> 1], c_wg2[j >> 1]) : S(0);
+  const S fsum = f1 + f2;
+  S rk = wsum<S>(wk * fsum) + fc * kr<S>(c_wgk[20], c_wgk2[20]);
+  S rg = wsum<S>(wg * fsum);
+  S ra = wsum<S>(wk * (s_abs(f1) + s_abs(f2))) + s_abs(fc * kr<S>(c_wgk[20], c_wgk2[20]));
+  const S mean = rk * S(0.5);
+  S rasc = wsum<S>(wk * (s_abs(f1 - mean) + s_abs(f2 - mean))) + kr<S>(c_wgk[20], c_wgk2[20]) * s_abs(fc - mean);
+  const S err = (rk - rg) * half;
+  rk *= half;
+  ra *= abs_half;
+  rasc *= abs_half;
+  *result = rk;
+  *resabs = ra;
+  *resasc = rasc;
+  *abserr = rescale_error<S>(err, ra, rasc);
+}
+
+// QUADPACK qag (GSL gsl_integration_qag, key GSL_INTEG_GAUSS41, epsabs 0, epsrel 1e-3):
+// global adaptive bisection of the interval with the largest error.  Control is replicated in
+// the lanes of warp 0; interval lists live in shared memory (kQagCap entries).
+// Returns 0 on success, nonzero as GSL's status would be.
+template <class S>
+__device__ __noinline__ int qag_warp(MargShared<S>& sh, int n, bool cubic, S a, S b, S* out) {
+  const int lane = threadIdx.x & 31;
+  const S epsabs = S(0), epsrel = S(1.e-3);
+  S result0, abserr0, resabs0, resasc0;
+  qk41_warp<S>(sh, n, cubic, a, b, &result0, &abserr0, &resabs0, &resasc0);
+  S tolerance = s_max(epsabs, epsrel * s_abs(result0));
+  const S round_off = S(50) * Consts<S>::dbl_eps() * resabs0;
+  *out = result0;
+  if (abserr0 <= round_off && abserr0 > tolerance) return 18;        // GSL_EROUND
+  if ((abserr0 <= tolerance && abserr0 != resasc0) || abserr0 == S(0)) return 0;
+  if (lane == 0) { sh.qa[0] = a; sh.qb[0] = b; sh.qr[0] = result0; sh.qe[0] = abserr0; }
+  __syncwarp();
+  S area = result0, errsum = abserr0;
+  int nint = 1, iteration = 1, roundoff1 = 0, roundoff2 = 0, error_type = 0;
+  const int limit = 1000;
+  do {
+    // interval with the largest error (lowest index on ties)
+    S best = S(-1);
+    int bi = 0x7fffffff;
+    for (int k = lane; k < nint; k += 32) {
+      S e = sh.qe[k];
+      if (e > best) { best = e; bi = k; }
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+      S ob = sshfl_xor(best, m);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, m);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int imax = bi;
+    const S a_i = sh.qa[imax], b_i = sh.qb[imax], r_i = sh.qr[imax], e_i = sh.qe[imax];
+    const S a1 = a_i, b1 = S(0.5) * (a_i + b_i), a2 = b1, b2 = b_i;
+    S area1, area2, error1, error2, resabs1, resabs2, resasc1, resasc2;
+    qk41_warp<S>(sh, n, cubic, a1, b1, &area1, &error1, &resabs1, &resasc1);
+    qk41_warp<S>(sh, n, cubic, a2, b2, &area2, &error2, &resabs2, &resasc2);
+    const S area12 = area1 + area2, error12 = error1 + error2;
+    errsum += (error12 - e_i);
+    area += area12 - r_i;
+    if (resasc1 != error1 && resasc2 != error2) {
+      const S delta = r_i - area12;
+      if (s_abs(delta) <= S(1.0e-5) * s_abs(area12) && error12 >= S(0.99) * e_i) roundoff1++;
+      if (iteration >= 10 && error12 > e_i) roundoff2++;
+    }
+    tolerance = s_max(epsabs, epsrel * s_abs(area));
+    if (errsum > tolerance) {
+      if (roundoff1 >= 6 || roundoff2 >= 20) error_type = 2;
+      const S tmp = (S(1) + S(100) * Consts<S>::dbl_eps()) * (s_abs(a2) + S(1000) * Consts<S>::dbl_min());
+      if (s_abs(a1) <= tmp && s_abs(b2) <= tmp) error_type = 3;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      sh.qa[imax] = a1; sh.qb[imax] = b1; sh.qr[imax] = area1; sh.qe[imax] = error1;
+      sh.qa[nint] = a2; sh.qb[nint] = b2; sh.qr[nint] = area2; sh.qe[nint] = error2;
+    }
+    __syncwarp();
+    nint++;
+    iteration++;
+    if (nint >= kQagCap && errsum > tolerance && !error_type) {
+      if (lane == 0) sh.status |= 2;
+      error_type = 4;  // device interval capacity: reported like GSL_EMAXITER
+    }
+  } while (iteration < limit && !error_type && errsum > tolerance);
+  S sum = S(0);
+  for (int k = lane; k < nint; k += 32) sum += sh.qr[k];
+  sum = wsum<S>(sum);
+  *out = sum;
+  if (errsum <= tolerance) return 0;
+  if (error_type == 2) return 18;
+  if (error_type == 3) return 21;
+  return 11;
+}
+
+// marginalise_r.c:81-223 on warp 0; (xs, ys, numvals) already in shared memory.
+template <class S>
+__device__ __noinline__ S marginalise_posterior_warp(MargShared<S>& sh, int n) {
+  const int lane = threadIdx.x & 31;
+  const bool in = lane < n;
+  const S y_l = in ? sh.ys[lane] : S(0);
+  const S x_l = in ? sh.xs[lane] : S(0);
+  // ymax: the first maximum above -10 (strict comparison from ymax = -10, marginalise_r.c:90-96)
+  S ymax = (in && y_l > S(-10.0)) ? y_l : S(-10.0);
+  int ypos = (in && y_l > S(-10.0)) ? lane : 0x7fffffff;
+  // xmin, xmax: the node range (it contains the maximum's neighbours, marginalise_r.c:97-106)
+  S xmin = in ? x_l : S(1e300), xmax = in ? x_l : S(-1e300);
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    const S oy = sshfl_xor(ymax, m);
+    const int op = __shfl_xor_sync(0xffffffffu, ypos, m);
+    if (oy > ymax || (oy == ymax && op < ypos)) { ymax = oy; ypos = op; }
+    xmin = s_min(xmin, sshfl_xor(xmin, m));
+    xmax = s_max(xmax, sshfl_xor(xmax, m));
+  }
+  if (in) { sh.ys[lane] = y_l - ymax; sh.cs[lane] = S(0); }
+  // natural cubic spline: c_0 = c_{n-1} = 0, interior from the symmetric tridiagonal system
+  // solved by LDL^T (as gsl_interp_cspline).  The lanes form the rows; the factorisation
+  // (alpha, gamma) depends only on the abscissae and is kept while they do not change.
+  const int m = n - 2;
+  __syncwarp();
+  if (lane < m) {
+    const int i = lane;
+    const S h_i = sh.xs[i + 1] - sh.xs[i], h_ip1 = sh.xs[i + 2] - sh.xs[i + 1];
+    const S dy_i = sh.ys[i + 1] - sh.ys[i], dy_ip1 = sh.ys[i + 2] - sh.ys[i + 1];
+    const S g_i = (h_i != S(0)) ? S(1) / h_i : S(0);
+    const S g_ip1 = (h_ip1 != S(0)) ? S(1) / h_ip1 : S(0);
+    sh.soff[i] = h_ip1;
+    sh.sdiag[i] = S(2) * (h_ip1 + h_i);
+    sh.sg[i] = S(3) * (dy_ip1 * g_ip1 - dy_i * g_i);
+  }
+  const bool same = __all_sync(0xffffffffu, !in || sh.fac_x[lane] == x_l) && sh.fac_n == n;
+  __syncwarp();
+  if (m == 1) {
+    if (lane == 0) sh.cs[1] = sh.sg[0] / sh.sdiag[0];
+  } else if (m > 1) {
+    if (!same) {
+      if (lane == 0) {
+        sh.salpha[0] = sh.sdiag[0];
+        sh.sgamma[0] = sh.soff[0] / sh.salpha[0];
+        for (int i = 1; i < m - 1; i++) {
+          sh.salpha[i] = sh.sdiag[i] - sh.soff[i - 1] * sh.sgamma[i - 1];
+          sh.sgamma[i] = sh.soff[i] / sh.salpha[i];
+        }
+        sh.salpha[m - 1] = sh.sdiag[m - 1] - sh.soff[m - 2] * sh.sgamma[m - 2];
+        sh.fac_n = n;
+      }
+      if (in) sh.fac_x[lane] = x_l;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      S z = sh.sg[0];
+      sh.sz[0] = z;
+      for (int i = 1; i < m; i++) {
+        z = sh.sg[i] - sh.sgamma[i - 1] * z;
+        sh.sz[i] = z;
+      }
+    }
+    __syncwarp();
+    if (lane < m) sh.sz[lane] = sh.sz[lane] / sh.salpha[lane];
+    __syncwarp();
+    if (lane == 0) {
+      S c = sh.sz[m - 1];
+      sh.cs[m] = c;
+      for (int k = m - 1; k-- > 0;) {
+        c = sh.sz[k] - sh.sgamma[k] * c;
+        sh.cs[k + 1] = c;
+      }
+    }
+  }
+  __syncwarp();
+  spline_coeffs<S>(sh, n);
+  if (xmax <= xmin) return S(kBad);  // the reference exits the process here
+  S sump;
+  int status = qag_warp<S>(sh, n, true, xmin, xmax, &sump);
+  if (status) status = qag_warp<S>(sh, n, false, xmin, xmax, &sump);
+  if (status) return S(kBad);
+  return s_log(sump) + ymax;
+}
+
+// ------------------------------------------------------------ phased nodes
 // Ei(x1) and Ei(x2), 0 < x <= 100, evaluated by one lane (each lane its own x).
 //   x <= 2.5: the power series  gamma + ln x + sum_k x^k / (k k!)  (at most 26 terms);
 //   x > 2.5: the Taylor expansion about the nearest integer x0 of
@@ -1202,15 +1306,15 @@ __device__ typename P::S eval_loglike(FitShared<typename P::S>& sh, NodeCache& n
     const unsigned okm = __ballot_sync(0xffffffffu, ok);
     if (ok) {
       const int pos = __popc(okm & ((1u << lane) - 1u));
-      sh.xs[pos] = S(c_fit.ro[lane]);
-      sh.ys[pos] = sh.Lr[lane] + sh.rprior[lane];
+      sh.mg.xs[pos] = MargNum<S>(c_fit.ro[lane]);
+      sh.mg.ys[pos] = MargNum<S>(sh.Lr[lane] + sh.rprior[lane]);
     }
     const int num = __popc(okm);
     __syncwarp();
     S L_e;
     int err = 0;
     if (num > 4) {
-      L_e = marginalise_posterior_warp<S>(sh, num);
+      L_e = S(marginalise_posterior_warp<MargNum<S>>(sh.mg, num));
     } else {
       err = 1;
       L_e = S(kBad);
@@ -1786,7 +1890,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
   extern __shared__ __align__(16) unsigned char dyn[];
   NodeCache nc = node_cache_view(dyn, c_fit.numr);
   const int tid = threadIdx.x;
-  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.mg.status = 0; sh.mg.fac_n = -1; }
   while (true) {
     if (tid == 0) sh.g = atomicAdd(b.queue, 1);
     __syncthreads();
@@ -1799,7 +1903,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
     }
     const Cell* cp[5];
     const int n = bind_galaxy<P>(b, g, cp, sh);
-    if (tid == 0) { sh.newton = 0; sh.status = 0; }
+    if (tid == 0) { sh.newton = 0; sh.status = 0; sh.mg.status = 0; }
     __syncthreads();
     double se1 = 0., se2 = 0., step = 0.1;
     if (b.start) { se1 = b.start[3 * g]; se2 = b.start[3 * g + 1]; step = b.start[3 * g + 2]; }
@@ -1809,7 +1913,7 @@ __global__ void __launch_bounds__(kFitThreads, kFitMinBlocks) k_fit(FacetBatch b
     __syncthreads();
     if (tid == 0) {
       o.newton_iters = sh.newton + (b.board.slot ? *(volatile int*)&b.board.newton[g] : 0);
-      o.status |= sh.status;
+      o.status |= sh.status | sh.mg.status;
       o.ncoords = n;
       b.out[g] = o;
       if (b.board.slot) {
@@ -1834,7 +1938,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_loglike_once(FacetBatch b, d
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
-  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.mg.status = 0; sh.mg.fac_n = -1; }
   __syncthreads();
   int err = 0;
   S L = eval_loglike<P>(sh, nc, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
@@ -1855,7 +1959,7 @@ __global__ void __launch_bounds__(kFitThreads, 1) k_sampling_once(FacetBatch b, 
   const int n = b.count[0];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMaxNodes; i += blockDim.x) sh.rprior[i] = S(b.rprior[i]);
-  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.fac_n = -1; }
+  if (tid == 0) { sh.newton = 0; sh.status = 0; sh.mg.status = 0; sh.mg.fac_n = -1; }
   __syncthreads();
   FitCtx<P> c{&sh, &nc, reinterpret_cast<const Cell*>(b.gu), reinterpret_cast<const Cell*>(b.gv),
               reinterpret_cast<const Cell*>(b.dre), reinterpret_cast<const Cell*>(b.dim),
@@ -1885,7 +1989,7 @@ __global__ void k_xcorr(int n, const double* gu, const double* gv, const double*
 }
 
 __global__ void k_marginalise_once(int n, const double* x, double* y, double* out1) {
-  __shared__ FitShared<double> sh;
+  __shared__ MargShared<double> sh;
   const int lane = threadIdx.x;
   if (lane == 0) { sh.status = 0; sh.fac_n = -1; for (int i = 0; i < n; ++i) { sh.xs[i] = x[i]; sh.ys[i] = y[i]; } }
   __syncwarp();
