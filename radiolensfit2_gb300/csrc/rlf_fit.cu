@@ -428,6 +428,9 @@ struct NodeCache {
   double *cu, *cv;    // [kNodeCache] 2 pi u and 2 pi v of the cells
   double* isg;        // [kNodeCache] 1 / variance of the cells
   f2 *cu2, *cv2;      // [kNodeCache] 2 pi u, 2 pi v as double-float pairs
+  f2 *gu2, *gv2;      // [kNodeCache] u, v (FP64 policy, exponential profile: the double-float passes)
+  f2 *dre2, *dim2;    // [kNodeCache] facet visibility / variance
+  f2* isg2;           // [kNodeCache] 1 / variance
   int nr;
   __device__ __forceinline__ double* P(int k, int node) const { return part + ((size_t)k * nr + node) * kNodePart; }
   __device__ __forceinline__ CacheSlot& H(int node, int i) const { return hre[node * kNodeStride + i]; }
@@ -436,7 +439,7 @@ struct NodeCache {
 // bytes of a NodeCache for nr node rows (a multiple of 16)
 __host__ __device__ __forceinline__ size_t node_cache_bytes(int nr) {
   return (size_t)7 * nr * kNodePart * sizeof(double) + (size_t)2 * nr * kNodeStride * sizeof(CacheSlot) +
-         (size_t)kNodeCache * (3 * sizeof(double) + 2 * sizeof(f2));
+         (size_t)kNodeCache * (3 * sizeof(double) + 7 * sizeof(f2));
 }
 __device__ __forceinline__ NodeCache node_cache_view(unsigned char* base, int nr) {
   NodeCache c;
@@ -449,6 +452,11 @@ __device__ __forceinline__ NodeCache node_cache_view(unsigned char* base, int nr
   c.isg = c.cv + kNodeCache;
   c.cu2 = reinterpret_cast<f2*>(c.isg + kNodeCache);
   c.cv2 = c.cu2 + kNodeCache;
+  c.gu2 = c.cv2 + kNodeCache;
+  c.gv2 = c.gu2 + kNodeCache;
+  c.dre2 = c.gv2 + kNodeCache;
+  c.dim2 = c.dre2 + kNodeCache;
+  c.isg2 = c.dim2 + kNodeCache;
   return c;
 }
 
@@ -1035,6 +1043,40 @@ __device__ __forceinline__ void dsincos_small(double a, double* sa, double* ca) 
   *sa = df_to_double(s);
   *ca = df_to_double(c);
 }
+// a double as a float pair from its bits with integer operations (a conversion through the FP64
+// pipe costs ~80 cycles here): hi = the sign, exponent and top 23 fraction bits, lo = the low 29
+// bits (rounded to 24) scaled to their place (a normal float for exponents from -74).  Zero and
+// subnormal doubles give 0; other exponents below -74 or above 127 take the FP64 conversion.
+__device__ __forceinline__ f2 df_from_double_bits(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < -74 || e > 127) return (b & 0x7ff0000000000000ull) ? df_from_double(d) : f2{0.f, 0.f};
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  const float scale = __uint_as_float((unsigned)(e - 52 + 127) << 23);  // 2^(e - 52), e - 52 >= -126
+  const float lo = (float)(unsigned)(b & 0x1fffffffull) * scale;
+  return f2{hi, sign ? -lo : lo};
+}
+
+// (1 + q)^(-3/2), q >= 0, in double-float.  With y the FP32 estimate of (1 + q)^(-1/2) and
+// e = 1 - (1 + q) y^2 (|e| ~1e-7), (1 + q)^(-1/2) = y (1 - e)^(-1/2) = y (1 + e/2 + 3e^2/8 + ...)
+// by the binomial series; the terms kept leave O(e^3) ~1e-21, below the pair's precision.
+__device__ __forceinline__ f2 df_profile_exp(f2 q) {
+  const f2 den = df_add(f2{1.f, 0.f}, q);
+  const float y = rsqrtf(den.hi);
+  const f2 e = df_sub(f2{1.f, 0.f}, df_mul(den, two_prod(y, y)));
+  const f2 c = df_add(f2{0.5f * e.hi, 0.5f * e.lo}, f2{0.375f * e.hi * e.hi, 0.f});
+  const f2 r = df_add(f2{y, 0.f}, df_mul(f2{y, 0.f}, c));
+  return df_mul(df_sqr(r), r);
+}
+// the exponential-profile model of one cell (galaxy_visibilities.c:48-53 with the sheared k of
+// :63-69), double-float: k1 = a1 u + a2 v, k2 = a2 u + a3 v, (1 + sfw (k1^2 + k2^2))^(-3/2)
+__device__ __forceinline__ f2 df_cell_model(f2 a1, f2 a2, f2 a3, f2 u, f2 v, f2 sfw) {
+  const f2 k1 = df_add(df_mul(a1, u), df_mul(a2, v));
+  const f2 k2 = df_add(df_mul(a2, u), df_mul(a3, v));
+  return df_profile_exp(df_mul(sfw, df_add(df_sqr(k1), df_sqr(k2))));
+}
+
 __device__ __forceinline__ void pass_sincos(double a, double* sa, double* ca) {
   if (fabs(a) <= 0.78539816339744831) dsincos_small(a, sa, ca);
   else sincos(a, sa, ca);
@@ -1099,11 +1141,45 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
     nc.cu2[i] = df_from_double(nc.cu[i]);
     nc.cv2[i] = df_from_double(nc.cv[i]);
     nc.isg[i] = (double)(T(1) / T(sig2[i]));
+    if (!P::kMixed && !gaussian) {
+      nc.gu2[i] = df_from_double((double)gu[i]);
+      nc.gv2[i] = df_from_double((double)gv[i]);
+      nc.dre2[i] = df_from_double((double)dre[i]);
+      nc.dim2[i] = df_from_double((double)dim[i]);
+      nc.isg2[i] = df_from_double(nc.isg[i]);
+    }
   }
   __syncthreads();
+  // FP64 policy, exponential profile: the model and zero-shift passes and the model of the cells
+  // beyond the cache in double-float (an FP64 (1 + q)^(-3/2) chain costs ~1200 cycles here)
+  const bool dfm = !P::kMixed && !gaussian;
+  const f2 a1d = df_from_double(1.0 + e1), a2d = df_from_double(e2), a3d = df_from_double(1.0 - e1);
+  auto sfw_df = [&](int node) -> f2 {
+    const double sc = c_fit.ro[node] * (kPi / 648000.0);
+    return df_from_double(((sc * sc) / (detA * detA)) * (4 * kPi * kPi));
+  };
+  auto model_df = [&](int i, f2 sfw, f2 inn) -> f2 {
+    return df_mul(df_cell_model(a1d, a2d, a3d, df_from_double_bits((double)gu[i]), df_from_double_bits((double)gv[i]),
+                                sfw), inn);
+  };
   for (int g = warp; g < groups; g += nw) {
     const int node = 1 + g * kNodesPerWarp + seg;
-    if (node < numR) {
+    if (dfm && node < numR) {
+      const f2 sfw = sfw_df(node);
+      f2 acc{0.f, 0.f};
+      int i = c0;
+      for (; i < ncache; i += kNodePart) {
+        const f2 m = df_cell_model(a1d, a2d, a3d, nc.gu2[i], nc.gv2[i], sfw);
+        nc.H(node, i).f = m;
+        acc = df_add(acc, df_mul(df_sqr(m), nc.isg2[i]));
+      }
+      for (; i < n; i += kNodePart) {
+        const f2 m = df_cell_model(a1d, a2d, a3d, df_from_double_bits((double)gu[i]), df_from_double_bits((double)gv[i]),
+                                   sfw);
+        acc = df_add(acc, df_div(df_sqr(m), df_from_double_bits((double)sig2[i])));
+      }
+      nc.P(0, node)[c0] = df_to_double(acc);
+    } else if (node < numR) {
       const T sfw = sfw_of(node);
       Acc<T> acc;
       acc.zero();
@@ -1132,7 +1208,32 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
   // ---- B: cross-correlation at zero shift; caches data x model
   for (int g = warp; g < groups; g += nw) {
     const int node = 1 + g * kNodesPerWarp + seg;
-    if (node < numR) {
+    if (dfm && node < numR) {
+      const f2 sfw = sfw_df(node), inn = df_from_double(sh.nnorm[node]);
+      f2 val{0.f, 0.f}, dx{0.f, 0.f}, dy{0.f, 0.f}, d2x{0.f, 0.f}, d2y{0.f, 0.f}, dxy{0.f, 0.f};
+      for (int i = c0; i < n; i += kNodePart) {
+        const bool cached = i < kNodeCache;
+        const f2 m = cached ? df_mul(nc.H(node, i).f, inn) : model_df(i, sfw, inn);
+        const f2 hre = df_mul(cached ? nc.dre2[i] : df_from_double_bits((double)dre[i]), m);
+        const f2 him = df_neg(df_mul(cached ? nc.dim2[i] : df_from_double_bits((double)dim[i]), m));
+        if (cached) {
+          nc.H(node, i).f = hre;
+          nc.M(node, i).f = him;
+        }
+        const f2 u = cached ? nc.cu2[i] : df_from_double_bits((2 * kPi) * (double)gu[i]);
+        const f2 v = cached ? nc.cv2[i] : df_from_double_bits((2 * kPi) * (double)gv[i]);
+        val = df_add(val, hre);
+        dx = df_sub(dx, df_mul(him, u));
+        dy = df_sub(dy, df_mul(him, v));
+        const f2 ru = df_mul(hre, u), rv = df_mul(hre, v);
+        d2x = df_sub(d2x, df_mul(ru, u));
+        d2y = df_sub(d2y, df_mul(rv, v));
+        dxy = df_sub(dxy, df_mul(ru, v));
+      }
+      nc.P(1, node)[c0] = df_to_double(val); nc.P(2, node)[c0] = df_to_double(dx);
+      nc.P(3, node)[c0] = df_to_double(dy); nc.P(4, node)[c0] = df_to_double(d2x);
+      nc.P(5, node)[c0] = df_to_double(d2y); nc.P(6, node)[c0] = df_to_double(dxy);
+    } else if (node < numR) {
       const T sfw = sfw_of(node), nn = T(sh.nnorm[node]);
       Acc<T> val, dx, dy, d2x, d2y, dxy;
       val.zero(); dx.zero(); dy.zero(); d2x.zero(); d2y.zero(); dxy.zero();
@@ -1232,10 +1333,21 @@ __device__ void eval_nodes(FitShared<typename P::S>& sh, NodeCache& nc, const ty
         };
         int i = c0;
         for (; i < ncache; i += kNodePart) cell(nc.H(node, i).f, nc.M(node, i).f, nc.cu2[i], nc.cv2[i]);
+        f2 sfwd{0.f, 0.f}, innd{0.f, 0.f};
+        if (dfm && i < n) {
+          sfwd = sfw_df(node);
+          innd = df_from_double(sh.nnorm[node]);
+        }
         for (; i < n; i += kNodePart) {
-          const T m = model(i, sfw, nn);
-          cell(df_from_double(T(dre[i]) * m), df_from_double(-T(dim[i]) * m), df_from_double(cc * T(gu[i])),
-               df_from_double(cc * T(gv[i])));
+          if (dfm) {
+            const f2 m = model_df(i, sfwd, innd);
+            cell(df_mul(df_from_double_bits((double)dre[i]), m), df_neg(df_mul(df_from_double_bits((double)dim[i]), m)),
+                 df_from_double_bits((2 * kPi) * (double)gu[i]), df_from_double_bits((2 * kPi) * (double)gv[i]));
+          } else {
+            const T m = model(i, sfw, nn);
+            cell(df_from_double(T(dre[i]) * m), df_from_double(-T(dim[i]) * m), df_from_double(cc * T(gu[i])),
+                 df_from_double(cc * T(gv[i])));
+          }
         }
         nc.P(1, node)[c0] = df_to_double(val); nc.P(2, node)[c0] = df_to_double(dx);
         nc.P(3, node)[c0] = df_to_double(dy); nc.P(4, node)[c0] = df_to_double(d2x);
