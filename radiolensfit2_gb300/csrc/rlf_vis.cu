@@ -820,12 +820,6 @@ int launch_average_facets(long long size, double2* vis, double* sigma2, const do
   return check("k_average_facets");
 }
 
-__global__ void k_c64_to_f32(long long n, const double2* in, float2* out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double2 x = in[i];
-    out[i] = make_float2((float)x.x, (float)x.y);
-  }
-}
 __global__ void k_f32_to_c64(long long n, const float2* in, double2* out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float2 x = in[i];
@@ -898,11 +892,6 @@ int launch_invert_perm(int n, const int* perm, int* inv, cudaStream_t st) {
   return check("k_invert_perm");
 }
 
-int launch_convert_c64_to_f32(long long n, const double2* in, float2* out, cudaStream_t st) {
-  if (n <= 0) return 0;
-  k_c64_to_f32<<<4096, 256, 0, st>>>(n, in, out);
-  return check("k_c64_to_f32");
-}
 int launch_convert_f32_to_c64(long long n, const float2* in, double2* out, cudaStream_t st) {
   if (n <= 0) return 0;
   k_f32_to_c64<<<4096, 256, 0, st>>>(n, in, out);

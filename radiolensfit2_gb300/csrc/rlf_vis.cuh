@@ -115,10 +115,9 @@ int launch_facet_coords(double* gu, double* gv, double len, unsigned F, const do
                         unsigned* n_out, cudaStream_t st);
 int launch_average_facets(long long size, double2* vis, double* sigma2, const double* sum_w,
                           cudaStream_t st);
-// visibility layout conversion: complexd [ch][row] <-> float2 [ch][row] / double2
-int launch_convert_c64_to_f32(long long n, const double2* in, float2* out, cudaStream_t st);
+// visibility conversion float2 [ch][row] -> double2 [ch][row]
 int launch_convert_f32_to_c64(long long n, const float2* in, double2* out, cudaStream_t st);
-// The same between the caller's visibility order ([ch][row], index ch * n_rows + row) and an
+// Conversions between the caller's visibility order ([ch][row], index ch * n_rows + row) and an
 // observation stored with its rows permuted (position inv[row]; launch_row_order): the caller's
 // elements [i0, i0 + count) from / to a buffer holding just those elements, so that the host side
 // is read or written in order and the device side is scattered or gathered.
