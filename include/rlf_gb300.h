@@ -145,6 +145,11 @@ int rlf_debug_fit_trace(void *likelihood_params_facet, double *trace, int cap, d
  * node_L[1..numr-1] = the per-scalelength-node log-likelihoods before the marginalisation. */
 int rlf_debug_loglike_nodes(void *likelihood_params_facet, double e1, double e2, int precision,
                             double *out2, double *node_L);
+/* Testing aid (no counterpart in the reference): the fit's double-float functions on n inputs,
+ * out[i] = f(x[i]) (or x[i] / y[i]) evaluated in float pairs and returned as doubles; op 0 exp,
+ * 1 log (inputs in the float range), 2 log of any positive normal double, 3 x / y, 4 sqrt,
+ * 5 (1 + x)^(-3/2), 6 the integer split of a double into a float pair.  Returns nonzero on error. */
+int rlf_debug_df_math(int op, int n, const double *x, const double *y, double *out);
 /* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
  * [total, extract, fit, remove] */
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);

@@ -79,6 +79,7 @@ def load():
         "rlf_obs_extract": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.c_int, PD, C.c_int, PI]),
         "rlf_debug_fit_trace": (C.c_int, [C.c_void_p, PD, C.c_int, PD, C.c_int]),
         "rlf_debug_loglike_nodes": (C.c_int, [C.c_void_p, D, D, C.c_int, PD, PD]),
+        "rlf_debug_df_math": (C.c_int, [C.c_int, C.c_int, PD, PD, PD]),
         "rlf_gridding_visibilities_noalloc": (C.c_int, [PD, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p,
                                                         C.c_void_p, C.c_void_p, D, C.c_uint, C.c_void_p,
                                                         C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -127,7 +128,7 @@ EXPORTED = [
     "rlf_ms_read_flag", "rlf_ms_read_vis", "rlf_ms_read_sigma2", "rlf_ms_write_vis",
     "rlf_obs_set_vis", "rlf_obs_set_data_c64", "rlf_obs_get_vis", "rlf_obs_simulate",
     "rlf_obs_sky_model", "rlf_obs_snapshot", "rlf_obs_restore", "rlf_obs_process",
-    "rlf_obs_last_timing", "rlf_obs_last_stats", "rlf_obs_extract", "rlf_debug_fit_trace", "rlf_debug_loglike_nodes", "rlf_gridding_visibilities_noalloc", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
+    "rlf_obs_last_timing", "rlf_obs_last_stats", "rlf_obs_extract", "rlf_debug_fit_trace", "rlf_debug_loglike_nodes", "rlf_debug_df_math", "rlf_gridding_visibilities_noalloc", "facet_size", "evaluate_uv_grid_size", "evaluate_facet_coords",
     "gridding_visibilities", "average_facets", "gaussian_shape", "sersic_shape",
     "model_galaxy_visibilities_at_zero", "data_galaxy_visibilities", "data_visibilities_phase_shift",
     "f_likelihood", "loglikelihood", "loglikelihood_r", "cross_correlation",

@@ -1647,6 +1647,21 @@ int rlf_debug_fit_trace(void* pv, double* trace, int cap, double* out6, int prec
   return 0;
 }
 
+int rlf_debug_df_math(int op, int n, const double* x, const double* y, double* out) {
+  if (op < 0 || op > 6 || n < 0 || (n > 0 && (!x || !out || (op == 3 && !y)))) return 1;
+  if (n == 0) return 0;
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  DevBuf<double> dx, dy, dout;
+  RLF_OK(dx.upload(x, (size_t)n, st));
+  if (op == 3) RLF_OK(dy.upload(y, (size_t)n, st));
+  RLF_OK(dout.ensure((size_t)n));
+  RLF_OK(launch_df_math(op, n, dx.p, op == 3 ? dy.p : nullptr, dout.p, st));
+  RLF_OK(dout.download(out, (size_t)n, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
 int rlf_debug_loglike_nodes(void* pv, double e1, double e2, int precision, double* out2, double* node_L) {
   likelihood_params* par = (likelihood_params*)pv;
   cudaStream_t st;

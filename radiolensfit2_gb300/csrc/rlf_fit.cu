@@ -482,8 +482,9 @@ __device__ __forceinline__ f2 df_horner(f2 P, f2 y, float c_hi, float c_lo) {
 // ---- double-float division, square root, exp and log for the fit's serial phases.  Dependent
 // FP64 operations on this GPU take 64 cycles (fma) to ~550 (division), ~700 (square root), ~1150
 // (exp) and ~2100 (log); an FP32 fma ~5 and a double-float multiply ~22.  Largest relative errors
-// against FP64 over the ranges the fit uses: division 1.3e-14, square root 6e-15, exp 7e-14 (the
-// squarings of its reduced argument amplify), log 4e-14.
+// against FP64 (tests/test_gpu_dfmath.py): division 1e-14, square root 6e-15, exp 1e-13 over
+// [-40, 40] (the squarings of its reduced argument amplify), log 5e-13 of max(|log|, 1) over
+// e^[-80, 80], log of a double 4e-14.
 __device__ __forceinline__ f2 df_sqr(f2 a) {
   f2 p = two_prod(a.hi, a.hi);
   p.lo = fmaf(2.f * a.hi, a.lo, p.lo);
@@ -543,15 +544,18 @@ __device__ __forceinline__ f2 df_ln2_times(float e) {
   f2 l = df_add(two_prod(e, 3.194618329871446e-05f), f2{e * 1.6465949697480609e-12f, 0.f});
   return df_add(f2{e * 0.693115234375f, 0.f}, l);
 }
-// log(a), a > 0 within the float range: y0 = log(a.hi) from the SFU, then
-// log(a) = y0 + log(1 + d), d = a exp(-y0) - 1 (|d| ~1e-6): y0 + d - d^2 / 2; -inf for 0, NaN
-// below, inf for inf
+// log(a), a > 0 within the float range: a = m 2^e with m in [1, 2) (an exact scaling), then
+// y0 = log(m.hi) from the SFU and log(m) = y0 + log(1 + d), d = m exp(-y0) - 1 (|d| ~1e-6):
+// y0 + d - d^2 / 2, plus e ln2; -inf for 0, NaN below, inf for inf
 __device__ __forceinline__ f2 df_log(f2 a) {
   if (!(a.hi > 0.f) || isinf(a.hi))
     return f2{a.hi == 0.f ? -__int_as_float(0x7f800000) : (a.hi > 0.f ? a.hi : __int_as_float(0x7fc00000)), 0.f};
-  const float y0 = __logf(a.hi);
-  const f2 d = df_sub(df_mul(a, df_exp(f2{-y0, 0.f})), f2{1.f, 0.f});
-  return df_add(f2{y0, 0.f}, df_add(d, f2{-0.5f * d.hi * d.hi, 0.f}));
+  int e = ((__float_as_int(a.hi) >> 23) & 0xff) - 127;  // -127 for subnormal high parts
+  if (e > 126) e = 126;
+  const f2 m = df_scale(a, __int_as_float((127 - e) << 23));
+  const float y0 = __logf(m.hi);
+  const f2 d = df_sub(df_mul(m, df_exp(f2{-y0, 0.f})), f2{1.f, 0.f});
+  return df_add(df_add(f2{y0, 0.f}, df_add(d, f2{-0.5f * d.hi * d.hi, 0.f})), df_ln2_times((float)e));
 }
 // log(x) of a positive normal double of any magnitude: x = m 2^e with m in [1, 2) split into a
 // float pair from its bits (the low part's 29 bits rounded to 24), log m + e ln2
@@ -2276,6 +2280,29 @@ int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double
 int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st) {
   k_marginalise_once<<<1, 32, 0, st>>>(n, x, y, out1);
   return check("k_marginalise_once");
+}
+__global__ void k_df_math(int op, int n, const double* __restrict__ x, const double* __restrict__ y,
+                          double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const f2 a = df_from_double(x[i]);
+    f2 r{0.f, 0.f};
+    switch (op) {
+      case 0: r = df_exp(a); break;
+      case 1: r = df_log(a); break;
+      case 2: r = df_log_double(x[i]); break;
+      case 3: r = df_div(a, df_from_double(y[i])); break;
+      case 4: r = df_sqrt(a); break;
+      case 5: r = df_profile_exp(a); break;
+      default: r = df_from_double_bits(x[i]); break;
+    }
+    out[i] = df_to_double(r);
+  }
+}
+int launch_df_math(int op, int n, const double* x, const double* y, double* out, cudaStream_t st) {
+  if (op < 0 || op > 6) return 1;
+  if (n <= 0) return 0;
+  k_df_math<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, st>>>(op, n, x, y, out);
+  return check("k_df_math");
 }
 int launch_set_posterior_values(int numR, const double* Lr, const double* rprior, const double* ro,
                                 double* x, double* y, int* numvals, cudaStream_t st) {

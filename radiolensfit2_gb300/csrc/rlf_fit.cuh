@@ -92,6 +92,8 @@ int launch_loglikelihood_prec(const FacetBatch& b, double e1, double e2, double*
 int launch_likelihood_sampling(const FacetBatch& b, double e1, double e2, double maxL, int np_max,
                                double* out5, cudaStream_t st);
 int launch_marginalise_posterior_r(int n, const double* x, double* y, double* out1, cudaStream_t st);
+// the double-float functions of the fit on device arrays (rlf_debug_df_math)
+int launch_df_math(int op, int n, const double* x, const double* y, double* out, cudaStream_t st);
 int launch_set_posterior_values(int numR, const double* Lr, const double* rprior, const double* ro,
                                 double* x, double* y, int* numvals, cudaStream_t st);
 int launch_position_marginal(int n, const double* x, double* y, cudaStream_t st);
