@@ -7,7 +7,7 @@
   through the batched path, including the final data and sky model.
 
 Tolerances: the F64 path follows the reference arithmetic (fitted e within 1e-7); the batched
-path (FP32 visibility passes, FP64 fit, 3 rounds) within the benchmark spec bound 1e-4 in e.
+path (FP32 visibility passes, FP64 fit, 3 rounds) within 1e-4 in e, the accuracy required of it.
 """
 import numpy as np
 import pytest

@@ -2,7 +2,7 @@
 kernel, fits of the F64 and mixed paths, and the batched mode against the one-galaxy-at-a-time
 mode.  Tolerances: F64 follows the reference arithmetic (1e-11 on facets); the mixed path keeps
 visibilities and model arithmetic in FP32 with compensated sums, so its facets agree to ~1e-6 of
-the facet noise level and its fitted ellipticities to 1e-4 (the benchmark spec tolerance)."""
+the facet noise level and its fitted ellipticities to 1e-4 (the accuracy required of it)."""
 import numpy as np
 import pytest
 
