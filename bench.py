@@ -169,12 +169,6 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def cpu_baseline_sample(obs, cat, galaxies=1):
-    """Time the oracle (OpenMP, all cores) on `galaxies` galaxies of the workload (first pass)."""
-    ns = argparse.Namespace(workload=None, galaxies=0, steps=1, warmup=0, cpu_sample_galaxies=galaxies, gpus=1)
-    return ns
-
-
 def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec):
     """Galaxies/s through the reference-facing entry point data_processing() with pinned host
     buffers: catalogue pass + re-fit pass (RadioLensfit2.cpp:597-606), copies inside the timing.
@@ -187,7 +181,7 @@ def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec
     from radiolensfit2_gb300.abi import LikelihoodParams, dptr, fptr, cptr, bptr
     opt = _lib.Options()
     opt.precision, opt.batch, opt.refit, opt.fit_precision = _lib.RLF_MIXED, B, 1, fit_prec
-    opt.fresh_obs = 0
+    opt.reuse_obs = 1  # the two passes pass the same uvw, variances and flags
     lib.rlf_configure(C.byref(opt))
     n_vis = obs.n_vis
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()

@@ -23,7 +23,8 @@ typedef struct {
   int iters;         /* simplex iterations */
   int nevals;        /* likelihood evaluations */
   int newton_iters;  /* Newton iterations over all nodes and evaluations */
-  int status;        /* 0, or device-side limits reached (2: QAG intervals, 4: bad simplex start) */
+  int status;        /* 0, or device-side limits reached (2: QAG intervals, 4: bad simplex start,
+                        8: a sampling-grid point not delivered within rlf_options.board_wait_us) */
   int ncoords;       /* facet cells */
   double max_e1, max_e2;  /* simplex maximum, before the likelihood sampling */
 } rlf_fit_result;
@@ -44,11 +45,16 @@ typedef struct {
                         extracts every galaxy of the batch from the same data; each further round
                         removes the previous round's fitted models of the earlier galaxies of the
                         batch from each facet, converging to the one-galaxy-at-a-time result. */
-  int fresh_obs;     /* data_processing: 0 (default) keeps the observation's device copies of uvw,
-                        sigma2_vis, flag and the facet tables built from them between calls that pass
-                        the same arrays (same addresses and sizes, same sampled contents), as the
-                        reference driver's two passes do; visibilities and sky model are uploaded on
-                        every call.  1 rebuilds everything on every call (arrays changed in place). */
+  int reuse_obs;     /* data_processing: 0 (default) uploads uvw, sigma2_vis and flag and builds the
+                        facet tables on every call, as the reference reads them fresh on every call.
+                        1 keeps them on the device between calls that pass the same arrays (same
+                        addresses and sizes, same sampled contents), as the reference driver's two
+                        passes do: the caller promises not to change uvw, sigma2_vis or flag in place
+                        between such calls (a change at an unsampled position is not seen).
+                        Visibilities and sky model are uploaded on every call either way. */
+  int board_wait_us; /* the fit's limit, in microseconds, on a galaxy's wait for sampling-grid points
+                        that other thread blocks claimed (0 = default 2 s); a point not delivered in
+                        time counts as a failed evaluation and sets status bit 8 */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -136,20 +142,6 @@ int rlf_obs_process(rlf_observation *obs, int n_gal, const double *flux, const d
 int rlf_obs_extract(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
                     const double *l, const double *m, int batch, double *facets, int stride,
                     int *ncoords);
-/* Debugging aid: source_fitting of one facet given as likelihood_params (datatype.h:49-74) in
- * the given precision, recording (e1, e2, L, error) of every likelihood evaluation into
- * trace[cap][4]; out6 = (e1, e2, simplex max e1, max e2, maxL, evaluations). */
-int rlf_debug_fit_trace(void *likelihood_params_facet, double *trace, int cap, double *out6,
-                        int precision);
-/* Debugging aid: one loglikelihood evaluation of a facet in the given precision; out2 = (L, error),
- * node_L[1..numr-1] = the per-scalelength-node log-likelihoods before the marginalisation. */
-int rlf_debug_loglike_nodes(void *likelihood_params_facet, double e1, double e2, int precision,
-                            double *out2, double *node_L);
-/* Testing aid (no counterpart in the reference): the fit's double-float functions on n inputs,
- * out[i] = f(x[i]) (or x[i] / y[i]) evaluated in float pairs and returned as doubles; op 0 exp,
- * 1 log (inputs in the float range), 2 log of any positive normal double, 3 x / y, 4 sqrt,
- * 5 (1 + x)^(-3/2), 6 the integer split of a double into a float pair.  Returns nonzero on error. */
-int rlf_debug_df_math(int op, int n, const double *x, const double *y, double *out);
 /* CUDA events around the last rlf_obs_process: total and per-stage milliseconds
  * [total, extract, fit, remove] */
 int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
@@ -196,9 +188,12 @@ int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
  * Limits: sizeg <= RLF_NOALLOC_MAX_FACET, 1 <= num_channels <= 512; other sizes return an error.
  * The partial sums live in one fixed 4.6 MiB array of this library's device memory that every
  * GPU loading the library holds until exit.  The first call on a device looks up that array's
- * device address, so make a first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU (other threads or streams) race and must be serialised by the
- * caller.  Returns 0, or non-zero with a message on stderr. */
+ * device address and caches it for the process (not valid across cudaDeviceReset).  The call
+ * synchronises `stream` and cannot be captured into a CUDA graph.  Every call rewrites the
+ * library's constant channel table and the gridding kernel's shared-memory attribute, which all
+ * entry points of this library share: a call that overlaps any other call of the library (other
+ * threads or streams, no-allocation or not) races with it, so the caller serialises all calls.
+ * Returns 0, or non-zero with a message on stderr. */
 #define RLF_NOALLOC_MAX_FACET 48
 int rlf_gridding_visibilities_noalloc(const double *wavenumbers, unsigned int num_channels,
                                       unsigned int ncoords, const double *u, const double *v,

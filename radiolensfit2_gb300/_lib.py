@@ -35,7 +35,8 @@ class Options(C.Structure):
     """rlf_options (include/rlf_gb300.h)"""
     _fields_ = [("precision", C.c_int), ("batch", C.c_int), ("gaussian", C.c_int),
                 ("refit", C.c_int), ("verbose", C.c_int), ("start", PD), ("fit_precision", C.c_int),
-                ("rounds", C.c_int), ("fresh_obs", C.c_int)]
+                ("rounds", C.c_int), ("reuse_obs", C.c_int),
+                ("board_wait_us", C.c_int)]
 
 
 _lib = None

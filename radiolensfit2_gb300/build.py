@@ -43,7 +43,8 @@ def _stale(target: str, deps) -> bool:
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(os.path.dirname(HERE), "include", "rlf_gb300.h"))
+    for h in ("rlf_gb300.h", "rlf_testing.h", "rlf_reference_abi.h"):
+        headers.append(os.path.join(os.path.dirname(HERE), "include", h))
     cc = nvcc()
     objs = []
     jobs = []

@@ -21,6 +21,7 @@
 #include "rlf_batch.cuh"
 #include "rlf_ms.cuh"
 #include "../../include/rlf_gb300.h"
+#include "../../include/rlf_testing.h"
 
 typedef struct {
   double real;
@@ -117,7 +118,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -498,6 +499,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       fb.board.flag = bflag.p;
       fb.board.newton = bnewton.p;
       fb.board.done_gal = bdone.p;
+      fb.board.wait_ns = opt.board_wait_us > 0 ? (unsigned long long)opt.board_wait_us * 1000ull : 0ull;
     }
     SeqBatch sb{};
     if (u.seq) {
@@ -1767,13 +1769,16 @@ void sky_model(double* wavenumbers, double* spec, double channel_bandwidth_hz, i
   delete ob;
 }
 
-// The observation of the last data_processing call, kept with its device copies (uvw, variances,
-// flags, row table) and the facet tables built from them while later calls pass the same arrays:
-// the reference driver passes the same uvw, sigma2_vis, flag and channel arrays to both passes
-// (RadioLensfit2.cpp:597-606).  The key holds the arrays' addresses and sizes and a fingerprint of
-// their sampled contents (all channel values, 4096 evenly spaced rows and visibilities), so a
-// different observation placed at the same addresses is rebuilt.  Visibilities and sky model are
-// uploaded on every call.  rlf_options.fresh_obs = 1 rebuilds on every call; rlf_release frees it.
+// With rlf_options.reuse_obs = 1, the observation of the last data_processing call is kept with its
+// device copies (uvw, variances, flags, row table) and the facet tables built from them while later
+// calls pass the same arrays: the reference driver passes the same uvw, sigma2_vis, flag and channel
+// arrays to both passes (RadioLensfit2.cpp:597-606).  The key holds the arrays' addresses and sizes
+// and a fingerprint of their sampled contents (all channel values, 4096 evenly spaced rows and
+// visibilities), so a different observation placed at the same addresses is rebuilt; a change at an
+// unsampled position is the caller's promise not to make.  The default (reuse_obs = 0) builds the
+// observation on every call, as the reference reads its arrays on every call
+// (data_processing.c:82-84).  Visibilities and sky model are uploaded on every call; rlf_release
+// frees a kept observation.
 struct ObsKey {
   int n_rows = 0, n_ch = 0, precision = -1, has_flag = 0;
   const void *uu = nullptr, *vv = nullptr, *ww = nullptr, *sigma2 = nullptr, *flag = nullptr;
@@ -1828,7 +1833,7 @@ void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, doub
   rlf_observation* ob = nullptr;
   const ObsKey key = obs_key((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres, par->wavenumbers,
                              par->spec, len, sigma2_vis, flag8, opt.precision);
-  if (!opt.fresh_obs && g_obs_cached && key == g_obs_key) {
+  if (opt.reuse_obs && g_obs_cached && key == g_obs_key) {
     ob = g_obs_cached;
   } else {
     delete g_obs_cached;
@@ -1836,7 +1841,7 @@ void data_processing(bool re_fitting, unsigned int* bad_list, int nsources, doub
     ob = obs_create((int)num_coords, (int)par->nchannels, uu_metres, vv_metres, ww_metres, par->wavenumbers, par->spec,
                     len, sigma2_vis, flag8, opt.precision, st);
     if (!ob) return;
-    if (!opt.fresh_obs) { g_obs_cached = ob; g_obs_key = key; }
+    if (opt.reuse_obs) { g_obs_cached = ob; g_obs_key = key; }
   }
   // the observation is freed on the way out unless it is the cached one
   struct Release {

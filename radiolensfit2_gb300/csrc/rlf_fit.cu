@@ -1551,10 +1551,11 @@ __device__ void board_chunk(FitCtx<P>& c, int seq, const SampleSlot& prm) {
   if (threadIdx.x == 0) {
     const size_t row = board_row(c.g, seq);
     const unsigned long long t0 = global_ns();
+    const unsigned long long limit = bd.wait_ns ? bd.wait_ns : kBoardWaitNs;
     for (int k = 0; k < prm.npts; ++k) {
       const volatile int* f = bd.flag + row + k;
       while (*f != seq) {
-        if (global_ns() - t0 > kBoardWaitNs) break;
+        if (global_ns() - t0 > limit) break;
         __nanosleep(200);
       }
       if (*f != seq) {  // a helper did not deliver within the limit: the point counts as an error

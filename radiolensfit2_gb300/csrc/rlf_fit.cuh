@@ -12,7 +12,8 @@ struct FitOut {
   int iters;         // simplex iterations
   int nevals;        // likelihood evaluations (simplex + sampling)
   int newton_iters;  // Newton iterations summed over scalelength nodes and evaluations
-  int status;        // 0 ok; bit 1: QAG interval capacity reached; bit 2: non-finite simplex start
+  int status;        // 0 ok; bit 1: QAG interval capacity reached; bit 2: non-finite simplex start;
+                     // bit 3: a sampling-grid point not delivered within the board wait limit
   int ncoords;       // facet cells used
   double max_e1, max_e2;  // simplex maximum (before the sampling of likelihood.c:428-554)
 };
@@ -42,6 +43,7 @@ struct SampleBoard {
   int* flag;                    // [n_gal][2][kBoardCap] sequence of the chunk the result belongs to
   int* newton;                  // [n_gal] Newton iterations of the helpers' evaluations
   int* done_gal;                // galaxies finished in this launch
+  unsigned long long wait_ns;   // an owner's limit on waiting for the helpers' points (0: kBoardWaitNs)
 };
 
 // A batch of facets packed back to back.  Cell arrays hold either double (kF64) or float

@@ -10,6 +10,15 @@
 // The scratch array holds kNoAllocParts partial facets of 4 sums (re, im, sigma^2, weight) of
 // up to kNoAllocMaxFacet^2 cells, plus the reduced sums: (64 * 4 + 4) * 48^2 doubles, 4.6 MiB.
 // Every GPU on which the library is loaded holds this memory until the process exits.
+//
+// Shared state: besides the scratch array, a call writes two things every other entry point of
+// this library uses too: the __constant__ channel table (set_channels, through a static host
+// staging array) and the gridding kernel's dynamic shared-memory attribute.  A call that overlaps
+// ANY other call of this library on the GPU or on another host thread (data_processing,
+// source_extraction, gridding_visibilities, ...) can change that call's wavenumbers, so callers
+// serialise all calls into the library, not only the no-allocation ones.  The call synchronises
+// the caller's stream (inside set_channels and at its end), so it cannot be captured into a CUDA
+// graph.
 #include <mutex>
 #include <stdio.h>
 #include "rlf_vis.cuh"
@@ -29,7 +38,9 @@ static double* g_noalloc_ptr[kNoAllocMaxDevices];
 
 // Device address of g_noalloc_scratch on the current device.  In host code the symbol itself is
 // a host-side stand-in, so the address is looked up once per device (first call on that device)
-// and cached.
+// and cached for the life of the process.  The cache is not valid across cudaDeviceReset (the
+// module is loaded again in the new context): a caller that resets a device does not call this
+// entry point on it afterwards.
 static int noalloc_scratch(double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference's own code.
 
 Runs oracle/_ref/librlf_ref.so (the reference's hot-path sources compiled against the project's
-GSL-subset shim by `make -C oracle ref`; needs the reference checkout) on seeded small cases and
+GSL-subset shim by `make -C oracle ref REF=<reference checkout>`) on seeded small cases and
 stores inputs and outputs:
 
   golden_small.npz   one small observation (16 antennas, 24 times, 4 channels, 7 galaxies, one too faint

@@ -87,10 +87,34 @@ def test_gridding_and_facet_coords(lib, orc, case):
         n2 = orc.orc_facet_coords(O.dp(u2), O.dp(v2), case.len, F, O.dp(sw2))
         assert n1 == n2 == n
         assert np.array_equal(u1[:n], u2[:n]) and np.array_equal(v1[:n], v2[:n])
-        # average_facets on the un-compacted sums
-        a_vis = np.zeros(nc, np.complex128)
-        a_s2 = np.zeros(nc)
-        lib.average_facets(nc, cptr(a_vis), dptr(a_s2), dptr(np.zeros(nc)))
+
+def test_average_facets(lib, orc):
+    """average_facets (evaluate_uv_grid.c:216-230): compaction of summed facets to the non-empty
+    cells, visibilities times the weight over the variance, variances over the weight squared.
+    Every cell's result is one product and one quotient of the same operands: bit-equal."""
+    rng = np.random.default_rng(5)
+    for F in (4, 10, 34):
+        nc = F * F
+        sw = rng.integers(0, 50, nc).astype(np.float64)
+        sw[rng.random(nc) < 0.3] = 0.0
+        sw[0] = 0.0
+        sw[-1] = 7.0
+        vis = (rng.standard_normal(nc) + 1j * rng.standard_normal(nc)) * 1e5
+        s2 = rng.random(nc) * 1e9 + 1e6
+        v1, s1 = vis.copy(), s2.copy()
+        v2, s2o = vis.copy(), s2.copy()
+        lib.average_facets(nc, cptr(v1), dptr(s1), dptr(sw))
+        orc.orc_average_facets(nc, O.cp(v2), O.dp(s2o), O.dp(sw))
+        n = int(np.count_nonzero(sw))
+        assert np.array_equal(v1[:n], v2[:n])
+        assert np.array_equal(s1[:n], s2o[:n])
+        # cells beyond the compacted ones keep their inputs, as in the reference's in-place loop
+        assert np.array_equal(v1[n:], v2[n:]) and np.array_equal(s1[n:], s2o[n:])
+    # an all-empty facet leaves the arrays unchanged
+    z = np.ones(16, np.complex128)
+    zs = np.ones(16)
+    lib.average_facets(16, cptr(z), dptr(zs), dptr(np.zeros(16)))
+    assert np.all(z == 1) and np.all(zs == 1)
 
 
 def test_model_and_visibility_kernels(lib, orc, case):
@@ -339,7 +363,7 @@ def test_data_processing_keeps_observation(lib, orc):
     A = Case(flag_frac=0.03, n_gal=6)
     B = Case(seed=5, flag_frac=0.05, noise=700.0, n_gal=6)
     opt = _lib.Options()
-    opt.precision, opt.batch, opt.refit, opt.fresh_obs = _lib.RLF_F64, 1, 1, 0
+    opt.precision, opt.batch, opt.refit, opt.reuse_obs = _lib.RLF_F64, 1, 1, 1
     lib.rlf_configure(C.byref(opt))
     lib.rlf_release()
     uu, vv, ww = A.obs.uu.copy(), A.obs.vv.copy(), A.obs.ww.copy()
@@ -380,13 +404,43 @@ def test_data_processing_keeps_observation(lib, orc):
     lib.rlf_release()
 
 
+def test_data_processing_reads_arrays_every_call(lib, orc):
+    """Default mode (reuse_obs = 0): a flag changed in place between two calls, at a position the
+    kept observation's sampled fingerprint does not look at, is seen by the second call, which
+    gives the oracle's result with the new flags (the reference reads its arrays on every call,
+    data_processing.c:82-84)."""
+    A = Case(flag_frac=0.03, n_gal=6)
+    opt = _lib.Options()
+    opt.precision, opt.batch, opt.refit, opt.reuse_obs = _lib.RLF_F64, 1, 1, 0
+    lib.rlf_configure(C.byref(opt))
+    lib.rlf_release()
+    sky_a = oracle_sky_model(orc, A)
+    flag = A.flag.copy()
+    nv = A.obs.n_vis
+    sampled = {(nv - 1) * i // 4096 for i in range(4097)}
+    # unsampled, unflagged visibilities of the first channel: flag a run of them
+    idx = [i for i in range(A.obs.n_rows) if i not in sampled and not flag[i]][:40]
+    assert len(idx) == 40
+    data, skym = A.data.copy(), sky_a.copy()
+    _data_processing(lib, A, data, skym, A.obs.uu, A.obs.vv, A.obs.ww, A.sigma2, flag)
+    flag[idx] = 1
+    A.flag = flag.copy()
+    d_ref, s_ref, bad_ref, bl_ref, _ = oracle_data_processing(orc, A, A.data, sky_a)
+    data, skym = A.data.copy(), sky_a.copy()
+    bad, bl = _data_processing(lib, A, data, skym, A.obs.uu, A.obs.vv, A.obs.ww, A.sigma2, flag)
+    assert bad == bad_ref and np.array_equal(bl[:bad], bl_ref[:bad])
+    assert rel(data, d_ref) < 1e-11
+    assert np.max(np.abs(skym - s_ref)) < 1e-11 * np.max(np.abs(sky_a))
+    lib.rlf_release()
+
+
 def test_data_processing_pinned_buffers(lib, orc):
     """Page-locked host buffers (converted by kernels reading and writing them directly) give the
     same data, sky model and bad list as pageable ones (staged copies)."""
     torch = pytest.importorskip("torch")
     A = Case(flag_frac=0.03, n_gal=6)
     opt = _lib.Options()
-    opt.precision, opt.batch, opt.refit, opt.fresh_obs = _lib.RLF_MIXED, 6, 1, 0
+    opt.precision, opt.batch, opt.refit, opt.reuse_obs = _lib.RLF_MIXED, 6, 1, 1
     lib.rlf_configure(C.byref(opt))
     lib.rlf_release()
     sky_a = oracle_sky_model(orc, A)

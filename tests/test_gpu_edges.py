@@ -1,6 +1,7 @@
 """Edge cases of the device pipeline against the oracle's data_processing: an empty catalogue, a
 single galaxy through a batch, every visibility flagged (empty facets: every fit is bad and nothing
-is removed), a batch larger than the catalogue, and four rounds."""
+is removed), a batch larger than the catalogue, four rounds, and the fit's bounded wait for
+sampling-grid points running out."""
 import dataclasses
 
 import numpy as np
@@ -87,3 +88,28 @@ def test_batch_shapes(orc, batch, rounds):
     pr = dev.process(case.cat, batch=batch, refit=False, rounds=rounds)
     dev.close()
     _check(pr.results, ref, 1e-4)
+
+
+def test_board_wait_runs_out(orc):
+    """The fit's wait for sampling-grid points claimed by other thread blocks is bounded: with a
+    1 us limit (rlf_options.board_wait_us) the owners give up on points still in flight, count
+    them as failed evaluations and set status bit 8, and the launch returns instead of waiting.
+    The GPU stays usable: the next call with the default limit matches the oracle."""
+    case = Case(n_gal=6, fmin=150.0, fmax=200.0, noise=300.0)
+    sky = oracle_sky_model(orc, case)
+    _, _, _, _, ref = oracle_data_processing(orc, case, case.data, sky)
+    dev = _dev(case, sky, _lib.RLF_F64)
+    dev.snapshot()
+    hit = 0
+    for _ in range(3):
+        dev.restore()
+        pr = dev.process(case.cat, batch=1, refit=False, board_wait_us=1)
+        hit += int(np.count_nonzero(pr.results["status"] & 8))
+        if hit:
+            break
+    assert hit > 0
+    dev.restore()
+    pr = dev.process(case.cat, batch=1, refit=False)
+    dev.close()
+    assert not np.any(pr.results["status"] & 8)
+    _check(pr.results, ref, 1e-7)

@@ -63,9 +63,12 @@ def test_pipeline_modes(orc, case, sky):
     mixed      FP32 visibility passes, FP64 fit: the FP32 facet error is a smooth perturbation of
                the likelihood surface, so the fit follows the reference's simplex path and the
                fitted ellipticities stay within 1e-4 (log-likelihood within 1e-6 relative).
-    mixed-fit  FP32 visibility passes and FP32 fit cells: the log-likelihood stays within 1e-6
-               relative, but its rounding noise varies with (e1, e2) and can change nmsimplex2
-               decisions, so e agrees only statistically (checked on the median).
+    mixed-fit  FP32 visibility passes and FP32 fit cells (rlf_options.fit_precision = RLF_MIXED):
+               this mode does NOT meet the required bounds (|dL/L| <= 1e-6, |de| <= 1e-4).  Its
+               log-likelihood is within ~4e-6 relative, and the rounding noise varies with
+               (e1, e2) and changes nmsimplex2 decisions, so e agrees only statistically.  It is
+               not the default and neither the bench nor the drop-in entry points select it; the
+               asserts below pin what it achieves (median |de| < 1e-3, |dL/L| < 1e-5).
     """
     d_ref, s_ref, bad_ref, bl_ref, ref = oracle_data_processing(orc, case, case.data, sky)
     e_ref = np.array([(r[0], r[1]) for r in ref])
@@ -107,5 +110,6 @@ def test_pipeline_modes(orc, case, sky):
     assert nerr == 0
     assert de.max() < 1e-4 and dL.max() < 1e-6
     de, dL, nerr = stats["mixed-fit"]
+    # below the required bounds by design (see the docstring): a statistical check only
     assert nerr <= 1
     assert np.median(de) < 1e-3 and dL.max() < 1e-5
