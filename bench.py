@@ -1,19 +1,27 @@
 """Benchmark: galaxies/s of the shape-measurement hot path on one GB300.
 
-A step is one full pass of the path over the synthetic observation: extraction, fit and
-removal of every galaxy in catalogue order, then the re-fit pass over the bad ones
-(RadioLensfit2.cpp:597-606), starting from the same data and sky model each step.
+Workload (default c4_ska_mid_64ch, the configuration the throughput target is stated on): 197
+antennas (19,306 baselines) x 960 times at 30 s x 64 channels = 1.19e9 visibilities, 50,000
+galaxies at 5-200 uJy with shear g = (0.02, 0.01), seeded synthetic array, catalogue and noise
+(no public dataset exists for this path).
 
-  value : device-resident run (rlf_obs_process) of the batched mixed-precision path
-  e2e   : the same work through the reference-facing C entry point data_processing() with host
-          buffers (two calls: catalogue pass and re-fit pass), H2D/D2H copies inside the timing
-  plain : the one-launch-chain-per-galaxy mixed-precision path (batch 1), per-galaxy |de| of the
-          batched result against it
-  --impl reference : the CPU oracle (restatement of the reference, OpenMP on all host cores) on a
-          bounded sample of the same workload
+A step is one window of consecutive galaxies of the flux-ordered catalogue (default 2,000)
+through the whole path: extraction, fit and removal of every galaxy of the window in catalogue
+order, then the re-fit pass over the window's bad galaxies (RadioLensfit2.cpp:597-606 applied to
+the window).  Steps walk down the catalogue and the data carry every earlier window's removals,
+as one long run does; when the catalogue is exhausted the data are restored and the walk starts
+again.  W warm-up windows, then K timed windows.
 
-Workload (default): 197 antennas (19,306 baselines) x 480 times x 16 channels = 148M
-visibilities, 1,000 galaxies at 10-200 uJy, seeded synthetic data (no public dataset exists).
+  value : device-resident run (rlf_obs_process) of the batched mixed-precision path, CUDA events
+          on the library's stream around each window, inputs (FP32 data and sky model, larger than
+          L2) resident in HBM
+  e2e   : windows through the reference-facing C entry point data_processing() with host
+          complex128 buffers (catalogue pass + re-fit pass per window), copies inside the timing
+  plain : the one-launch-chain-per-galaxy path (batch 1) on a prefix of the catalogue against the
+          batched path on the same prefix from the same data: galaxies/s of both and per-galaxy |de|
+  cpu_baseline : the oracle (the reference's arithmetic, OpenMP on all host cores) on the first
+          galaxies of the same data, both passes, with its fitted e against the GPU's
+  --impl reference : the oracle on a bounded sample of the workload, nothing on the GPU
 """
 from __future__ import annotations
 
@@ -34,25 +42,30 @@ sys.path.insert(0, ROOT)
 
 from radiolensfit2_gb300 import constants as K, synth  # noqa: E402
 
-METRIC = "galaxies/s on 1 GB300 (extract+fit+remove, both passes)"
+METRIC = "galaxies/s on 1 GB300: learned+batched vs plain GPU fit at |Δe|≤1e-3; HBM GB/s"
+DEFAULT_WORKLOAD = "c4_ska_mid_64ch"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1_ska_mid_16ch")
-    ap.add_argument("--galaxies", type=int, default=0)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--galaxies", type=int, default=0, help="catalogue size (0 = the workload's)")
+    ap.add_argument("--window", type=int, default=2000, help="galaxies per step (at most the catalogue)")
     ap.add_argument("--batch", type=int, default=1000)
     ap.add_argument("--rounds", type=int, default=0,
                     help="extraction + fit rounds per batch (0 = library default)")
     ap.add_argument("--fit-precision", default="f64", choices=["f64", "mixed"],
                     help="arithmetic of the fit (visibility passes are always mixed)")
-    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-prefix", type=int, default=400,
+                    help="galaxies of the plain-vs-batched comparison (0 = none)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--cpu-sample-galaxies", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e windows (at most --steps)")
+    ap.add_argument("--cpu-sample-galaxies", type=int, default=-1,
+                    help="oracle galaxies of the CPU baseline (-1 = by workload size, 0 = none)")
     return ap.parse_args()
 
 
@@ -104,6 +117,21 @@ def workload(args):
     return w, obs, cat
 
 
+def window_size(args, n_gal):
+    w = min(max(1, args.window), n_gal)
+    return w + (w % 2) if w < n_gal else w  # keep the opposite-orientation pairs together
+
+
+def windows(n_gal, w, count):
+    """(start, stop, restore_before) of `count` consecutive windows, wrapping at the end."""
+    per = -(-n_gal // w)
+    out = []
+    for k in range(count):
+        j = k % per
+        out.append((j * w, min(n_gal, (j + 1) * w), k > 0 and j == 0))
+    return out
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -112,80 +140,142 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def snr_of(obs, cat):
+    """Signal-to-noise of each galaxy's round model, sqrt(sum over visibilities of |V|^2) / sigma
+    (the sum data_simulation.c:79-98 accumulates), from a radial histogram of the uv coverage: used
+    only for the shear estimator's SNR >= 10 selection (shear.py:58)."""
+    q = obs.uu * obs.uu + obs.vv * obs.vv
+    hist, edges = np.histogram(q, bins=1024)
+    qc = 0.5 * (edges[1:] + edges[:-1])
+    sc = cat.scale * K.ARCS2RAD
+    tot = np.zeros(cat.n)
+    for c in range(obs.n_ch):
+        x = (sc * sc)[:, None] * (obs.wavenumbers[c] ** 2 * qc)[None, :]
+        tot += (cat.flux * obs.spec[c]) ** 2 * ((1.0 + x) ** -3.0 @ hist)
+    return np.sqrt(tot) / obs.sigma
+
+
+def shear_block(cat, res, snr, label):
+    """Recovered shear (the estimator of shear.py:32-145, radiolensfit2_gb300.shear) against the
+    input shear of the field."""
+    from radiolensfit2_gb300 import shear as SH
+    err1 = np.sqrt(np.maximum(res["var_e1"], 0.0))
+    err2 = np.sqrt(np.maximum(res["var_e2"], 0.0))
+    est = SH.estimate_shear(res["e1"], res["e2"], err1, err2, res["oneDimvar"], snr)
+    g1, g2 = cat.g
+    return {"fit": label, "g_true": [g1, g2], "g": [est.g1, est.g2], "g_err": [est.g1_err, est.g2_err],
+            "bias": [est.g1 - g1, est.g2 - g2], "galaxies_used": est.n_used,
+            "within_1sigma": bool(abs(est.g1 - g1) <= est.g1_err and abs(est.g2 - g2) <= est.g2_err)}
+
+
+def cpu_sample_size(args, obs):
+    if args.cpu_sample_galaxies >= 0:
+        return args.cpu_sample_galaxies
+    # about 10-30 s of oracle work on 16 host cores (~1.3 s per galaxy per 1.5e8 visibilities)
+    return max(1, min(16, int(3e9 // max(obs.n_vis, 1))))
+
+
+def oracle_two_passes(O, orc, obs, sub, d, s, gal, sigma2, flag, ro, fmax):
+    """data_processing (oracle) over `sub`: catalogue pass, then the re-fit pass of its bad galaxies;
+    results [(e1, e2, error)] after both passes (bad ones written with e = 0)."""
+    out = (O.OrcFitResult * sub.n)()
+    bl = np.zeros(sub.n, np.uint32)
+    bad = C.c_int(0)
+    sumw = np.zeros(fmax * fmax)
+    tail = (obs.len_lambda, obs.n_rows, obs.n_ch, O.dp(obs.spec), O.dp(obs.wavenumbers), len(ro), O.dp(ro),
+            O.dp(sub.l), O.dp(sub.m), O.dp(sub.flux), O.dp(sub.scale), O.dp(sumw), O.cp(gal), O.cp(s), O.cp(d),
+            O.fp(sigma2), O.bp(flag), O.dp(obs.uu), O.dp(obs.vv), O.dp(obs.ww), 0)
+    orc.orc_data_processing(0, bl.ctypes.data_as(O.PU), sub.n, *tail, out, C.byref(bad))
+    res = np.array([(r.e1, r.e2, r.error) for r in out])
+    nb = bad.value
+    if nb:
+        out2 = (O.OrcFitResult * sub.n)()
+        bad2 = C.c_int(0)
+        orc.orc_data_processing(1, bl.ctypes.data_as(O.PU), nb, *tail, out2, C.byref(bad2))
+        for k in range(nb):
+            r = out2[k]
+            res[int(bl[k])] = (0.0, 0.0, 1) if r.error else (r.e1, r.e2, 0)
+        nb = bad2.value
+    return res, nb
+
+
 def run_reference(args):
-    """CPU baseline: the oracle restatement (reference arithmetic, OpenMP over scalelength nodes and
-    channels as the reference) on a bounded sample of the workload."""
+    """Reference arm: the oracle restatement of the reference's data_processing (its arithmetic and
+    order, OpenMP over scalelength nodes and channels as the reference) on the host cores, on a
+    bounded sample of the workload: the first galaxies of the catalogue, both passes, on data holding
+    those galaxies' models plus noise.  Nothing runs on the GPU."""
     w, obs, cat = workload(args)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
     orc = O.load_oracle()
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    n = max(1, args.cpu_sample_galaxies)
-    # data for the sample: the sample galaxies' models + noise; sky model of the sample
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    n = cpu_sample_size(args, obs) if args.cpu_sample_galaxies < 0 else max(1, args.cpu_sample_galaxies)
+    # each step stays a bounded sample (a few seconds of host work at the largest workload)
+    n = max(1, min(n, int(1.5e9 // max(obs.n_vis, 1)) or 1))
     sub = cat.subset(range(n))
-    rng = np.random.default_rng(synth.NOISE_SEED)
-    data = np.zeros(obs.n_vis, np.complex128)
     sky = np.zeros(obs.n_vis, np.complex128)
     gal = np.zeros(obs.n_vis, np.complex128)
     orc.orc_sky_model(O.dp(obs.wavenumbers), O.dp(obs.spec), obs.n_ch, sub.n, O.dp(sub.flux), O.dp(sub.scale),
                       O.dp(sub.l), O.dp(sub.m), obs.n_rows, O.dp(obs.uu), O.dp(obs.vv), O.dp(obs.ww), O.cp(gal),
                       O.cp(sky), 0)
-    data[:] = sky
-    data += obs.sigma * (rng.standard_normal(obs.n_vis) + 1j * rng.standard_normal(obs.n_vis))
+    # noise: a seeded block of up to 2^24 complex samples tiled over the visibilities (a timing sample)
+    rng = np.random.default_rng(synth.NOISE_SEED)
+    blk = min(obs.n_vis, 1 << 24)
+    noise = obs.sigma * (rng.standard_normal(blk) + 1j * rng.standard_normal(blk))
+    data = sky.copy()
+    for i0 in range(0, obs.n_vis, blk):
+        i1 = min(obs.n_vis, i0 + blk)
+        data[i0:i1] += noise[:i1 - i0]
+    del noise
     sigma2 = np.full(obs.n_vis, np.float32(obs.sigma2), np.float32)
     flag = np.zeros(obs.n_vis, np.uint8)
     ro = np.array(K.ro_grid())
     fmax = K.facet_size(K.RMAX, obs.len_lambda)
+    d = np.empty_like(data)
+    s = np.empty_like(sky)
     times = []
     steps = max(1, args.steps)
-    for it in range(max(0, min(args.warmup, 1)) + steps):
-        d, s = data.copy(), sky.copy()
-        out = (O.OrcFitResult * sub.n)()
-        bl = np.zeros(sub.n, np.uint32)
-        bad = C.c_int(0)
-        sumw = np.zeros(fmax * fmax)
+    warm = max(0, min(args.warmup, 1))
+    for it in range(warm + steps):
+        np.copyto(d, data)
+        np.copyto(s, sky)
         t0 = time.perf_counter()
-        orc.orc_data_processing(0, bl.ctypes.data_as(O.PU), sub.n, obs.len_lambda, obs.n_rows, obs.n_ch,
-                                O.dp(obs.spec), O.dp(obs.wavenumbers), len(ro), O.dp(ro), O.dp(sub.l), O.dp(sub.m),
-                                O.dp(sub.flux), O.dp(sub.scale), O.dp(sumw), O.cp(gal), O.cp(s), O.cp(d),
-                                O.fp(sigma2), O.bp(flag), O.dp(obs.uu), O.dp(obs.vv), O.dp(obs.ww), 0, out,
-                                C.byref(bad))
+        oracle_two_passes(O, orc, obs, sub, d, s, gal, sigma2, flag, ro, fmax)
         dt = time.perf_counter() - t0
-        if it >= min(args.warmup, 1):
+        if it >= warm:
             times.append(dt)
     t = float(np.mean(times))
     value = sub.n / t
+    sample = (f"first {sub.n} galaxies of {w['n_gal']} (flux {sub.flux.min():.0f}-{sub.flux.max():.0f} uJy) on the "
+              f"full {obs.n_vis}-visibility arrays holding those galaxies plus noise, both passes")
     line = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": args.gpus, "steps": steps,
-            "warmup": min(args.warmup, 1), "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded array, catalogue and noise)",
             "config": {"workload": args.workload, "n_vis": obs.n_vis, "galaxies": w["n_gal"],
                        "sample_galaxies": sub.n},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "galaxies/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
-                             "kind": "port", "sample": f"{sub.n} galaxies of {w['n_gal']} on the full "
-                                                       f"{obs.n_vis}-visibility array, first pass"},
+                             "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "galaxies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    print(json.dumps(line), flush=True)
 
 
-def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec):
+def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, steps, fit_prec):
     """Galaxies/s through the reference-facing entry point data_processing() with pinned host
-    buffers: catalogue pass + re-fit pass (RadioLensfit2.cpp:597-606), copies inside the timing.
-    The library keeps the observation (uvw, variances, flags, facet tables) between calls that
-    pass the same arrays, as the reference driver's do; visibilities and sky model cross the
-    boundary on every call.  Bytes per step are the library's own copy counters; cold_ms is the
-    first call pair, which builds the observation."""
+    complex128 buffers, one window per step: catalogue pass + re-fit pass of the window (two calls),
+    copies inside the timing.  rlf_options.reuse_obs keeps uvw, variances, flags and the facet tables
+    on the device between calls (the arrays are the same); visibilities and sky model cross the
+    boundary on every call.  One warm-up window (it builds the observation), then `steps` windows.
+    Bytes per step are the library's own copy counters."""
     import torch
     from radiolensfit2_gb300 import _lib
     from radiolensfit2_gb300.abi import LikelihoodParams, dptr, fptr, cptr, bptr
     opt = _lib.Options()
     opt.precision, opt.batch, opt.refit, opt.fit_precision = _lib.RLF_MIXED, B, 1, fit_prec
-    opt.reuse_obs = 1  # the two passes pass the same uvw, variances and flags
+    opt.reuse_obs = 1  # the two passes and the windows pass the same uvw, variances and flags
     lib.rlf_configure(C.byref(opt))
     n_vis = obs.n_vis
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
-    d0, s0 = pin(data_h), pin(sky_h)
     d, s = pin(data_h), pin(sky_h)
     sigma2 = pin(np.full(n_vis, np.float32(obs.sigma2), np.float32))
     flag = pin(np.zeros(n_vis, np.uint8))
@@ -198,17 +288,18 @@ def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec
     p.spec, p.wavenumbers = dptr(obs.spec), dptr(obs.wavenumbers)
     fmax = K.facet_size(K.RMAX, obs.len_lambda)
     sumw = np.zeros(fmax * fmax)
-    snr = np.zeros(cat.n)
-    flux, scale, l, m, e1, e2 = (np.ascontiguousarray(x) for x in (cat.flux, cat.scale, cat.l, cat.m, cat.e1, cat.e2))
-    times, h2d, d2h = [], [], []
+    times, h2d, d2h, ngal = [], [], [], []
     cold_ms = None
-    nbad_final = 0
     c_in, c_out = C.c_ulonglong(0), C.c_ulonglong(0)
     lib.rlf_release()
-    for it in range(warmup + steps):
-        np.copyto(d, d0)
-        np.copyto(s, s0)
-        bad_list = np.zeros(cat.n, np.uint32)
+    for it, (a, b, restore) in enumerate(windows(cat.n, win, 1 + steps)):
+        if restore:
+            np.copyto(d, data_h)
+            np.copyto(s, sky_h)
+        l, m, flux, scale, e1, e2 = (np.ascontiguousarray(x[a:b]) for x in
+                                    (cat.l, cat.m, cat.flux, cat.scale, cat.e1, cat.e2))
+        snr = np.zeros(b - a)
+        bad_list = np.zeros(b - a, np.uint32)
         bad = C.c_int(0)
         ft = C.c_double(0)
         args = [C.byref(p), dptr(l), dptr(m), dptr(flux), dptr(scale), dptr(e1), dptr(e2), dptr(snr), dptr(sumw),
@@ -217,114 +308,105 @@ def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps, warmup, fit_prec
         lib.rlf_transfer_bytes(C.byref(c_in), C.byref(c_out))
         b_in, b_out = c_in.value, c_out.value
         t0 = time.perf_counter()
-        lib.data_processing(False, bad_list.ctypes.data_as(_lib.PU), cat.n, obs.len_lambda, obs.n_rows, None, *args)
+        lib.data_processing(False, bad_list.ctypes.data_as(_lib.PU), b - a, obs.len_lambda, obs.n_rows, None, *args)
         nb = bad.value
         lib.data_processing(True, bad_list.ctypes.data_as(_lib.PU), nb, obs.len_lambda, obs.n_rows, None, *args)
         dt = time.perf_counter() - t0
         lib.rlf_transfer_bytes(C.byref(c_in), C.byref(c_out))
-        nbad_final = bad.value
         if it == 0:
             cold_ms = dt * 1e3
-        if it >= warmup:
+        else:
             times.append(dt)
+            ngal.append(b - a)
             h2d.append(c_in.value - b_in)
             d2h.append(c_out.value - b_out)
     lib.rlf_release()
-    t = float(np.mean(times))
-    return {"value": cat.n / t, "unit": "galaxies/s", "h2d_bytes_per_step": int(np.mean(h2d)),
-            "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": t * 1e3, "cold_ms": cold_ms,
-            "path": "data_processing() x2 (catalogue + re-fit pass), host complex128 buffers, mixed, batch %d" % B,
-            "bad_after_refit": nbad_final}
+    t = float(np.sum(times))
+    return {"value": float(np.sum(ngal)) / t, "unit": "galaxies/s", "h2d_bytes_per_step": int(np.mean(h2d)),
+            "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": t / len(times) * 1e3, "steps": len(times),
+            "warmup": 1, "cold_ms": cold_ms,
+            "path": ("data_processing() x2 per window (catalogue + re-fit pass), pinned host complex128 buffers, "
+                     "mixed, batch %d, windows 2..%d of %d galaxies" % (B, steps + 1, win))}
 
 
-def cpu_baseline(obs, cat, data_h, sky_h, n_sample):
-    """The oracle (reference arithmetic, OpenMP over all host cores as the reference) on the
-    first n_sample galaxies of the workload: extraction + fit + removal, first pass."""
+def cpu_baseline(obs, cat, data_h, sky_h, n_sample, gpu_first):
+    """The oracle (reference arithmetic, OpenMP over all host cores as the reference) on the first
+    n_sample galaxies of the same data, both passes, run in place on data_h / sky_h; its fitted e
+    against the GPU's for the same galaxies (the first galaxies' results do not depend on the rest
+    of the catalogue)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
     orc = O.load_oracle()
     sub = cat.subset(range(n_sample))
-    d, s = data_h.copy(), sky_h.copy()
     gal = np.zeros(obs.n_vis, np.complex128)
     sigma2 = np.full(obs.n_vis, np.float32(obs.sigma2), np.float32)
     flag = np.zeros(obs.n_vis, np.uint8)
     ro = np.array(K.ro_grid())
     fmax = K.facet_size(K.RMAX, obs.len_lambda)
-    out = (O.OrcFitResult * sub.n)()
-    bl = np.zeros(sub.n, np.uint32)
-    bad = C.c_int(0)
     t0 = time.perf_counter()
-    orc.orc_data_processing(0, bl.ctypes.data_as(O.PU), sub.n, obs.len_lambda, obs.n_rows, obs.n_ch, O.dp(obs.spec),
-                            O.dp(obs.wavenumbers), len(ro), O.dp(ro), O.dp(sub.l), O.dp(sub.m), O.dp(sub.flux),
-                            O.dp(sub.scale), O.dp(np.zeros(fmax * fmax)), O.cp(gal), O.cp(s), O.cp(d), O.fp(sigma2),
-                            O.bp(flag), O.dp(obs.uu), O.dp(obs.vv), O.dp(obs.ww), 0, out, C.byref(bad))
+    res, nb = oracle_two_passes(O, orc, obs, sub, data_h, sky_h, gal, sigma2, flag, ro, fmax)
     dt = time.perf_counter() - t0
-    res = np.array([(r.e1, r.e2, r.error) for r in out])
-    return sub.n / dt, dt, res
+    g = gpu_first[:n_sample]
+    ok = (res[:, 2] == 0) & (g["error"] == 0)
+    de = np.maximum(np.abs(res[ok, 0] - g["e1"][ok]), np.abs(res[ok, 1] - g["e2"][ok]))
+    parity = {"galaxies": int(n_sample), "good_in_both": int(ok.sum()),
+              "error_flags_equal": bool(np.array_equal(res[:, 2].astype(int), g["error"])),
+              "max_abs_de": float(de.max()) if de.size else None,
+              "frac_le_1e-4": float(np.mean(de <= 1e-4)) if de.size else None,
+              "gpu_path": "batched mixed-precision, both passes, same data"}
+    return sub.n / dt, dt, parity
 
 
-# DRAM bytes of one k_extract_seq launch per row of the observation, from the ncu capture of
-# profiles/k_extract_seq_mid_128ant_16ch.md (dram__bytes_read.sum + dram__bytes_write.sum =
-# 335.9 MB + 7.7 MB over 975,360 rows); a launch reads data, sky model, the row table, the
-# work-item list and the run descriptors once per row, so the traffic of a launch grows with the
-# rows
-EXTRACT_DRAM_BYTES_PER_ROW = (335.856384e6 + 7.741184e6) / 975360
+# DRAM bytes of one k_extract_seq launch per algorithmic byte, from the ncu capture of
+# profiles/k_extract_seq_mid_128ant_16ch.md: dram__bytes_read.sum + dram__bytes_write.sum =
+# 335.9 MB + 7.7 MB against 16 B per visibility (975,360 rows x 16 channels) + 32 B per row.  A launch
+# reads data and sky model once per visibility and the row table, work items and run descriptors once
+# per (row, 16-channel chunk), so its traffic grows with those units.
+EXTRACT_DRAM_PER_ALG_BYTE = (335.856384e6 + 7.741184e6) / (975360 * 16 * 16 + 975360 * 32)
+EXTRACT_TRAFFIC_SOURCE = ("ncu DRAM bytes of one k_extract_seq launch on mid_128ant_16ch "
+                          "(profiles/k_extract_seq_mid_128ant_16ch.md) per algorithmic byte, times this "
+                          "launch's algorithmic bytes")
 
 
-def roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak):
-    """Roofline of the dominant stage of a step.
+def roofline_of(obs, st, steps, hbm_peak, peak_kind, fp32_peak):
+    """Roofline of the dominant kernel, k_extract_seq (the sequential batch extraction).
 
-    Algorithmic bytes of the streaming passes: a sequential batch extraction pass reads data and
-    sky model (2 x 8 B FP32 complex) per visibility and the 32 B row table entry per row; a removal
-    pass reads and writes data and sky model (32 B) per visibility and reads the row table.
-    Algorithmic FP32 work per galaxy-visibility pair (FMA = 2): extraction 15 FLOP in a first round
-    (Horner step 8, round-model profile 5, spectral sum 2) and 33 FLOP in a correction round (phase
-    recurrence 6, rotation 8, two profiles 10, model difference and residual update 9); removal
-    40 FLOP.  The fit reads only facets (kilobytes) and has no streaming roofline."""
+    Algorithmic bytes per launch: data and sky model (2 x 8 B FP32 complex) per visibility and the
+    32 B row-table entry per row.  Algorithmic FP32 work per galaxy-visibility pair (FMA = 2): 15
+    FLOP in a first round (Horner step 8, round-model profile 5, spectral sum 2) and 33 FLOP in a
+    correction round (phase recurrence 6, rotation 8, two profiles 10, model difference and residual
+    update 9).  Time: the kernel's own launches, CUDA events on the launching stream
+    (RLF_STAT_EXTRACT_SEQ_US), summed over the timed steps."""
     n_vis, n_rows = float(obs.n_vis), float(obs.n_rows)
-    good = int(np.sum(batched["error"] == 0))
-    st = res.stats  # passes of the last step (both passes), counted by the library
-    dominant = max(stage_ms, key=stage_ms.get)
-    t = stage_ms[dominant] * 1e-3
-    if dominant == "extract":
-        nbytes = (st["extract_passes"] + st["extract_single"]) * (16.0 * n_vis + 32.0 * n_rows)
-        first = st["extract_gal_first"]
-        flops = n_vis * (15.0 * first + 33.0 * (st["extract_gal"] - first))
-    elif dominant == "remove":
-        nbytes = (st["remove_batches"] + st["remove_single"]) * (32.0 * n_vis + 32.0 * n_rows)
-        flops = 40.0 * n_vis * good
-    else:
-        nbytes, flops = None, None
-    kernel = {"remove": "k_remove_batch", "extract": "k_extract_seq", "fit": "k_fit"}[dominant]
-    r = {"kernel": kernel, "bound": "hbm", "unit": "GB/s",
-         "achieved": nbytes / t / 1e9 if nbytes else None, "peak": hbm_peak,
+    launches = st["extract_passes"]
+    t = st["extract_seq_us"] * 1e-6
+    per_launch = 16.0 * n_vis + 32.0 * n_rows
+    first = st["extract_gal_first"]
+    flops = n_vis * (15.0 * first + 33.0 * (st["extract_gal"] - first))
+    achieved = per_launch * launches / t / 1e9 if t > 0 and launches else None
+    r = {"kernel": "k_extract_seq", "bound": "hbm", "unit": "GB/s", "achieved": achieved, "peak": hbm_peak,
          "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-         "traffic": None, "time_ms_per_step": stage_ms[dominant], "passes": st}
-    r["frac"] = r["achieved"] / hbm_peak if r["achieved"] else None
-    if dominant == "extract":
-        # per launch, from the mid-size capture scaled by rows (this workload is too large for a
-        # multi-pass capture); algorithmic bytes per launch beside it
-        r["traffic"] = EXTRACT_DRAM_BYTES_PER_ROW * n_rows
-        r["traffic_algorithmic"] = 16.0 * n_vis + 32.0 * n_rows
-        r["traffic_source"] = ("ncu DRAM bytes of one k_extract_seq launch on mid_128ant_16ch "
-                               "(profiles/k_extract_seq_mid_128ant_16ch.md), scaled by rows")
-    if flops:
+         "frac": achieved / hbm_peak if achieved else None,
+         "traffic": EXTRACT_DRAM_PER_ALG_BYTE * per_launch, "traffic_algorithmic": per_launch,
+         "traffic_source": EXTRACT_TRAFFIC_SOURCE, "launches": int(launches),
+         "avg_launch_ms": t / launches * 1e3 if launches else None, "kernel_ms_per_step": t * 1e3 / steps}
+    if t > 0:
         # the batched passes are FP32-pipe bound (profiles, phase recurrences), not HBM bound
         r["compute"] = {"bound": "fp32", "unit": "TFLOP/s", "achieved": flops / t / 1e12,
                         "peak": fp32_peak / 1e3, "peak_kind": "measured FP32 FMA probe kernel",
                         "frac": flops / t / 1e12 / (fp32_peak / 1e3)}
     return r
 
+
 def main():
     args = parse()
     if args.impl == "reference":
-        rank = int(os.environ.get("RANK", "0"))
-        if rank == 0:
+        if int(os.environ.get("RANK", "0")) == 0:
             run_reference(args)
         return
     import torch
     from radiolensfit2_gb300 import _lib
-    from radiolensfit2_gb300.pipeline import DeviceObservation
+    from radiolensfit2_gb300.pipeline import DeviceObservation, RESULT_DTYPE
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -333,20 +415,35 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl")
     lib = _lib.load()
+    t_setup = time.perf_counter()
     w, obs, cat = workload(args)
     dev = DeviceObservation(obs, precision=_lib.RLF_MIXED)
     dev.simulate(cat, obs.sigma, seed=synth.NOISE_SEED + rank)
     dev.sky_model(cat)
     dev.snapshot()
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
     B = max(1, args.batch)
     fit_prec = _lib.RLF_F64 if args.fit_precision == "f64" else _lib.RLF_MIXED
+    win = window_size(args, cat.n)
+    plan = windows(cat.n, win, args.warmup + args.steps)
+    # the first walk over the catalogue: its results (shear) and device time (whole-job throughput)
+    full = np.zeros(cat.n, RESULT_DTYPE)
+    seen = np.zeros(cat.n, bool)
+    walk = {"ms": 0.0}
 
-    def step():
-        dev.restore()
-        return dev.process(cat, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
+    def step(a, b, restore):
+        if restore:
+            dev.restore()
+        r = dev.process(cat.subset(range(a, b)), batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
+        if not seen[a:b].any():
+            full[a:b] = r.results
+            seen[a:b] = True
+            walk["ms"] += r.ms[0]
+        return r
 
-    for _ in range(args.warmup):
-        step()
+    for (a, b, restore) in plan[:args.warmup]:
+        step(a, b, restore)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -355,10 +452,14 @@ def main():
     l0 = lib.rlf_launch_count()
     t0 = time.perf_counter()
     stage = np.zeros(4)  # device time from CUDA events on the library's stream: total, extract, fit, remove
-    res = None
-    for _ in range(args.steps):
-        res = step()
-        stage += np.array(res.ms)
+    stats = None
+    n_timed = n_bad = 0
+    for (a, b, restore) in plan[args.warmup:]:
+        r = step(a, b, restore)
+        stage += np.array(r.ms)
+        n_timed += b - a
+        n_bad += r.n_bad
+        stats = dict(r.stats) if stats is None else {k: stats[k] + r.stats[k] for k in stats}
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -370,55 +471,82 @@ def main():
         t = torch.tensor([elapsed], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed = float(t.item())
-    value = cat.n * args.steps * world / elapsed
-    batched = res.results
+    value = n_timed * world / elapsed
     stage_ms = {"extract": stage[1] / args.steps, "fit": stage[2] / args.steps, "remove": stage[3] / args.steps}
     peaks, peak_kind = measured_peaks()
     hbm_peak = float(peaks.get("hbm_gbs") or 6800.0)
     fp32_peak = float(lib.rlf_fp32_peak_gflops())  # measured here by an FMA probe kernel, GFLOP/s
-    roofline = roofline_of(obs, cat, batched, res, B, stage_ms, hbm_peak, peak_kind, fp32_peak)
     out = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "fp32 visibilities (FP64 phase argument), %s fit" % args.fit_precision,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp32 visibilities (FP64 phase argument), %s fit" % args.fit_precision,
            "data": "synthetic (seeded array, catalogue and noise)",
            "config": {"workload": args.workload, "antennas": w["n_ant"], "rows": obs.n_rows, "channels": obs.n_ch,
-                      "n_vis": obs.n_vis, "galaxies": cat.n, "batch": B, "precision": "mixed",
-                      "fit_precision": args.fit_precision,
+                      "n_vis": obs.n_vis, "galaxies": cat.n, "window": win, "timed_galaxies": n_timed,
+                      "batch": B, "precision": "mixed", "fit_precision": args.fit_precision,
+                      "proposal": "none (simplex start (0, 0), step 0.1)",
                       "l2_policy": "inputs larger than L2 (data + sky model %.1f GB)" % (16 * obs.n_vis / 1e9),
-                      "timing": "CUDA events on the library stream around both passes of each step"},
-           "wall_ms_per_step": wall / args.steps * 1e3,
-           "stage_ms_per_step": stage_ms, "bad_galaxies": int(res.n_bad), "gpu_launches": launches,
-           "roofline": roofline, "clocks": ck, "peaks": peak_kind}
-    if rank == 0 and not args.no_plain:
+                      "timing": "CUDA events on the library stream around both passes of each window"},
+           "setup_s": setup_s, "wall_ms_per_step": wall / args.steps * 1e3, "stage_ms_per_step": stage_ms,
+           "bad_galaxies_timed": int(n_bad), "gpu_launches": launches, "work": stats,
+           "roofline": roofline_of(obs, stats, args.steps, hbm_peak, peak_kind, fp32_peak),
+           "clocks": ck, "peaks": peak_kind}
+    snr = None
+    if seen.all():
+        out["catalogue_walk"] = {"galaxies": cat.n, "device_s": walk["ms"] * 1e-3,
+                                 "galaxies_per_s": cat.n / (walk["ms"] * 1e-3),
+                                 "note": "the W+K windows covered the catalogue: whole-job throughput"}
+        if rank == 0:
+            snr = snr_of(obs, cat)
+            out["shear"] = [shear_block(cat, full, snr, "batched, whole catalogue")]
+    gpu_first = None
+    if rank == 0 and args.plain_prefix > 0:
+        P = min(args.plain_prefix, cat.n)
+        pre = cat.subset(range(P))
         dev.restore()
-        t1 = time.perf_counter()
-        pr = dev.process(cat, batch=1, refit=True, fit_precision=fit_prec)
-        tp = time.perf_counter() - t1
-        pl = pr.results
-        ok = (pl["error"] == 0) & (batched["error"] == 0)
-        de = np.maximum(np.abs(pl["e1"][ok] - batched["e1"][ok]), np.abs(pl["e2"][ok] - batched["e2"][ok]))
-        out["plain_gpu"] = {"value": cat.n / tp, "unit": "galaxies/s", "ms": tp * 1e3,
-                            "stage_ms": dict(zip(("extract", "fit", "remove"), pr.ms[1:])),
-                            "speedup_batched_vs_plain": value / (cat.n / tp),
+        rb = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
+        dev.restore()
+        rp = dev.process(pre, batch=1, refit=True, fit_precision=fit_prec)
+        bt, pl = rb.results, rp.results
+        gpu_first = bt
+        ok = (pl["error"] == 0) & (bt["error"] == 0)
+        de = np.maximum(np.abs(pl["e1"][ok] - bt["e1"][ok]), np.abs(pl["e2"][ok] - bt["e2"][ok]))
+        plain_rate = P / (rp.ms[0] * 1e-3)
+        out["plain_gpu"] = {"value": plain_rate, "unit": "galaxies/s", "prefix_galaxies": P, "ms": rp.ms[0],
+                            "stage_ms": dict(zip(("extract", "fit", "remove"), rp.ms[1:])),
+                            "batched_on_prefix": {"value": P / (rb.ms[0] * 1e-3), "ms": rb.ms[0]},
+                            "speedup_batched_vs_plain_same_prefix": rp.ms[0] / rb.ms[0],
+                            "speedup_value_vs_plain": value / plain_rate,
                             "abs_de_vs_batched": {"max": float(de.max()) if de.size else None,
                                                   "median": float(np.median(de)) if de.size else None,
                                                   "frac_le_1e-3": float(np.mean(de <= 1e-3)) if de.size else None,
-                                                  "n": int(de.size)}}
+                                                  "frac_le_1e-4": float(np.mean(de <= 1e-4)) if de.size else None,
+                                                  "n": int(de.size)},
+                            "error_flags_differ": int(np.sum(pl["error"] != bt["error"]))}
+        if snr is not None:
+            out["shear"].append(shear_block(pre, bt, snr[:P], "batched, prefix"))
+            out["shear"].append(shear_block(pre, pl, snr[:P], "plain, prefix"))
+    n_cpu = cpu_sample_size(args, obs) if gpu_first is not None else 0
     data_h = sky_h = None
-    if rank == 0 and (not args.no_e2e or args.cpu_sample_galaxies > 0):
+    if rank == 0 and (not args.no_e2e or n_cpu > 0):
         dev.restore()
         data_h, sky_h = dev.get_vis()
+    dev.close()
     if rank == 0 and not args.no_e2e:
-        out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, steps=1, warmup=1, fit_prec=fit_prec)
-    if rank == 0 and args.cpu_sample_galaxies > 0:
-        v, dt, _ = cpu_baseline(obs, cat, data_h, sky_h, args.cpu_sample_galaxies)
-        out["cpu_baseline"] = {"value": v, "unit": "galaxies/s", "cores": os.cpu_count(), "kind": "port",
-                               "sample": f"first {args.cpu_sample_galaxies} galaxies of {cat.n}, full "
-                                         f"{obs.n_vis}-visibility arrays, extraction+fit+removal, first pass "
+        out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, max(1, min(args.steps, args.e2e_steps)),
+                                         fit_prec)
+    if rank == 0 and n_cpu > 0:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        n_cpu = min(n_cpu, len(gpu_first))
+        v, dt, parity = cpu_baseline(obs, cat, data_h, sky_h, n_cpu, gpu_first)
+        out["cpu_baseline"] = {"value": v, "unit": "galaxies/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                               "kind": "port",
+                               "sample": f"first {n_cpu} galaxies of {cat.n} (the brightest), full "
+                                         f"{obs.n_vis}-visibility arrays, extraction+fit+removal, both passes "
                                          f"({dt:.1f} s)"}
+        out["parity"] = {"vs_cpu_oracle": parity}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    dev.close()
 
 
 if __name__ == "__main__":

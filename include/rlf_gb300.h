@@ -160,7 +160,9 @@ int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
  *                                 differences removed),
  * stats[RLF_STAT_SKIPPED_GAL]     galaxy rounds not run because they could not change: the galaxies
  *                                 of a sub-batch up to the first good fit of the round before, and
- *                                 every later round of a sub-batch without good fits. */
+ *                                 every later round of a sub-batch without good fits,
+ * stats[RLF_STAT_EXTRACT_SEQ_US]  device time of the sequential batch extraction kernel's launches
+ *                                 (RLF_STAT_EXTRACT_PASSES of them), microseconds, CUDA events. */
 enum {
   RLF_STAT_EXTRACT_PASSES = 0,
   RLF_STAT_EXTRACT_SINGLE = 1,
@@ -171,7 +173,8 @@ enum {
   RLF_STAT_CHANGED = 6,
   RLF_STAT_EXTRACT_GAL_FIRST = 7,
   RLF_STAT_SKIPPED_GAL = 8,
-  RLF_NSTATS = 9
+  RLF_STAT_EXTRACT_SEQ_US = 9,
+  RLF_NSTATS = 10
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
 

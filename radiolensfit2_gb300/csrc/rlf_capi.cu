@@ -284,7 +284,9 @@ static std::vector<GalaxyParams> make_gals(int n, const double* flux, const doub
 }
 
 // ------------------------------------------------------------------ pipeline
-// CUDA-event intervals labelled extract / fit / remove, summed per label
+enum { kPhaseExtract = 0, kPhaseFit = 1, kPhaseRemove = 2, kPhaseExtractSeq = 3 };
+// CUDA-event intervals labelled extract / fit / remove (and the k_extract_seq launches within the
+// extraction), summed per label
 struct PhaseTimer {
   std::vector<cudaEvent_t> ev;
   std::vector<int> label;  // label of the interval that ends at ev[i]
@@ -296,16 +298,22 @@ struct PhaseTimer {
     RLF_CUDA(cudaEventRecord(e, st));
     return 0;
   }
-  void sum(double* ms3) const {
+  // ms3[0..2]: extract (the k_extract_seq launches included), fit, remove; seq_ms: the
+  // k_extract_seq launches alone
+  void sum(double* ms3, double* seq_ms = nullptr) const {
     for (size_t i = 1; i < ev.size(); ++i) {
       float x = 0;
       cudaEventElapsedTime(&x, ev[i - 1], ev[i]);
-      if (label[i] >= 0 && label[i] < 3) ms3[label[i]] += x;
+      if (label[i] == kPhaseExtractSeq) {
+        ms3[kPhaseExtract] += x;
+        if (seq_ms) *seq_ms += x;
+      } else if (label[i] >= 0 && label[i] < 3) {
+        ms3[label[i]] += x;
+      }
     }
   }
   ~PhaseTimer() { for (auto e : ev) cudaEventDestroy(e); }
 };
-enum { kPhaseExtract = 0, kPhaseFit = 1, kPhaseRemove = 2 };
 
 // galaxies whose fit differs between two rounds (ellipticity by more than tol, or the error flag)
 __global__ void k_count_changed(int n, const FitOut* a, const FitOut* b, double tol, unsigned long long* count) {
@@ -569,8 +577,10 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         ob->stats[RLF_STAT_EXTRACT_PASSES] += 1;
         ob->stats[RLF_STAT_EXTRACT_GAL] += bk;
         if (rd == 0) ob->stats[RLF_STAT_EXTRACT_GAL_FIRST] += bk;
+        RLF_OK(pt.mark(kPhaseExtract, st));
         RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sr, opt.gaussian, seq_ctas,
                                   ob->bpartial.p, st));
+        RLF_OK(pt.mark(kPhaseExtractSeq, st));
         RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + bj, dsw.p + bj, ob->len, fq, st));
       } else {
         const int i = b0;
@@ -667,7 +677,11 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   if (dchanged.p) RLF_CUDA(copy_async(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   ob->stats[RLF_STAT_CHANGED] += (long long)changed;
-  if (ms3) pt.sum(ms3);
+  if (ms3) {
+    double seq_ms = 0;
+    pt.sum(ms3, &seq_ms);
+    ob->stats[RLF_STAT_EXTRACT_SEQ_US] += (long long)(seq_ms * 1000.0 + 0.5);
+  }
   return 0;
 }
 

@@ -142,7 +142,8 @@ class DeviceObservation:
         ms = (C.c_double * 4)()
         self.lib.rlf_obs_last_timing(self.h, ms)
         names = ("extract_passes", "extract_single", "remove_batches", "remove_single", "fitted",
-                 "extract_gal", "changed", "extract_gal_first", "skipped_gal")  # RLF_NSTATS entries
+                 "extract_gal", "changed", "extract_gal_first", "skipped_gal",
+                 "extract_seq_us")  # RLF_NSTATS entries
         sv = (C.c_longlong * len(names))()
         self.lib.rlf_obs_last_stats(self.h, sv)
         stats = dict(zip(names, (int(x) for x in sv)))
