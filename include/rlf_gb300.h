@@ -55,6 +55,9 @@ typedef struct {
   int board_wait_us; /* the fit's limit, in microseconds, on a galaxy's wait for sampling-grid points
                         that other thread blocks claimed (0 = default 2 s); a point not delivered in
                         time counts as a failed evaluation and sets status bit 8 */
+  int proposal;      /* 1: start each galaxy's simplex at the learned proposal (rlf_proposal_set_params)
+                        instead of (0, 0) with step 0.1; ignored when `start` is given or no network is
+                        loaded */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -177,6 +180,41 @@ enum {
   RLF_NSTATS = 10
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
+
+/* -------- learned proposal of the simplex start --------
+ * No counterpart in the reference (whose simplex starts at (0, 0) with step 0.1,
+ * galaxy_fitting.c:59-65).  A convolutional network (4 convolutions 3x3 stride 2 of 32 channels on
+ * bf16 tensor cores, FP32 accumulation, a dense head) reads a 64 x 64 x 4 resampling of a galaxy's
+ * facet (visibility / flux re and im, cell mask, cell SNR) and proposes (e1, e2, ln r, ln sigma);
+ * the fit starts at (e1, e2) with step 2 sigma in [0.02, 0.1] and stays the judge.  Parameters:
+ * rlf_cnn_param_count() floats, per convolution W[32][9 cin] (k = (3 ky + kx) cin + ci) and b[32],
+ * then the head's W[4][512] (feature (4 y + x) 32 + c) and b[4]. */
+typedef struct rlf_cnn rlf_cnn;
+int rlf_cnn_param_count(void);
+/* a network for training and prediction: batches of up to max_batch images, a device store of
+ * `capacity` images and their targets (e1, e2, ln r) */
+rlf_cnn *rlf_cnn_create(int max_batch, int capacity);
+void rlf_cnn_destroy(rlf_cnn *cnn);
+int rlf_cnn_set_params(rlf_cnn *cnn, const float *params);
+int rlf_cnn_get_params(rlf_cnn *cnn, float *params);
+/* resample n facets (host, rlf_obs_extract's layout facets[g][5][stride], ncoords[g], facet side
+ * facet[g], flux[g]) into the store at [first, first + n) */
+int rlf_cnn_store_facets(rlf_cnn *cnn, int first, int n, const double *facets, int stride,
+                         const int *ncoords, const int *facet, const double *flux, double len);
+int rlf_cnn_set_targets(rlf_cnn *cnn, int first, int n, const float *targets);
+/* the store's images [n][64][64][4] as bf16 bit patterns: write, read */
+int rlf_cnn_set_images(rlf_cnn *cnn, int first, int n, const uint16_t *images);
+int rlf_cnn_read_images(rlf_cnn *cnn, int first, int n, uint16_t *images);
+/* forward and backward of the store images idx[0 .. n): gradient of the mean loss (Gaussian
+ * negative log-likelihood of (e1, e2) with the predicted sigma, plus half the squared error of
+ * ln r) in the parameter layout, the loss, the head's outputs [n][4]; any output may be NULL */
+int rlf_cnn_grads(rlf_cnn *cnn, const int *idx, int n, float *grads, float *loss, float *out);
+/* one Adam step (learning rate lr) on the batch idx[0 .. n); loss may be NULL */
+int rlf_cnn_train_step(rlf_cnn *cnn, const int *idx, int n, float lr, float *loss);
+/* head outputs [n][4] of the store images [first, first + n) */
+int rlf_cnn_predict(rlf_cnn *cnn, int first, int n, float *out);
+/* the network rlf_obs_process / data_processing use with rlf_options.proposal (NULL unloads) */
+int rlf_proposal_set_params(const float *params);
 
 /* -------- gridding without device allocation --------
  * No counterpart in the reference.  The gridding of gridding_visibilities (evaluate_uv_grid.c),

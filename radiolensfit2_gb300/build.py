@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "librlf_gb300.so")
-SOURCES = ["rlf_fit.cu", "rlf_vis.cu", "rlf_batch.cu", "rlf_capi.cu", "rlf_noalloc.cu", "rlf_ms.cu"]
+SOURCES = ["rlf_fit.cu", "rlf_vis.cu", "rlf_batch.cu", "rlf_capi.cu", "rlf_noalloc.cu", "rlf_ms.cu", "rlf_proposal.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

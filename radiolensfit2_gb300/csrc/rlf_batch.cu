@@ -260,7 +260,7 @@ struct __align__(16) SeqGal {
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes) {
-  return align16((size_t)total_cells * sizeof(float2)) + align16((size_t)n_gal * sizeof(SeqGal)) +
+  return align16((size_t)total_cells * kSeqCellBytes) + align16((size_t)n_gal * sizeof(SeqGal)) +
          (size_t)n_sizes * kSeqThreads * (sizeof(uint32_t) + sizeof(uint16_t));
 }
 
@@ -424,6 +424,23 @@ int launch_classify_items(long long total, const SeqBatch& b, int* items, int* i
   return check("k_classify_items");
 }
 
+// Compensated deposit into a facet cell: the FP32 accumulator pair (hi, lo) of the cell's real and
+// imaginary sums, hi at fac[k] and lo at fac[k + lo_off].  The atomic add to hi returns the value it
+// replaced, so the depositing thread knows the sum hi took, RN(old + v), and adds that addition's
+// rounding error (Knuth's TwoSum, exact in FP32) to lo: hi + lo carries the cell's sum to about
+// 2^-48 relative, independent of the order and number of deposits.
+__device__ __forceinline__ void comp_add(float* hi, float* lo, float v) {
+  const float old = atomicAdd(hi, v);
+  const float s = old + v;
+  const float bv = s - old;
+  const float err = (old - (s - bv)) + (v - bv);
+  atomicAdd(lo, err);
+}
+__device__ __forceinline__ void comp_add2(float2* fac, int k, int lo_off, float vr, float vi) {
+  comp_add(&fac[k].x, &fac[k + lo_off].x, vr);
+  comp_add(&fac[k].y, &fac[k + lo_off].y, vi);
+}
+
 // The deposits of a warp's lanes into one galaxy's facet (key: the lane's cell, negative for none).
 // Float atomic adds to shared memory from several lanes of an instruction to one address are
 // retried lane by lane, and with the rows in uv order a warp's lanes mostly fall in one cell of
@@ -431,8 +448,9 @@ int launch_classify_items(long long total, const SeqBatch& b, int* items, int* i
 // are summed exactly as integers (redux.sync) on the fixed-point grid of 2^-24 .. 2^-25 of the
 // group's largest magnitude (a power of two, so the scaling is exact; the sum stays below 2^30)
 // and the group's first lane adds the sum; lanes of further cells, or of groups with non-finite or
-// tiny values, add their own.  All 32 lanes must call it.
-__device__ __forceinline__ void warp_deposit(float2* fac, int key, float vr, float vi, int lane) {
+// tiny values, add their own.  Every addition is compensated (comp_add2, lo_off: the offset of the
+// lo accumulators).  All 32 lanes must call it.
+__device__ __forceinline__ void warp_deposit(float2* fac, int lo_off, int key, float vr, float vi, int lane) {
   const unsigned mag = max(__float_as_uint(fabsf(vr)), __float_as_uint(fabsf(vi)));  // NaN above inf
   unsigned todo = __ballot_sync(0xffffffffu, key >= 0), rest = 0;
 #pragma unroll 1
@@ -447,19 +465,13 @@ __device__ __forceinline__ void warp_deposit(float2* fac, int key, float vr, flo
       const float inv = __uint_as_float((unsigned)(e - 24) << 23);  // 2^(e - 151)
       const int sr = __reduce_add_sync(0xffffffffu, in ? __float2int_rn(vr * sc) : 0);
       const int si = __reduce_add_sync(0xffffffffu, in ? __float2int_rn(vi * sc) : 0);
-      if (lane == src) {
-        atomicAdd(&fac[k].x, (float)sr * inv);
-        atomicAdd(&fac[k].y, (float)si * inv);
-      }
+      if (lane == src) comp_add2(fac, k, lo_off, (float)sr * inv, (float)si * inv);
     } else {
       rest |= m;
     }
     todo &= ~m;
   }
-  if (((todo | rest) >> lane) & 1u) {
-    atomicAdd(&fac[key].x, vr);
-    atomicAdd(&fac[key].y, vi);
-  }
+  if (((todo | rest) >> lane) & 1u) comp_add2(fac, key, lo_off, vr, vi);
 }
 
 // sin(2 pi t) and cos(2 pi t) for a phase in turns: quadrant q = rint(4t), remainder
@@ -643,7 +655,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
         cr = fmaf(rs, g.flux, ar);
         ci = ai;
       }
-      warp_deposit(fac, live ? (int)(d & 0xffffu) : -1, cr, ci, tid & 31);
+      warp_deposit(fac, b.total_cells, live ? (int)(d & 0xffffu) : -1, cr, ci, tid & 31);
     } else {
       // flagged channels, several cells or a short chunk: channel by channel, each run of
       // channels in one cell summed before its deposit
@@ -664,10 +676,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
             const float cr = fmaf(pr[k], zr, fmaf(-pi[k], zi, s0 * spec * g.flux));
             const float ci = fmaf(pr[k], zi, pi[k] * zr);
             if (c != cur) {
-              if (cur != kNoCell) {
-                atomicAdd(&fac[cur].x, ur);
-                atomicAdd(&fac[cur].y, ui);
-              }
+              if (cur != kNoCell) comp_add2(fac, cur, b.total_cells, ur, ui);
               cur = c;
               ur = cr;
               ui = ci;
@@ -688,10 +697,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
           zi = nzi;
         }
       }
-      if (cur != kNoCell) {
-        atomicAdd(&fac[cur].x, ur);
-        atomicAdd(&fac[cur].y, ui);
-      }
+      if (cur != kNoCell) comp_add2(fac, cur, b.total_cells, ur, ui);
     }
   }
 #undef XB
@@ -800,9 +806,9 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
       }
     }
     const int lane = tid & 31;
-    warp_deposit(fac, live ? cell_a : -1, fmaf(rs_a, g.flux, ar), ai, lane);
-    warp_deposit(fac, live && split < kChunk && cell_b != kNoCell ? (int)cell_b : -1, fmaf(rs_b, g.flux, br), bi,
-                 lane);
+    warp_deposit(fac, b.total_cells, live ? cell_a : -1, fmaf(rs_a, g.flux, ar), ai, lane);
+    warp_deposit(fac, b.total_cells, live && split < kChunk && cell_b != kNoCell ? (int)cell_b : -1,
+                 fmaf(rs_b, g.flux, br), bi, lane);
   }
 }
 
@@ -810,15 +816,15 @@ template <int GAUSS, int MODE, bool FIT>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
                                                                 const float2* __restrict__ sky, SeqBatch b,
-                                                                float2* __restrict__ partial) {
+                                                                double2* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* acc = reinterpret_cast<float2*>(smem_raw);
-  SeqGal* sg = reinterpret_cast<SeqGal*>(smem_raw + align16((size_t)b.total_cells * sizeof(float2)));
+  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [total_cells] hi, then [total_cells] lo
+  SeqGal* sg = reinterpret_cast<SeqGal*>(smem_raw + align16((size_t)b.total_cells * kSeqCellBytes));
   uint32_t* dcache = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sg) +
                                                  align16((size_t)b.n_gal * sizeof(SeqGal)));
   uint16_t* d1cache = reinterpret_cast<uint16_t*>(dcache + (size_t)b.n_sizes * kSeqThreads);
   const int tid = threadIdx.x;
-  for (int i = tid; i < b.total_cells; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+  for (int i = tid; i < 2 * b.total_cells; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
   for (int i = tid; i < b.n_gal; i += blockDim.x) {
     SeqGal s;
     const bool has_fit = b.fit != nullptr;
@@ -868,12 +874,15 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     seq_item<GAUSS, true, MODE, FIT>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
-  float2* out = partial + (size_t)blockIdx.x * b.total_cells;
-  for (int i = tid; i < b.total_cells; i += blockDim.x) out[i] = acc[i];
+  double2* out = partial + (size_t)blockIdx.x * b.total_cells;
+  for (int i = tid; i < b.total_cells; i += blockDim.x) {
+    const float2 hi = acc[i], lo = acc[i + b.total_cells];
+    out[i] = make_double2((double)hi.x + (double)lo.x, (double)hi.y + (double)lo.y);
+  }
 }
 
 int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
-                       int gaussian, int ctas, float2* partial, cudaStream_t st) {
+                       int gaussian, int ctas, double2* partial, cudaStream_t st) {
   if (b.n_gal < 1 || b.n_gal > kSeqMaxGal || b.n_sizes < 1 || b.n_sizes > kSeqMaxSizes) {
     fprintf(stderr, "rlf: sequential extraction batch of %d galaxies / %d facet sizes unsupported\n", b.n_gal,
             b.n_sizes);
@@ -908,7 +917,7 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
 
 // one block per galaxy of the batch: FP64 sums of the CTA partials, then the facet finalisation of
 // evaluate_uv_grid.c:196-209 / 113-133 with compaction to the non-empty cells in row-major order
-__global__ void k_finalize_seq(SeqBatch b, int ctas, const float2* __restrict__ partial,
+__global__ void k_finalize_seq(SeqBatch b, int ctas, const double2* __restrict__ partial,
                                const double* const* __restrict__ ss_of, const double* const* __restrict__ sw_of,
                                double len, FacetOut out) {
   const int slot = blockIdx.x;
@@ -932,9 +941,9 @@ __global__ void k_finalize_seq(SeqBatch b, int ctas, const float2* __restrict__ 
       if (w != 0.0) {
         double sre = 0.0, sim = 0.0;
         for (int p = 0; p < ctas; ++p) {
-          const float2 v = partial[(size_t)p * b.total_cells + off + c];
-          sre += (double)v.x;
-          sim += (double)v.y;
+          const double2 v = partial[(size_t)p * b.total_cells + off + c];
+          sre += v.x;
+          sim += v.y;
         }
         const double s2 = ss[c];
         vre = sre * w / s2;
@@ -976,7 +985,7 @@ __global__ void k_finalize_seq(SeqBatch b, int ctas, const float2* __restrict__ 
   if (threadIdx.x == 0) out.ncoords[slot] = base;
 }
 
-int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, const double* const* ss,
+int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
                         const double* const* sw, double len, FacetOut out, cudaStream_t st) {
   k_finalize_seq<<<b.n_gal, 256, 0, st>>>(b, ctas, partial, ss, sw, len, out);
   return check("k_finalize_seq");

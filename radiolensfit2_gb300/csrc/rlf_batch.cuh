@@ -28,13 +28,17 @@ int launch_row_table(int n_rows, const double* uu, const double* vv, const doubl
 #define RLF_SEQ_CTAS_PER_SM 1
 #endif
 #ifndef RLF_SEQ_FACET_KB
-#define RLF_SEQ_FACET_KB 96
+#define RLF_SEQ_FACET_KB 128
 #endif
 constexpr int kSeqThreads = RLF_SEQ_THREADS;      // threads of a sequential extraction CTA
 constexpr int kSeqCtasPerSm = RLF_SEQ_CTAS_PER_SM;  // CTAs per SM (register budget of the kernel)
 constexpr int kSeqMaxSizes = 16;                  // distinct facet sizes in one batch
 constexpr int kSeqMaxGal = 512;                   // galaxies in one batch
 constexpr size_t kSeqFacetBudget = (size_t)RLF_SEQ_FACET_KB * 1024;  // shared facet accumulators of one batch
+// shared memory per facet cell of the sequential extraction: compensated (hi, lo) FP32 pairs of the
+// real and imaginary sums
+constexpr size_t kSeqCellBytes = 2 * sizeof(float2);
+constexpr size_t kSeqMaxSmem = 227 * 1024;  // shared memory of one sequential extraction CTA
 
 // Run descriptor of one 16-channel chunk of one row for one facet size: the cell of the chunk's
 // first channel in bits 0-15, bit 16+k set when channel k of the chunk is flagged, beyond the last
@@ -83,12 +87,12 @@ size_t seq_smem_bytes(int n_gal, int total_cells, int n_sizes);
 // Each class keeps the items' order within a block of 256 items.
 int launch_classify_items(long long total, const SeqBatch& b, int* items, int* items2, int* counters,
                           cudaStream_t st);
-// partial: [ctas][total_cells] float2
+// partial: [ctas][total_cells] double2, each CTA's compensated sums
 int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const float2* sky, const SeqBatch& b,
-                       int gaussian, int ctas, float2* partial, cudaStream_t st);
+                       int gaussian, int ctas, double2* partial, cudaStream_t st);
 // partial sums of every CTA -> facet of each galaxy (FP64 sums in CTA order), evaluate_uv_grid.c
 // finalisation and compaction into out (slot = galaxy index in the batch)
-int launch_finalize_seq(const SeqBatch& b, int ctas, const float2* partial, const double* const* ss,
+int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
                         const double* const* sw, double len, FacetOut out, cudaStream_t st);
 // vis += the round models (sheared = 0: the sky model) or the sheared models (sheared = 1: the
 // simulator) of n_gal galaxies, FP32 visibilities, evenly spaced channels (batch_set_channels)

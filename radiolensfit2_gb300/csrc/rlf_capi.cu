@@ -20,6 +20,7 @@
 #include "rlf_vis.cuh"
 #include "rlf_batch.cuh"
 #include "rlf_ms.cuh"
+#include "rlf_proposal.cuh"
 #include "../../include/rlf_gb300.h"
 #include "../../include/rlf_testing.h"
 
@@ -118,7 +119,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -172,7 +173,7 @@ struct rlf_observation {
   std::map<unsigned, rlf::FacetCache*> facets;
   rlf::DevBuf<double> partial;
   rlf::DevBuf<rlf::RowF> rows;      // FP32 row table of the batched kernels (built on first use)
-  rlf::DevBuf<float2> bpartial;     // partial facets of the batched extraction
+  rlf::DevBuf<double2> bpartial;    // partial facets of the batched extraction
   // mixed-precision observations store their rows in uv order (launch_row_order), so that the
   // batched extraction's consecutive work items are neighbours in uv and in memory: perm[p] is the
   // caller's row at position p, inv its inverse; empty for FP64 observations (caller's order)
@@ -399,8 +400,9 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       while (j < n && j - i < std::min(B, kSeqMaxGal) && (unsigned)facets[j] <= kBatchMaxFacet) {
         const int F = facets[j];
         const bool new_size = std::find(sizes.begin(), sizes.end(), F) == sizes.end();
-        if ((size_t)(cells + F * F) * sizeof(float2) > kSeqFacetBudget) break;
+        if ((size_t)(cells + F * F) * kSeqCellBytes > kSeqFacetBudget) break;
         if (new_size && (int)sizes.size() == kSeqMaxSizes) break;
+        if (seq_smem_bytes(j - i + 1, cells + F * F, (int)sizes.size() + (new_size ? 1 : 0)) > kSeqMaxSmem) break;
         if (new_size) sizes.push_back(F);
         fidx[j] = (int)(std::find(sizes.begin(), sizes.end(), F) - sizes.begin());
         foff[j] = cells;
@@ -431,6 +433,9 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   RLF_OK(dfidx.upload(fidx.data(), n, st));
   RLF_OK(dfoff.upload(foff.data(), n, st));
   RLF_OK(dfac.upload(facets.data(), n, st));
+  // learned proposal of the simplex starts: computed on the device from each round's facets
+  const bool learned = !opt.start && opt.proposal && proposal_ready() && !facets_out;
+  if (learned) RLF_OK(dstart.ensure((size_t)3 * n));
   if (opt.start) {
     std::vector<double> sv((size_t)3 * n);
     for (int i = 0; i < n; ++i)
@@ -564,7 +569,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       fr.offset = doff.p + j0;
       fr.count = dnc.p + bj;
       fr.rprior = dprior.p + (size_t)bj * kMaxNodes;
-      fr.start = opt.start ? dstart.p + (size_t)3 * bj : nullptr;
+      fr.start = (opt.start || learned) ? dstart.p + (size_t)3 * bj : nullptr;
       fr.out = dout.p + bj;
       // ---- extraction
       if (u.seq) {
@@ -599,6 +604,14 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       RLF_OK(pt.mark(kPhaseExtract, st));
       if (facets_out) break;
       // ---- fit
+      if (learned) {
+        static_assert(sizeof(GalaxyParams) % sizeof(double) == 0, "GalaxyParams holds whole doubles");
+        const double* flux = reinterpret_cast<const double*>(reinterpret_cast<const char*>(dg.p + bj) +
+                                                             offsetof(GalaxyParams, flux));
+        RLF_OK(propose_starts(bk, doff.p + j0, dnc.p + bj, dfac.p + bj, gu, gv, dre, dim, sg, fprec == kMixed ? 1 : 0,
+                              flux, (int)(sizeof(GalaxyParams) / sizeof(double)), ob->len, dstart.p + (size_t)3 * bj,
+                              st));
+      }
       const bool last = rd == nr - 1;
       if (u.seq && last && nr > 1)
         RLF_CUDA(copy_async(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));

@@ -118,7 +118,7 @@ class DeviceObservation:
 
     def process(self, cat: Catalogue, *, batch: int = 1, refit: bool = True, gaussian: int = 0,
                 start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64, rounds: int = 0,
-                board_wait_us: int = 0) -> ProcessResult:
+                board_wait_us: int = 0, proposal: int = 0) -> ProcessResult:
         ro, pro = _d(K.ro_grid())
         arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
         opt = _lib.Options()
@@ -130,6 +130,7 @@ class DeviceObservation:
         opt.fit_precision = int(fit_precision)
         opt.rounds = int(rounds)
         opt.board_wait_us = int(board_wait_us)
+        opt.proposal = int(proposal)
         st = None
         if start is not None:
             st = np.ascontiguousarray(start, dtype=np.float64).reshape(-1)
