@@ -58,6 +58,9 @@ typedef struct {
   int proposal;      /* 1: start each galaxy's simplex at the learned proposal (rlf_proposal_set_params)
                         instead of (0, 0) with step 0.1; ignored when `start` is given or no network is
                         loaded */
+  int seq_facet_kb;  /* batched mode: shared memory (KB, 16..200) for the facet accumulators of one
+                        sub-batch, which bounds the galaxies extracted per pass (0 = 128) */
+  int fit_ctas_per_sm; /* persistent fit thread blocks per SM (1..3, 0 = 3) */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -180,6 +183,25 @@ enum {
   RLF_NSTATS = 10
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
+
+/* -------- channel shards --------
+ * No counterpart names in the reference; the steps of its MPI decomposition
+ * (data_processing-mpi.c:65-216), one process per GPU holding its own channels:
+ * rlf_obs_facet_partials: every galaxy's facet sums over this observation's channels, un-averaged,
+ *   out[g][4][stride] = sum of vis re, sum of vis im, sum of sigma^2, sum of weights per cell of the
+ *   galaxy's F x F facet (row-major, F^2 <= stride; the rest zero), extracted against the current
+ *   data and sky model as source_extraction does (evaluate_uv_grid.c:143-195 before averaging);
+ * rlf_fit_partials: the facets of the summed partials of all shards (average_facets,
+ *   evaluate_facet_coords), fitted together by the persistent fit kernel: source_fitting's results;
+ * rlf_obs_remove: removal of the given fits from this observation's data and sky model, in order,
+ *   bad fits (error != 0) skipped (data_processing.c:109-135). */
+int rlf_obs_facet_partials(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                           const double *l, const double *m, double *out, int stride);
+int rlf_fit_partials(int n_gal, const double *partials, int stride, const double *flux,
+                     const double *scale, double len, int numr, const double *ro,
+                     const rlf_options *opt, rlf_fit_result *out);
+int rlf_obs_remove(rlf_observation *obs, int n_gal, const double *flux, const double *scale,
+                   const double *l, const double *m, const rlf_fit_result *fits);
 
 /* -------- learned proposal of the simplex start --------
  * No counterpart in the reference (whose simplex starts at (0, 0) with step 0.1,

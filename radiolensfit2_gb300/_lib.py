@@ -36,7 +36,8 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("batch", C.c_int), ("gaussian", C.c_int),
                 ("refit", C.c_int), ("verbose", C.c_int), ("start", PD), ("fit_precision", C.c_int),
                 ("rounds", C.c_int), ("reuse_obs", C.c_int),
-                ("board_wait_us", C.c_int), ("proposal", C.c_int)]
+                ("board_wait_us", C.c_int), ("proposal", C.c_int), ("seq_facet_kb", C.c_int),
+                ("fit_ctas_per_sm", C.c_int)]
 
 
 _lib = None
@@ -84,6 +85,10 @@ def load():
         "rlf_gridding_visibilities_noalloc": (C.c_int, [PD, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p,
                                                         C.c_void_p, C.c_void_p, D, C.c_uint, C.c_void_p,
                                                         C.c_void_p, C.c_void_p, C.c_void_p]),
+        "rlf_obs_facet_partials": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, PD, C.c_int]),
+        "rlf_fit_partials": (C.c_int, [C.c_int, PD, C.c_int, PD, PD, D, C.c_int, PD, C.POINTER(Options),
+                                       C.POINTER(FitResult)]),
+        "rlf_obs_remove": (C.c_int, [C.c_void_p, C.c_int, PD, PD, PD, PD, C.POINTER(FitResult)]),
         "rlf_cnn_param_count": (C.c_int, []),
         "rlf_cnn_create": (C.c_void_p, [C.c_int, C.c_int]),
         "rlf_cnn_destroy": (None, [C.c_void_p]),
@@ -148,7 +153,8 @@ EXPORTED = [
     "f_likelihood", "loglikelihood", "loglikelihood_r", "cross_correlation",
     "marginalise_over_position_shift", "likelihood_sampling", "source_extraction", "source_fitting",
     "data_processing", "sky_model", "rfunc", "scale_mean", "rlf_set_posterior_values",
-    "rlf_marginalise_posterior_r", "rlf_marf", "rlf_cnn_param_count", "rlf_cnn_create", "rlf_cnn_destroy",
+    "rlf_marginalise_posterior_r", "rlf_marf", "rlf_obs_facet_partials", "rlf_fit_partials", "rlf_obs_remove",
+    "rlf_cnn_param_count", "rlf_cnn_create", "rlf_cnn_destroy",
     "rlf_cnn_set_params", "rlf_cnn_get_params", "rlf_cnn_store_facets", "rlf_cnn_set_targets",
     "rlf_cnn_read_images", "rlf_cnn_set_images", "rlf_cnn_grads", "rlf_cnn_train_step", "rlf_cnn_predict", "rlf_proposal_set_params",
 ]

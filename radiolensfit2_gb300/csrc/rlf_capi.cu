@@ -119,7 +119,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0, 0};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0, 0, 0, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -380,6 +380,10 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     if (bc < 0) batched = false;
     else if (bc > 0) return bc;
   }
+  // tunables (rlf_options, chosen by the autotuner): shared-memory facet budget of a sub-batch
+  const size_t facet_budget = opt.seq_facet_kb > 0
+                                  ? (size_t)std::min(std::max(opt.seq_facet_kb, 16), 200) * 1024
+                                  : kSeqFacetBudget;
   // units of work in order: sub-batches [u0, u1) of the sequential extraction, or single galaxies
   struct Unit { int b0, bn; bool seq; };
   std::vector<Unit> units;
@@ -400,7 +404,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       while (j < n && j - i < std::min(B, kSeqMaxGal) && (unsigned)facets[j] <= kBatchMaxFacet) {
         const int F = facets[j];
         const bool new_size = std::find(sizes.begin(), sizes.end(), F) == sizes.end();
-        if ((size_t)(cells + F * F) * kSeqCellBytes > kSeqFacetBudget) break;
+        if ((size_t)(cells + F * F) * kSeqCellBytes > facet_budget) break;
         if (new_size && (int)sizes.size() == kSeqMaxSizes) break;
         if (seq_smem_bytes(j - i + 1, cells + F * F, (int)sizes.size() + (new_size ? 1 : 0)) > kSeqMaxSmem) break;
         if (new_size) sizes.push_back(F);
@@ -473,10 +477,12 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   void* dim = cells.p + 3 * plane;
   void* sg = cells.p + 4 * plane;
   RLF_OK(ob->partial.ensure((size_t)ob->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
-  const int grid_fit = fit_max_grid(fprec);
   int sms = 0, dev = 0;
   RLF_CUDA(cudaGetDevice(&dev));
   RLF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // persistent fit CTAs: per SM at most the kernel's occupancy (fit_max_grid), fewer when tuned
+  const int grid_fit = opt.fit_ctas_per_sm > 0 ? std::min(fit_max_grid(fprec), sms * opt.fit_ctas_per_sm)
+                                               : fit_max_grid(fprec);
   const int seq_ctas = kSeqCtasPerSm * sms;
   if (batched && !ob->rows.p) {
     RLF_OK(ob->rows.ensure(ob->n_rows));
@@ -1289,6 +1295,197 @@ int rlf_obs_extract(rlf_observation* obs, int n_gal, const double* flux, const d
   std::vector<FitOut> out;
   std::vector<double> ro(kMaxNodes, 1.0);
   return run_pass(obs, gals, order, 24, ro.data(), o, out, st, nullptr, facets, ncoords, stride);
+}
+
+// -------------------------------------------------------------- channel shards
+// The reference's MPI decomposition (data_processing-mpi.c:65-216): every rank holds the
+// visibilities of its own channels, extracts every galaxy of a round into un-averaged facet sums
+// over those channels, the sums of all ranks are added (data_processing-mpi.c:95-124), the owner of
+// a galaxy fits the summed facet and every rank removes the fitted galaxies from its own channels
+// (:169-210).  These three steps are the entry points below; the exchange between them is the
+// caller's (radiolensfit2_gb300.shard: torch.distributed all-reduce and all-gather).
+
+int rlf_obs_facet_partials(rlf_observation* obs, int n_gal, const double* flux, const double* scale,
+                           const double* l, const double* m, double* out, int stride) {
+  if (!obs || n_gal < 0 || (n_gal && !out)) return 1;
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  const unsigned fmax = rlf::facet_size(kRMax, obs->len);
+  if ((unsigned)stride < fmax * fmax) { fprintf(stderr, "rlf: partials stride %d below %u\n", stride, fmax * fmax); return 1; }
+  std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, fmax);
+  DevBuf<GalaxyParams> dg;
+  RLF_OK(dg.upload(gals.data(), n_gal, st));
+  RLF_OK(obs->partial.ensure((size_t)obs->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
+  const Observation o = obs->view();
+  for (int g = 0; g < n_gal; ++g) {
+    const unsigned F = (unsigned)gals[g].facet;
+    const int nc = (int)(F * F);
+    FacetCache* fc = nullptr;
+    RLF_OK(obs_facet(obs, F, &fc, st));
+    if (obs->precision == RLF_F64)
+      RLF_OK(launch_extract_f64(o, obs->data64.p, obs->sky64.p, fc->cell.p, dg.p + g, F, g_lib.opt.gaussian,
+                                obs->partial.p, obs->n_part, st));
+    else
+      RLF_OK(launch_extract_mixed(o, obs->data32.p, obs->sky32.p, fc->cell.p, dg.p + g, F, g_lib.opt.gaussian,
+                                  obs->partial.p, obs->n_part, st));
+    double* sums = obs->partial.p + (size_t)obs->n_part * 2 * nc;
+    RLF_OK(launch_reduce_partials(obs->partial.p, obs->n_part, 2 * nc, sums, st));
+    double* row = out + (size_t)g * 4 * stride;
+    RLF_CUDA(copy_async(row, sums, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(copy_async(row + stride, sums + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(copy_async(row + 2 * stride, fc->ss.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(copy_async(row + 3 * stride, fc->sw.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RLF_CUDA(cudaStreamSynchronize(st));  // `sums` is reused by the next galaxy
+    for (int a = 0; a < 4; ++a)
+      for (int c = nc; c < stride; ++c) row[(size_t)a * stride + c] = 0.0;
+  }
+  return 0;
+}
+
+int rlf_fit_partials(int n_gal, const double* partials, int stride, const double* flux, const double* scale,
+                     double len, int numr, const double* ro, const rlf_options* opt, rlf_fit_result* out) {
+  if (n_gal < 0 || (n_gal && (!partials || !out))) return 1;
+  if (n_gal == 0) return 0;
+  if (numr < 2 || numr > kMaxNodes) { fprintf(stderr, "rlf: %d scalelength nodes unsupported\n", numr); return 1; }
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  const rlf_options o = opt ? *opt : g_lib.opt;
+  const Precision fprec = o.fit_precision == RLF_MIXED ? kMixed : kF64;
+  const unsigned fmax = rlf::facet_size(kRMax, len);
+  if ((unsigned)stride < fmax * fmax) { fprintf(stderr, "rlf: partials stride %d below %u\n", stride, fmax * fmax); return 1; }
+  const std::vector<double> zero(n_gal, 0.0);  // positions play no part in the fit
+  std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, zero.data(), zero.data(), len, fmax);
+  // sums as k_facet_finalize takes them: per galaxy [re (F^2) | im (F^2)] at 2 * stride; ss, sw planes
+  std::vector<double> sums((size_t)n_gal * 2 * stride, 0.0), ss((size_t)n_gal * stride, 0.0), sw((size_t)n_gal * stride, 0.0);
+  std::vector<int> facets(n_gal), offs(n_gal);
+  std::vector<double> rprior((size_t)n_gal * kMaxNodes, 0.0);
+  int max_cells = 0;
+  for (int g = 0; g < n_gal; ++g) {
+    const int F = gals[g].facet, nc = F * F;
+    facets[g] = F;
+    max_cells = std::max(max_cells, nc);
+    const double* row = partials + (size_t)g * 4 * stride;
+    std::copy(row, row + nc, sums.begin() + (size_t)g * 2 * stride);
+    std::copy(row + stride, row + stride + nc, sums.begin() + (size_t)g * 2 * stride + nc);
+    std::copy(row + 2 * stride, row + 2 * stride + nc, ss.begin() + (size_t)g * stride);
+    std::copy(row + 3 * stride, row + 3 * stride + nc, sw.begin() + (size_t)g * stride);
+    const double mu = scale_mean(flux[g]);
+    for (int r = 1; r < numr; ++r) rprior[(size_t)g * kMaxNodes + r] = rfunc(mu, kRStd, ro[r]);
+  }
+  for (int g = 0; g < n_gal; ++g) offs[g] = g * max_cells;
+  DevBuf<double> dsums, dss, dsw, dprior;
+  DevBuf<const double*> pss, psw;
+  DevBuf<int> dfac, doff, dnc, dqueue;
+  RLF_OK(dsums.upload(sums.data(), sums.size(), st));
+  RLF_OK(dss.upload(ss.data(), ss.size(), st));
+  RLF_OK(dsw.upload(sw.data(), sw.size(), st));
+  std::vector<const double*> pssh(n_gal), pswh(n_gal);
+  for (int g = 0; g < n_gal; ++g) {
+    pssh[g] = dss.p + (size_t)g * stride;
+    pswh[g] = dsw.p + (size_t)g * stride;
+  }
+  RLF_OK(pss.upload(pssh.data(), n_gal, st));
+  RLF_OK(psw.upload(pswh.data(), n_gal, st));
+  RLF_OK(dfac.upload(facets.data(), n_gal, st));
+  RLF_OK(doff.upload(offs.data(), n_gal, st));
+  RLF_OK(dnc.ensure(n_gal));
+  RLF_OK(dprior.upload(rprior.data(), rprior.size(), st));
+  RLF_OK(dqueue.ensure(1));
+  const size_t esz = fprec == kF64 ? sizeof(double) : sizeof(float);
+  const size_t plane = (size_t)n_gal * max_cells * esz;
+  DevBuf<unsigned char> cells;
+  RLF_OK(cells.ensure(5 * plane));
+  FacetOut fo;
+  fo.offset = doff.p;
+  fo.ncoords = dnc.p;
+  fo.gu = cells.p; fo.gv = cells.p + plane; fo.dre = cells.p + 2 * plane; fo.dim = cells.p + 3 * plane;
+  fo.sig2 = cells.p + 4 * plane;
+  fo.as_float = fprec == kMixed;
+  RLF_OK(launch_facet_finalize(n_gal, dfac.p, dsums.p, 1, 2LL * stride, pss.p, psw.p, len, fo, st));
+  FitConfigHost fc;
+  memset(&fc, 0, sizeof(fc));
+  fc.numr = numr;
+  fc.gaussian = o.gaussian;
+  fc.np_max = kNpMax;
+  for (int i = 0; i < numr; ++i) fc.ro[i] = ro[i];
+  RLF_OK(fit_set_config(fc, st));
+  DevBuf<FitOut> dout;
+  RLF_OK(dout.ensure(n_gal));
+  RLF_CUDA(cudaMemsetAsync(dout.p, 0, n_gal * sizeof(FitOut), st));
+  DevBuf<SampleSlot> bslot;
+  DevBuf<double> bL;
+  DevBuf<int> berr, bflag, bnewton, bdone;
+  RLF_OK(bslot.ensure(n_gal));
+  RLF_OK(bL.ensure((size_t)n_gal * 2 * kBoardCap));
+  RLF_OK(berr.ensure((size_t)n_gal * 2 * kBoardCap));
+  RLF_OK(bflag.ensure((size_t)n_gal * 2 * kBoardCap));
+  RLF_OK(bnewton.ensure(n_gal));
+  RLF_OK(bdone.ensure(1));
+  RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)n_gal * sizeof(SampleSlot), st));
+  RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)n_gal * 2 * kBoardCap * sizeof(int), st));
+  RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)n_gal * sizeof(int), st));
+  RLF_CUDA(cudaMemsetAsync(bdone.p, 0, sizeof(int), st));
+  RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
+  FacetBatch fb{};
+  fb.n_gal = n_gal;
+  fb.max_cells = max_cells;
+  fb.offset = doff.p;
+  fb.count = dnc.p;
+  fb.gu = fo.gu; fb.gv = fo.gv; fb.dre = fo.dre; fb.dim = fo.dim; fb.sig2 = fo.sig2;
+  fb.rprior = dprior.p;
+  fb.start = nullptr;
+  fb.active = nullptr;
+  fb.out = dout.p;
+  fb.queue = dqueue.p;
+  fb.trace = nullptr;
+  fb.trace_cap = 0;
+  fb.board.slot = bslot.p;
+  fb.board.L = bL.p;
+  fb.board.err = berr.p;
+  fb.board.flag = bflag.p;
+  fb.board.newton = bnewton.p;
+  fb.board.done_gal = bdone.p;
+  fb.board.wait_ns = o.board_wait_us > 0 ? (unsigned long long)o.board_wait_us * 1000ull : 0ull;
+  int sms = 0, dev = 0;
+  RLF_CUDA(cudaGetDevice(&dev));
+  RLF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = o.fit_ctas_per_sm > 0 ? std::min(fit_max_grid(fprec), sms * o.fit_ctas_per_sm) : fit_max_grid(fprec);
+  RLF_OK(fit_launch(fb, fprec, grid, st));
+  std::vector<FitOut> h(n_gal);
+  RLF_OK(dout.download(h.data(), n_gal, st));
+  RLF_CUDA(cudaStreamSynchronize(st));
+  for (int g = 0; g < n_gal; ++g) memcpy(&out[g], &h[g], sizeof(rlf_fit_result));
+  return 0;
+}
+
+int rlf_obs_remove(rlf_observation* obs, int n_gal, const double* flux, const double* scale, const double* l,
+                   const double* m, const rlf_fit_result* fits) {
+  if (!obs || n_gal < 0 || (n_gal && !fits)) return 1;
+  if (n_gal == 0) return 0;
+  cudaStream_t st;
+  RLF_OK(lib_stream(&st));
+  RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
+  const unsigned fmax = rlf::facet_size(kRMax, obs->len);
+  std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, fmax);
+  std::vector<FitOut> f(n_gal);
+  for (int g = 0; g < n_gal; ++g) memcpy(&f[g], &fits[g], sizeof(rlf_fit_result));
+  DevBuf<GalaxyParams> dg;
+  DevBuf<FitOut> df;
+  RLF_OK(dg.upload(gals.data(), n_gal, st));
+  RLF_OK(df.upload(f.data(), n_gal, st));
+  const Observation o = obs->view();
+  // in catalogue order, one galaxy at a time (data_processing.c:109-135), bad fits skipped
+  for (int g = 0; g < n_gal; ++g) {
+    const double* e12 = &df.p[g].e1;
+    const int* err = &df.p[g].error;
+    if (obs->precision == RLF_F64)
+      RLF_OK(launch_remove_f64(o, obs->data64.p, obs->sky64.p, dg.p + g, e12, err, g_lib.opt.gaussian, st));
+    else
+      RLF_OK(launch_remove_mixed(o, obs->data32.p, obs->sky32.p, dg.p + g, e12, err, g_lib.opt.gaussian, st));
+  }
+  RLF_CUDA(cudaStreamSynchronize(st));
+  return 0;
 }
 
 int rlf_obs_last_stats(rlf_observation* obs, long long* stats) {

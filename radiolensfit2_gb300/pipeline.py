@@ -118,7 +118,8 @@ class DeviceObservation:
 
     def process(self, cat: Catalogue, *, batch: int = 1, refit: bool = True, gaussian: int = 0,
                 start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64, rounds: int = 0,
-                board_wait_us: int = 0, proposal: int = 0) -> ProcessResult:
+                board_wait_us: int = 0, proposal: int = 0, seq_facet_kb: int = 0,
+                fit_ctas_per_sm: int = 0) -> ProcessResult:
         ro, pro = _d(K.ro_grid())
         arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
         opt = _lib.Options()
@@ -131,6 +132,8 @@ class DeviceObservation:
         opt.rounds = int(rounds)
         opt.board_wait_us = int(board_wait_us)
         opt.proposal = int(proposal)
+        opt.seq_facet_kb = int(seq_facet_kb)
+        opt.fit_ctas_per_sm = int(fit_ctas_per_sm)
         st = None
         if start is not None:
             st = np.ascontiguousarray(start, dtype=np.float64).reshape(-1)
@@ -149,6 +152,25 @@ class DeviceObservation:
         self.lib.rlf_obs_last_stats(self.h, sv)
         stats = dict(zip(names, (int(x) for x in sv)))
         return ProcessResult(res, nbad.value, tuple(ms), stats)
+
+    def facet_partials(self, cat: Catalogue, stride: int) -> np.ndarray:
+        """Un-averaged facet sums of every galaxy over this observation's channels,
+        [n][4][stride]: sum vis re, sum vis im, sum sigma^2, sum of weights per cell
+        (rlf_obs_facet_partials)."""
+        arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
+        out = np.zeros((cat.n, 4, stride))
+        self._check(self.lib.rlf_obs_facet_partials(self.h, cat.n, *[p for _, p in arrs],
+                                                    out.ctypes.data_as(_lib.PD), int(stride)),
+                    "rlf_obs_facet_partials")
+        return out
+
+    def remove(self, cat: Catalogue, results: np.ndarray):
+        """Removal of the given fits (RESULT_DTYPE rows; error != 0 skipped) from the data and sky
+        model, in catalogue order (rlf_obs_remove)."""
+        arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
+        r = np.ascontiguousarray(results, RESULT_DTYPE)
+        buf = (_lib.FitResult * cat.n).from_buffer_copy(r.tobytes()) if cat.n else (_lib.FitResult * 1)()
+        self._check(self.lib.rlf_obs_remove(self.h, cat.n, *[p for _, p in arrs], buf), "rlf_obs_remove")
 
     def extract(self, cat: Catalogue, *, batch: int = 1):
         """Facets of every galaxy against the current data and sky model (no fit, no removal).
