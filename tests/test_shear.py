@@ -25,3 +25,33 @@ def test_bias_fit():
     gm = 1.05 * gt + 0.001
     m, c, me, ce = shear.multiplicative_additive_bias(gt, gm, np.full(5, 1e-3))
     assert abs(m - 0.05) < 1e-9 and abs(c - 0.001) < 1e-9
+
+
+def test_against_reference_script_fixtures():
+    """The reference's own shear.py run on fixed tables (tests/golden/make_shear_golden.py: its
+    prints made calls, its bootstrap the identity so that the printed shear is the full-sample
+    weighted mean): galaxies kept, bad count, shape noise and shear agree, including a table
+    whose last row is a bad odd row (the reference's end-of-file slip)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "shear_golden.npz"))
+    for name in ("clean", "bad_even_and_odd", "last_odd_bad"):
+        t, ref = g[name + "_table"], g[name + "_out"]
+        est = shear.estimate_shear(t[:, 2], t[:, 5], t[:, 3], t[:, 6], t[:, 7], t[:, 8], bootnum=50)
+        ngal, bad, sigma, g1, g2 = ref[:5]
+        assert est.n_used == int(ngal) and est.n_rejected == int(bad), name
+        assert abs(est.shape_noise - sigma) <= 1e-12 * abs(sigma), name
+        assert abs(est.g1 - g1) <= 1e-12 * abs(g1) and abs(est.g2 - g2) <= 1e-12 * abs(g2), name
+
+
+def test_reference_selection_rules():
+    n = 10
+    ok = np.full(n, 0.01)
+    v = ok.copy()
+    v[3] = 0.0   # odd: drops row 2 (kept) and itself
+    v[6] = 0.0   # even: drops itself and row 7 unread
+    kept, bad = shear.reference_selection(np.full(n, 0.1), np.full(n, 0.1), v, np.full(n, 50.0))
+    assert kept.tolist() == [0, 1, 4, 5, 8, 9] and bad == 2
+    v = ok.copy()
+    v[9] = 0.0   # the last row, odd: the reference deletes row 7 instead of row 8
+    kept, bad = shear.reference_selection(np.full(n, 0.1), np.full(n, 0.1), v, np.full(n, 50.0))
+    assert kept.tolist() == [0, 1, 2, 3, 4, 5, 6, 8] and bad == 1
