@@ -5,7 +5,7 @@ antennas (19,306 baselines) x 960 times at 30 s x 64 channels = 1.19e9 visibilit
 galaxies at 5-200 uJy with shear g = (0.02, 0.01), seeded synthetic array, catalogue and noise
 (no public dataset exists for this path).
 
-A step is one window of consecutive galaxies of the flux-ordered catalogue (default 2,000)
+A step is one window of consecutive galaxies of the flux-ordered catalogue (default 500)
 through the whole path: extraction, fit and removal of every galaxy of the window in catalogue
 order, then the re-fit pass over the window's bad galaxies (RadioLensfit2.cpp:597-606 applied to
 the window).  Steps walk down the catalogue and the data carry every earlier window's removals,
@@ -54,7 +54,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--galaxies", type=int, default=0, help="catalogue size (0 = the workload's)")
-    ap.add_argument("--window", type=int, default=2000, help="galaxies per step (at most the catalogue)")
+    ap.add_argument("--window", type=int, default=500, help="galaxies per step (at most the catalogue)")
+    ap.add_argument("--proposal", default="auto", choices=["auto", "none"],
+                    help="learned simplex-start proposal: auto = the package's trained network when present")
+    ap.add_argument("--tune", default="auto", choices=["auto", "none"],
+                    help="autotune the batched launch shapes on the first window before the warm-up")
     ap.add_argument("--batch", type=int, default=1000)
     ap.add_argument("--rounds", type=int, default=0,
                     help="extraction + fit rounds per batch (0 = library default)")
@@ -260,7 +264,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, steps, fit_prec):
+def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, steps, fit_prec, extra=None):
     """Galaxies/s through the reference-facing entry point data_processing() with pinned host
     complex128 buffers, one window per step: catalogue pass + re-fit pass of the window (two calls),
     copies inside the timing.  rlf_options.reuse_obs keeps uvw, variances, flags and the facet tables
@@ -273,6 +277,8 @@ def e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, steps, fit_prec):
     opt = _lib.Options()
     opt.precision, opt.batch, opt.refit, opt.fit_precision = _lib.RLF_MIXED, B, 1, fit_prec
     opt.reuse_obs = 1  # the two passes and the windows pass the same uvw, variances and flags
+    for k, v in (extra or {}).items():  # proposal and tuned launch shapes, as the device-resident run
+        setattr(opt, k, int(v))
     lib.rlf_configure(C.byref(opt))
     n_vis = obs.n_vis
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -427,6 +433,20 @@ def main():
     fit_prec = _lib.RLF_F64 if args.fit_precision == "f64" else _lib.RLF_MIXED
     win = window_size(args, cat.n)
     plan = windows(cat.n, win, args.warmup + args.steps)
+    # the learned proposal of the simplex starts (trained network shipped with the package)
+    from radiolensfit2_gb300 import proposal as PR, autotune as AT
+    use_prop = 0
+    prop_desc = "none (simplex start (0, 0), step 0.1)"
+    if args.proposal == "auto" and os.path.exists(PR.WEIGHTS):
+        PR.load()
+        use_prop = 1
+        prop_desc = "learned (radiolensfit2_gb300/proposal_weights.npz, rlf_options.proposal = 1)"
+    # launch shapes tuned on the first window, from the snapshot (restored after every candidate)
+    shapes, tune_ms = {}, None
+    if args.tune == "auto" and B > 1:
+        a0, b0, _ = plan[0]
+        shapes, tune_ms = AT.tune(dev, cat.subset(range(a0, b0)), batch=B, fit_precision=fit_prec,
+                                  rounds=args.rounds, proposal=use_prop)
     # the first walk over the catalogue: its results (shear) and device time (whole-job throughput)
     full = np.zeros(cat.n, RESULT_DTYPE)
     seen = np.zeros(cat.n, bool)
@@ -435,7 +455,8 @@ def main():
     def step(a, b, restore):
         if restore:
             dev.restore()
-        r = dev.process(cat.subset(range(a, b)), batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
+        r = dev.process(cat.subset(range(a, b)), batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds,
+                        proposal=use_prop, **shapes)
         if not seen[a:b].any():
             full[a:b] = r.results
             seen[a:b] = True
@@ -484,11 +505,11 @@ def main():
            "config": {"workload": args.workload, "antennas": w["n_ant"], "rows": obs.n_rows, "channels": obs.n_ch,
                       "n_vis": obs.n_vis, "galaxies": cat.n, "window": win, "timed_galaxies": n_timed,
                       "batch": B, "precision": "mixed", "fit_precision": args.fit_precision,
-                      "proposal": "none (simplex start (0, 0), step 0.1)",
+                      "proposal": prop_desc, "tuned_shapes": shapes or "defaults",
                       "l2_policy": "inputs larger than L2 (data + sky model %.1f GB)" % (16 * obs.n_vis / 1e9),
                       "timing": "CUDA events on the library stream around both passes of each window"},
            "setup_s": setup_s, "wall_ms_per_step": wall / args.steps * 1e3, "stage_ms_per_step": stage_ms,
-           "bad_galaxies_timed": int(n_bad), "gpu_launches": launches, "work": stats,
+           "bad_galaxies_timed": int(n_bad), "gpu_launches": launches, "work": stats, "autotune_ms": tune_ms,
            "roofline": roofline_of(obs, stats, args.steps, hbm_peak, peak_kind, fp32_peak),
            "clocks": ck, "peaks": peak_kind}
     snr = None
@@ -503,28 +524,41 @@ def main():
     if rank == 0 and args.plain_prefix > 0:
         P = min(args.plain_prefix, cat.n)
         pre = cat.subset(range(P))
+        # the same prefix from the same data: learned+batched (the measured path), batched with the
+        # reference's simplex start, and the plain one-galaxy-at-a-time fit
         dev.restore()
-        rb = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds)
+        rb = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds, proposal=use_prop,
+                         **shapes)
+        dev.restore()
+        rn = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds, **shapes)
         dev.restore()
         rp = dev.process(pre, batch=1, refit=True, fit_precision=fit_prec)
-        bt, pl = rb.results, rp.results
+        bt, bn, pl = rb.results, rn.results, rp.results
         gpu_first = bt
-        ok = (pl["error"] == 0) & (bt["error"] == 0)
-        de = np.maximum(np.abs(pl["e1"][ok] - bt["e1"][ok]), np.abs(pl["e2"][ok] - bt["e2"][ok]))
+
+        def dev_of(a, b):
+            ok = (a["error"] == 0) & (b["error"] == 0)
+            de = np.maximum(np.abs(a["e1"][ok] - b["e1"][ok]), np.abs(a["e2"][ok] - b["e2"][ok]))
+            return {"max": float(de.max()) if de.size else None, "median": float(np.median(de)) if de.size else None,
+                    "frac_le_1e-3": float(np.mean(de <= 1e-3)) if de.size else None,
+                    "frac_le_1e-4": float(np.mean(de <= 1e-4)) if de.size else None, "n": int(de.size),
+                    "error_flags_differ": int(np.sum(a["error"] != b["error"]))}
+
         plain_rate = P / (rp.ms[0] * 1e-3)
         out["plain_gpu"] = {"value": plain_rate, "unit": "galaxies/s", "prefix_galaxies": P, "ms": rp.ms[0],
                             "stage_ms": dict(zip(("extract", "fit", "remove"), rp.ms[1:])),
-                            "batched_on_prefix": {"value": P / (rb.ms[0] * 1e-3), "ms": rb.ms[0]},
-                            "speedup_batched_vs_plain_same_prefix": rp.ms[0] / rb.ms[0],
+                            "evals_per_galaxy": float(np.mean(pl["nevals"])),
+                            "measured_path_on_prefix": {"value": P / (rb.ms[0] * 1e-3), "ms": rb.ms[0],
+                                                        "evals_per_galaxy": float(np.mean(bt["nevals"]))},
+                            "batched_reference_start_on_prefix": {"value": P / (rn.ms[0] * 1e-3), "ms": rn.ms[0],
+                                                                  "evals_per_galaxy": float(np.mean(bn["nevals"]))},
+                            "speedup_measured_path_vs_plain_same_prefix": rp.ms[0] / rb.ms[0],
                             "speedup_value_vs_plain": value / plain_rate,
-                            "abs_de_vs_batched": {"max": float(de.max()) if de.size else None,
-                                                  "median": float(np.median(de)) if de.size else None,
-                                                  "frac_le_1e-3": float(np.mean(de <= 1e-3)) if de.size else None,
-                                                  "frac_le_1e-4": float(np.mean(de <= 1e-4)) if de.size else None,
-                                                  "n": int(de.size)},
-                            "error_flags_differ": int(np.sum(pl["error"] != bt["error"]))}
+                            "abs_de_measured_vs_plain": dev_of(bt, pl),
+                            "abs_de_batched_reference_start_vs_plain": dev_of(bn, pl),
+                            "abs_de_learned_vs_reference_start": dev_of(bt, bn)}
         if snr is not None:
-            out["shear"].append(shear_block(pre, bt, snr[:P], "batched, prefix"))
+            out["shear"].append(shear_block(pre, bt, snr[:P], "measured path, prefix"))
             out["shear"].append(shear_block(pre, pl, snr[:P], "plain, prefix"))
     n_cpu = cpu_sample_size(args, obs) if gpu_first is not None else 0
     data_h = sky_h = None
@@ -534,7 +568,7 @@ def main():
     dev.close()
     if rank == 0 and not args.no_e2e:
         out["e2e"] = e2e_data_processing(lib, obs, cat, data_h, sky_h, B, win, max(1, min(args.steps, args.e2e_steps)),
-                                         fit_prec)
+                                         fit_prec, dict(shapes, proposal=use_prop))
     if rank == 0 and n_cpu > 0:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
         n_cpu = min(n_cpu, len(gpu_first))

@@ -208,7 +208,8 @@ int rlf_obs_remove(rlf_observation *obs, int n_gal, const double *flux, const do
  * galaxy_fitting.c:59-65).  A convolutional network (4 convolutions 3x3 stride 2 of 32 channels on
  * bf16 tensor cores, FP32 accumulation, a dense head) reads a 64 x 64 x 4 resampling of a galaxy's
  * facet (visibility / flux re and im, cell mask, cell SNR) and proposes (e1, e2, ln r, ln sigma);
- * the fit starts at (e1, e2) with step 2 sigma in [0.02, 0.1] and stays the judge.  Parameters:
+ * a galaxy with sigma <= 0.05 starts its fit at (e1, e2) with step 2 sigma (at least 0.02), the
+ * others at the reference's (0, 0) with step 0.1; the fit stays the judge.  Parameters:
  * rlf_cnn_param_count() floats, per convolution W[32][9 cin] (k = (3 ky + kx) cin + ci) and b[32],
  * then the head's W[4][512] (feature (4 y + x) 32 + c) and b[4]. */
 typedef struct rlf_cnn rlf_cnn;

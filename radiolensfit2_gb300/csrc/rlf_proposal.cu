@@ -576,7 +576,11 @@ __global__ void k_unpack_dw(const float* __restrict__ dwt, int k, float* __restr
 }
 
 // proposal (e1, e2, step) for the fit from the head's outputs: e clamped to |e| <= 0.7 (the fit's
-// objective is finite for |e|^2 < 0.65, likelihood.c:87-100), step 2 sigma in [0.02, 0.1]
+// objective is finite for |e|^2 < 0.65, likelihood.c:87-100), step 2 sigma in [0.02, 0.1].  A galaxy
+// whose predicted sigma exceeds kPropMaxSigma keeps the reference's start (0, 0) with step 0.1: for
+// the unresolved, noise-dominated galaxies the proposal carries no information beyond the prior,
+// and a different start only moves the end of the simplex on a flat likelihood.
+constexpr float kPropMaxSigma = 0.05f;
 __global__ void k_to_start(int n, const float* __restrict__ out, double* __restrict__ start) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
@@ -589,9 +593,10 @@ __global__ void k_to_start(int n, const float* __restrict__ out, double* __restr
     e2 *= s;
   }
   const float sig = __expf(fminf(fmaxf(o[3], -5.f), 0.5f));
-  start[3 * g + 0] = e1;
-  start[3 * g + 1] = e2;
-  start[3 * g + 2] = fminf(fmaxf(2.f * sig, 0.02f), 0.1f);
+  const bool use = sig <= kPropMaxSigma && isfinite(e1) && isfinite(e2);
+  start[3 * g + 0] = use ? (double)e1 : 0.0;
+  start[3 * g + 1] = use ? (double)e2 : 0.0;
+  start[3 * g + 2] = use ? (double)fminf(fmaxf(2.f * sig, 0.02f), 0.1f) : 0.1;
 }
 
 // ------------------------------------------------------------------ host side

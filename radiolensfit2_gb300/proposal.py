@@ -148,8 +148,9 @@ def training_set(net: ProposalNet, n_gal: int, *, workload="c2_ska_mid_32ch", pe
                  fmin=10.0, fmax=200.0, g=(0.03, -0.02), first=0, verbose=True):
     """Simulate n_gal galaxies (catalogue distributions of the small CPU configuration: flux 10-200 uJy,
     shear g) on `workload`'s array, per_obs per simulated observation, extract their facets and
-    store images and targets (e1, e2 sheared, ln scale) in the network's store from `first`.
-    Returns the catalogues."""
+    store images and targets in the network's store from `first`.  Targets: the maximum of the
+    plain fit's simplex (where the proposal should start it), else the true sheared ellipticity, and
+    ln scalelength.  Returns the observation and the catalogues."""
     from .pipeline import DeviceObservation
     w = dict(synth.WORKLOADS[workload])
     obs = synth.make_observation(**w)
@@ -164,9 +165,14 @@ def training_set(net: ProposalNet, n_gal: int, *, workload="c2_ska_mid_32ch", pe
         dev.simulate(cat, obs.sigma, seed=seed * 1000 + k)
         dev.sky_model(cat)
         buf, nc = extract_raw(dev, cat)
+        fit = dev.process(cat, batch=1000, refit=False).results
         dev.close()
+        me1, me2 = fit["max_e1"], fit["max_e2"]
+        ok = np.isfinite(me1) & np.isfinite(me2) & (me1 * me1 + me2 * me2 < 0.65)
+        t1 = np.where(ok, me1, cat.e1)
+        t2 = np.where(ok, me2, cat.e2)
         net.store_facets(first + done, buf, nc, facet_sizes(cat, obs.len_lambda), cat.flux, obs.len_lambda)
-        net.set_targets(first + done, np.stack([cat.e1, cat.e2, np.log(cat.scale)], 1))
+        net.set_targets(first + done, np.stack([t1, t2, np.log(cat.scale)], 1))
         cats.append(cat)
         done += m
         k += 1

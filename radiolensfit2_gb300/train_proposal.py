@@ -52,6 +52,13 @@ def evaluate(obs, n_gal, seed=11, batch=1000, fmin=10.0, fmax=200.0, g=(0.03, -0
                      "simplex_iters_per_galaxy": float(np.mean(res["iters"])),
                      "fit_ms": r.ms[2], "total_ms": r.ms[0], "wall_s": wall, "bad": int(r.n_bad)}
     rep["eval_reduction"] = 1.0 - rep["learned_start"]["evals_per_galaxy"] / rep["plain_start"]["evals_per_galaxy"]
+    # the galaxies the proposal started (predicted sigma <= 0.05): evaluations and |de| there
+    a_it, b_it = a["nevals"], b["nevals"]
+    moved = (a["iters"] != b["iters"]) | (a_it != b_it)
+    rep["galaxies_with_changed_path"] = int(moved.sum())
+    if moved.any():
+        rep["changed_path"] = {"evals_reference_start": float(np.mean(a_it[moved])),
+                               "evals_learned_start": float(np.mean(b_it[moved]))}
     return rep
 
 
