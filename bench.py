@@ -404,6 +404,64 @@ def roofline_of(obs, st, steps, hbm_peak, peak_kind, fp32_peak):
     return r
 
 
+def run_sharded(args, rank, world, local):
+    """N > 1: the reference's MPI decomposition (data_processing-mpi.c:65-216) across GPUs.  Rank r
+    holds channels channel_shards(n_ch, N)[r] of the observation (the same facet extent len on every
+    rank); per window every rank extracts un-averaged facet partials of the window's galaxies over its
+    channels, the partials are all-reduced over NCCL, each rank fits the galaxies it owns
+    (round-robin), the results are all-reduced, and every rank removes the good fits from its
+    channels; then the window's re-fit pass.  Windows play the reference's rounds (all galaxies of a
+    window extracted from the same data).  The total work is fixed as N grows (strong scaling);
+    timing: wall clock between barriers after CUDA synchronisation, max over ranks."""
+    import torch
+    import torch.distributed as dist
+    from radiolensfit2_gb300 import _lib, shard
+    from radiolensfit2_gb300.pipeline import DeviceObservation
+    w, obs, cat = workload(args)
+    so, (lo, hi) = shard.shard_observation(obs, world, rank)
+    dev = DeviceObservation(so, precision=_lib.RLF_MIXED)
+    dev.simulate(cat, so.sigma, seed=synth.NOISE_SEED + rank)
+    dev.sky_model(cat)
+    win = window_size(args, cat.n)
+    plan = windows(cat.n, win, args.warmup + args.steps)
+    dev.snapshot()
+    pipe = shard.ShardPipeline([dev], shard.TorchExchange(device=torch.device("cuda", local)), world=world, rank=rank,
+                               fit_precision=_lib.RLF_F64 if args.fit_precision == "f64" else _lib.RLF_MIXED)
+
+    def step(a, b, restore):
+        if restore:
+            dev.restore()
+        return pipe.process(cat.subset(range(a, b)), round_size=b - a, refit=True)
+
+    for (a, b, restore) in plan[:args.warmup]:
+        step(a, b, restore)
+    torch.cuda.synchronize()
+    dist.barrier()
+    lib = _lib.load()
+    l0 = lib.rlf_launch_count()
+    t0 = time.perf_counter()
+    n_timed = 0
+    for (a, b, restore) in plan[args.warmup:]:
+        step(a, b, restore)
+        n_timed += b - a
+    torch.cuda.synchronize()
+    dist.barrier()
+    t = torch.tensor([time.perf_counter() - t0], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed = float(t.item())
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": n_timed / elapsed, "unit": "galaxies/s", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+                          "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+                          "dtype": "fp32 visibilities (FP64 phase argument), %s fit" % args.fit_precision,
+                          "data": "synthetic (seeded array, catalogue and noise)",
+                          "config": {"workload": args.workload, "n_vis": obs.n_vis, "galaxies": cat.n, "window": win,
+                                     "parallelism": "channel shards x%d (data_processing-mpi decomposition)" % world,
+                                     "channels_rank0": [lo, hi]},
+                          "gpu_launches": int(lib.rlf_launch_count() - l0)}), flush=True)
+    dev.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -420,6 +478,7 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         torch.distributed.init_process_group("nccl")
+        return run_sharded(args, rank, world, local)
     lib = _lib.load()
     t_setup = time.perf_counter()
     w, obs, cat = workload(args)

@@ -61,6 +61,10 @@ typedef struct {
   int seq_facet_kb;  /* batched mode: shared memory (KB, 16..200) for the facet accumulators of one
                         sub-batch, which bounds the galaxies extracted per pass (0 = 128) */
   int fit_ctas_per_sm; /* persistent fit thread blocks per SM (1..3, 0 = 3) */
+  int graphs;        /* batched mode: 1 = each sub-batch's rounds (round control, extraction,
+                        finalisation, proposal, fit) and its removal are captured from the stream into
+                        one CUDA graph and launched as such; 0 = launched one by one.  Either way
+                        the host does not wait between rounds (the round control runs on the GPU). */
 } rlf_options;
 
 /* Mode of the reference-named drop-in entry points (data_processing, source_fitting, ...).
@@ -168,7 +172,8 @@ int rlf_obs_last_timing(rlf_observation *obs, double *ms4);
  *                                 of a sub-batch up to the first good fit of the round before, and
  *                                 every later round of a sub-batch without good fits,
  * stats[RLF_STAT_EXTRACT_SEQ_US]  device time of the sequential batch extraction kernel's launches
- *                                 (RLF_STAT_EXTRACT_PASSES of them), microseconds, CUDA events. */
+ *                                 (RLF_STAT_EXTRACT_PASSES of them), microseconds, CUDA events,
+ * stats[RLF_STAT_GRAPHS]          sub-batches launched as CUDA graphs (rlf_options.graphs). */
 enum {
   RLF_STAT_EXTRACT_PASSES = 0,
   RLF_STAT_EXTRACT_SINGLE = 1,
@@ -180,7 +185,8 @@ enum {
   RLF_STAT_EXTRACT_GAL_FIRST = 7,
   RLF_STAT_SKIPPED_GAL = 8,
   RLF_STAT_EXTRACT_SEQ_US = 9,
-  RLF_NSTATS = 10
+  RLF_STAT_GRAPHS = 10,
+  RLF_NSTATS = 11
 };
 int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
 

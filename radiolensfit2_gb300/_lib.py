@@ -37,7 +37,7 @@ class Options(C.Structure):
                 ("refit", C.c_int), ("verbose", C.c_int), ("start", PD), ("fit_precision", C.c_int),
                 ("rounds", C.c_int), ("reuse_obs", C.c_int),
                 ("board_wait_us", C.c_int), ("proposal", C.c_int), ("seq_facet_kb", C.c_int),
-                ("fit_ctas_per_sm", C.c_int)]
+                ("fit_ctas_per_sm", C.c_int), ("graphs", C.c_int)]
 
 
 _lib = None

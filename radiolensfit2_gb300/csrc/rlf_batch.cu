@@ -540,7 +540,7 @@ __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(
 // that the channel constants are compile-time operands.  Single-run items (SIMPLE) are called by
 // all lanes of a warp (run_deposit), a lane without an item with live = false and any valid t.
 template <int GAUSS, bool SIMPLE, int MODE, bool FIT>
-__device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, const RowF* __restrict__ rows,
+__device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, int ng, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
   constexpr bool POLY = MODE > 0;
@@ -566,7 +566,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
   const float invq = rw.q > 0.f ? 1.f / rw.q : 0.f;
   // wn^2 (u^2 + v^2) of channel c0 + k
 #define XB(k) (c_bch[c0 + (k)].wn2 * rw.q)
-  for (int j = 0; j < b.n_gal; ++j) {
+  for (int j = 0; j < ng; ++j) {
     const SeqGal s = sg[j];
     const GalF& g = s.g;
     const bool apply = FIT && s.apply;
@@ -711,7 +711,7 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
 // run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).  Called by all
 // lanes of a warp, as seq_item's single-run items.
 template <int GAUSS, int MODE, bool FIT>
-__device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const RowF* __restrict__ rows,
+__device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, int ng, const RowF* __restrict__ rows,
                                           const float2* __restrict__ data, const float2* __restrict__ sky,
                                           const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, uint16_t* d1cache,
                                           float2* acc) {
@@ -736,7 +736,7 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, const Ro
   const float uu = rw.u_hi * rw.u_hi, vv = rw.v_hi * rw.v_hi;
   const float invq = rw.q > 0.f ? 1.f / rw.q : 0.f;
   const float xq = c_chunk[ci].wn2c * rw.q;
-  for (int j = 0; j < b.n_gal; ++j) {
+  for (int j = 0; j < ng; ++j) {
     const SeqGal s = sg[j];
     const GalF& g = s.g;
     const bool apply = FIT && s.apply;
@@ -824,14 +824,19 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
                                                  align16((size_t)b.n_gal * sizeof(SeqGal)));
   uint16_t* d1cache = reinterpret_cast<uint16_t*>(dcache + (size_t)b.n_sizes * kSeqThreads);
   const int tid = threadIdx.x;
+  // galaxies [j0, n_gal) of the unit take part (device round control)
+  if (b.ctl && b.ctl[1]) return;
+  const int j0 = b.ctl ? b.ctl[0] : 0;
+  const int ng = b.n_gal - j0;
   for (int i = tid; i < 2 * b.total_cells; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
-  for (int i = tid; i < b.n_gal; i += blockDim.x) {
+  for (int i = tid; i < ng; i += blockDim.x) {
     SeqGal s;
+    const int gi = j0 + i;
     const bool has_fit = b.fit != nullptr;
-    s.g = load_gal(b.gals[i], has_fit ? &b.fit[i].e1 : nullptr, has_fit ? &b.fit[i].error : nullptr);
-    s.fidx = b.fidx[i];
-    s.off = b.foff[i];
-    s.apply = has_fit && b.fit[i].error == 0;
+    s.g = load_gal(b.gals[gi], has_fit ? &b.fit[gi].e1 : nullptr, has_fit ? &b.fit[gi].error : nullptr);
+    s.fidx = b.fidx[gi];
+    s.off = b.foff[gi];
+    s.apply = has_fit && b.fit[gi].error == 0;
     sg[i] = s;
   }
   __syncthreads();
@@ -843,15 +848,15 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
   // even out the end of the launch.  The general items (rare; a deposit per run of channels each)
   // come in chunks of 32 whose lane l takes item l * chunks + c of the list, so that the rows of a
   // warp lie far apart in uv and their deposits rarely meet in a cell.
-  const int ng = b.n_simple[1];
-  const int gch = (ng + 31) / 32;
+  const int ngen = b.n_simple[1];
+  const int gch = (ngen + 31) / 32;
   while (true) {
     int c = 0;
     if (lane == 0) c = atomicAdd(&b.queue[1], 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= gch) break;
     const int k = lane * gch + c;
-    if (k < ng) seq_item<GAUSS, false, MODE, FIT>(b.items[total - ng + k], true, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    if (k < ngen) seq_item<GAUSS, false, MODE, FIT>(b.items[total - ngen + k], true, n_rows, nch, ng, rows, data, sky, b, sg, dcache, acc);
   }
   // the two-run and single-run items: 32 consecutive items of the list (neighbours in uv) at a time
   if (MODE > 0) {
@@ -862,7 +867,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base >= nt) break;
       const int q = base + lane;
-      seq_item2<GAUSS, MODE, FIT>(b.items2[min(q, nt - 1)], q < nt, n_rows, rows, data, sky, b, sg, dcache, d1cache, acc);
+      seq_item2<GAUSS, MODE, FIT>(b.items2[min(q, nt - 1)], q < nt, n_rows, ng, rows, data, sky, b, sg, dcache, d1cache, acc);
     }
   }
   while (true) {
@@ -871,7 +876,7 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= ns) break;
     const int q = base + lane;
-    seq_item<GAUSS, true, MODE, FIT>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, rows, data, sky, b, sg, dcache, acc);
+    seq_item<GAUSS, true, MODE, FIT>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, ng, rows, data, sky, b, sg, dcache, acc);
   }
   __syncthreads();
   double2* out = partial + (size_t)blockIdx.x * b.total_cells;
@@ -922,6 +927,7 @@ __global__ void k_finalize_seq(SeqBatch b, int ctas, const double2* __restrict__
                                double len, FacetOut out) {
   const int slot = blockIdx.x;
   if (slot >= b.n_gal) return;
+  if (b.ctl && (b.ctl[1] || slot < b.ctl[0])) return;  // converged, or a galaxy before this round's first
   const int F = b.facet[slot], off = b.foff[slot];
   const int nc = F * F;
   const double inc = 2 * len / F;

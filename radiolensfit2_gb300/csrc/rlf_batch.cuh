@@ -61,6 +61,9 @@ int launch_row_order(int n_rows, const double* uu, const double* vv, double inv_
 
 struct SeqBatch {
   int n_gal;
+  const int* ctl;             // device round control of the unit, or nullptr: ctl[0] = j0, the first
+                              // galaxy taking part in this round (the earlier ones keep their
+                              // facets and fits); ctl[1] != 0: the unit has converged, skip
   const GalaxyParams* gals;   // [n_gal] in catalogue order
   const FitOut* fit;          // [n_gal] fits of the previous round, whose model differences
                               // (fitted - round) are removed from every later galaxy's facet; or

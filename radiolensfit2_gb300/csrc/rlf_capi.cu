@@ -119,7 +119,7 @@ struct DevBuf {
 
 struct Lib {
   cudaStream_t st = nullptr;
-  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0, 0, 0, 0};
+  rlf_options opt{RLF_F64, 1, 0, 1, 0, nullptr, RLF_F64, 0, 0, 0, 0, 0, 0, 0};
   // scratch for the per-function entry points
   DevBuf<double> d0, d1, d2, d3, d4, d5, d6, d7;
   DevBuf<double2> c0, c1;
@@ -296,7 +296,12 @@ struct PhaseTimer {
     RLF_CUDA(cudaEventCreate(&e));
     ev.push_back(e);
     label.push_back(lab);
-    RLF_CUDA(cudaEventRecord(e, st));
+    // inside a stream capture the record becomes a graph node that records the event when the
+    // graph runs (an external record), so the phase times stay measurable
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RLF_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusActive) RLF_CUDA(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
+    else RLF_CUDA(cudaEventRecord(e, st));
     return 0;
   }
   // ms3[0..2]: extract (the k_extract_seq launches included), fit, remove; seq_ms: the
@@ -315,6 +320,44 @@ struct PhaseTimer {
   }
   ~PhaseTimer() { for (auto e : ev) cudaEventDestroy(e); }
 };
+
+// Device round control of a sub-batch (SeqBatch::ctl): ctl[0] = j0, the first galaxy taking part in
+// the round, ctl[1] = converged.  k_round_begin marks the galaxies the round fits and counts the
+// round's work; k_round_end, after a round's fit, moves j0 to the first galaxy whose facet can still
+// change (a galaxy before it was good in this round or the one before) or marks the unit converged.
+// The host never waits between rounds.  dstats: RLF_STAT_* counters of the pass.
+__global__ void k_round_begin(int bn, int rd, const int* __restrict__ ctl, int* __restrict__ active,
+                              long long* __restrict__ dstats) {
+  const int done = ctl[1], j0 = ctl[0];
+  for (int i = threadIdx.x; i < bn; i += blockDim.x) active[i] = !done && i >= j0;
+  if (threadIdx.x == 0 && !done) {
+    dstats[RLF_STAT_EXTRACT_PASSES] += 1;
+    dstats[RLF_STAT_EXTRACT_GAL] += bn - j0;
+    if (rd == 0) dstats[RLF_STAT_EXTRACT_GAL_FIRST] += bn - j0;
+    dstats[RLF_STAT_FITTED] += bn - j0;
+  }
+}
+__global__ void k_round_end(int bn, int rd, int nr, const FitOut* __restrict__ out, int* __restrict__ good_prev,
+                            int* __restrict__ ctl, long long* __restrict__ dstats) {
+  __shared__ int first;
+  if (ctl[1]) return;
+  const int j0 = ctl[0];
+  if (threadIdx.x == 0) first = bn;
+  __syncthreads();
+  for (int k = j0 + threadIdx.x; k < bn; k += blockDim.x)
+    if (out[k].error == 0 || good_prev[k]) atomicMin(&first, k);
+  __syncthreads();
+  for (int k = j0 + threadIdx.x; k < bn; k += blockDim.x) good_prev[k] = out[k].error == 0;
+  if (threadIdx.x == 0) {
+    if (first == bn) {
+      ctl[1] = 1;
+      dstats[RLF_STAT_SKIPPED_GAL] += (long long)bn * (nr - 1 - rd);
+    } else {
+      ctl[0] = first;
+      dstats[RLF_STAT_SKIPPED_GAL] += first;
+    }
+  }
+}
 
 // galaxies whose fit differs between two rounds (ellipticity by more than tol, or the error flag)
 __global__ void k_count_changed(int n, const FitOut* a, const FitOut* b, double tol, unsigned long long* count) {
@@ -462,6 +505,14 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     RLF_OK(bnewton.ensure(max_unit));
     RLF_OK(bdone.ensure(1));
   }
+  // device round control of the sub-batches (k_round_begin / k_round_end)
+  DevBuf<int> dctl, dactive, dgoodp;
+  DevBuf<long long> dstats;
+  RLF_OK(dctl.ensure(2));
+  RLF_OK(dactive.ensure(max_unit));
+  RLF_OK(dgoodp.ensure(max_unit));
+  RLF_OK(dstats.ensure(RLF_NSTATS));
+  RLF_CUDA(cudaMemsetAsync(dstats.p, 0, RLF_NSTATS * sizeof(long long), st));
   if (batched && rounds > 1) {
     RLF_OK(dprev.ensure(std::min(n, max_unit)));
     RLF_OK(dchanged.ensure(1));
@@ -489,6 +540,17 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     RLF_OK(launch_row_table(ob->n_rows, ob->uu.p, ob->vv.p, ob->ww.p, ob->rows.p, st));
   }
   PhaseTimer pt;
+  // the sub-batches' executable graphs, destroyed once the stream has run them
+  std::vector<cudaGraphExec_t> execs;
+  struct ExecRelease {
+    std::vector<cudaGraphExec_t>& v;
+    cudaStream_t s;
+    ~ExecRelease() {
+      if (v.empty()) return;
+      cudaStreamSynchronize(s);
+      for (auto e : v) cudaGraphExecDestroy(e);
+    }
+  } exec_release{execs, st};
   RLF_OK(pt.mark(-1, st));
   for (size_t ui = 0; ui < units.size(); ++ui) {
     const Unit& u = units[ui];
@@ -556,47 +618,54 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       RLF_OK(launch_classify_items(n_items, sb, ob->items.p, ob->items2.p, ob->item_count.p, st));
     }
     const int nr = u.seq ? rounds : 1;
+    // CUDA graph of the sub-batch: every round (round control, extraction, finalisation, proposal,
+    // fit) and the removal are captured from the stream and launched as one graph, the host never
+    // waiting within the sub-batch (rlf_options.graphs)
+    const bool graph = u.seq && opt.graphs && !facets_out;
+    if (graph) RLF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the
     // fitted - round model differences of round r's good fits among the galaxies before k, round r
     // with those of round r-1 (none before round 1); a good fit's difference moves between rounds,
     // a bad fit's is zero.  So galaxy k keeps its facet and fit unless a galaxy before it was good
     // in round r or r-1: the next round starts at the first such galaxy (it is extracted again for
     // its model difference), and none means the unit has converged.
-    int j0 = 0;
-    std::vector<char> good_prev(u.seq ? bn : 0, 0);
+    if (u.seq) {
+      RLF_CUDA(cudaMemsetAsync(dctl.p, 0, 2 * sizeof(int), st));
+      RLF_CUDA(cudaMemsetAsync(dgoodp.p, 0, (size_t)bn * sizeof(int), st));
+    }
     for (int rd = 0; rd < nr; ++rd) {
-      const int bj = b0 + j0, bk = bn - j0;
+      // a sequential unit runs all its rounds with device round control (the galaxies before ctl[0]
+      // keep their facets and fits; a converged unit's remaining rounds do nothing); a single galaxy
+      // is one round
       SeqBatch sr = sb;
       FacetBatch fr = fb;
       FacetOut fq = fo;
-      fq.offset = doff.p + j0;
-      fq.ncoords = dnc.p + bj;
-      fr.n_gal = bk;
-      fr.offset = doff.p + j0;
-      fr.count = dnc.p + bj;
-      fr.rprior = dprior.p + (size_t)bj * kMaxNodes;
-      fr.start = (opt.start || learned) ? dstart.p + (size_t)3 * bj : nullptr;
-      fr.out = dout.p + bj;
+      fq.offset = doff.p;
+      fq.ncoords = dnc.p + b0;
+      fr.n_gal = bn;
+      fr.offset = doff.p;
+      fr.count = dnc.p + b0;
+      fr.rprior = dprior.p + (size_t)b0 * kMaxNodes;
+      fr.start = (opt.start || learned) ? dstart.p + (size_t)3 * b0 : nullptr;
+      fr.out = dout.p + b0;
+      fr.active = u.seq ? dactive.p : nullptr;
       // ---- extraction
       if (u.seq) {
-        sr.n_gal = bk;
-        sr.gals = dg.p + bj;
-        sr.fidx = dfidx.p + bj;
-        sr.foff = dfoff.p + bj;
-        sr.facet = dfac.p + bj;
-        sr.fit = rd == 0 ? nullptr : dout.p + bj;
-        ob->stats[RLF_STAT_EXTRACT_PASSES] += 1;
-        ob->stats[RLF_STAT_EXTRACT_GAL] += bk;
-        if (rd == 0) ob->stats[RLF_STAT_EXTRACT_GAL_FIRST] += bk;
+        sr.ctl = dctl.p;
+        sr.fit = rd == 0 ? nullptr : dout.p + b0;
+        k_round_begin<<<1, 256, 0, st>>>(bn, rd, dctl.p, dactive.p, dstats.p);
+        count_launch();
+        RLF_CUDA(cudaGetLastError());
         RLF_OK(pt.mark(kPhaseExtract, st));
         RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sr, opt.gaussian, seq_ctas,
                                   ob->bpartial.p, st));
         RLF_OK(pt.mark(kPhaseExtractSeq, st));
-        RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + bj, dsw.p + bj, ob->len, fq, st));
+        RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, ob->len, fq, st));
       } else {
         const int i = b0;
         const unsigned F = (unsigned)facets[i];
         ob->stats[RLF_STAT_EXTRACT_SINGLE] += 1;
+        ob->stats[RLF_STAT_FITTED] += 1;
         if (prec == kF64)
           RLF_OK(launch_extract_f64(o, ob->data64.p, ob->sky64.p, cache[i]->cell.p, dg.p + i, F, opt.gaussian,
                                     ob->partial.p, ob->n_part, st));
@@ -612,10 +681,10 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       // ---- fit
       if (learned) {
         static_assert(sizeof(GalaxyParams) % sizeof(double) == 0, "GalaxyParams holds whole doubles");
-        const double* flux = reinterpret_cast<const double*>(reinterpret_cast<const char*>(dg.p + bj) +
+        const double* flux = reinterpret_cast<const double*>(reinterpret_cast<const char*>(dg.p + b0) +
                                                              offsetof(GalaxyParams, flux));
-        RLF_OK(propose_starts(bk, doff.p + j0, dnc.p + bj, dfac.p + bj, gu, gv, dre, dim, sg, fprec == kMixed ? 1 : 0,
-                              flux, (int)(sizeof(GalaxyParams) / sizeof(double)), ob->len, dstart.p + (size_t)3 * bj,
+        RLF_OK(propose_starts(bn, doff.p, dnc.p + b0, dfac.p + b0, gu, gv, dre, dim, sg, fprec == kMixed ? 1 : 0,
+                              flux, (int)(sizeof(GalaxyParams) / sizeof(double)), ob->len, dstart.p + (size_t)3 * b0,
                               st));
       }
       const bool last = rd == nr - 1;
@@ -623,37 +692,24 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         RLF_CUDA(copy_async(dprev.p, dout.p + b0, bn * sizeof(FitOut), cudaMemcpyDeviceToDevice, st));
       RLF_CUDA(cudaMemsetAsync(dqueue.p, 0, sizeof(int), st));
       if (fr.board.slot) {
-        RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bk * sizeof(SampleSlot), st));
-        RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)bk * 2 * kBoardCap * sizeof(int), st));
-        RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)bk * sizeof(int), st));
+        RLF_CUDA(cudaMemsetAsync(bslot.p, 0, (size_t)bn * sizeof(SampleSlot), st));
+        RLF_CUDA(cudaMemsetAsync(bflag.p, 0, (size_t)bn * 2 * kBoardCap * sizeof(int), st));
+        RLF_CUDA(cudaMemsetAsync(bnewton.p, 0, (size_t)bn * sizeof(int), st));
         RLF_CUDA(cudaMemsetAsync(bdone.p, 0, sizeof(int), st));
       }
-      ob->stats[RLF_STAT_FITTED] += bk;
       // with the board, CTAs beyond the galaxy count start as helpers of the sampling grids
-      RLF_OK(fit_launch(fr, fprec, fr.board.slot ? grid_fit : std::min(grid_fit, bk), st));
+      RLF_OK(fit_launch(fr, fprec, fr.board.slot ? grid_fit : std::min(grid_fit, bn), st));
       if (u.seq && last && nr > 1) {
         k_count_changed<<<(bn + 127) / 128, 128, 0, st>>>(bn, dprev.p, dout.p + b0, 1e-9, dchanged.p);
         count_launch();
         RLF_CUDA(cudaGetLastError());
       }
-      RLF_OK(pt.mark(kPhaseFit, st));
       if (u.seq && !last) {
-        std::vector<FitOut> h(bk);
-        RLF_CUDA(copy_async(h.data(), dout.p + bj, bk * sizeof(FitOut), cudaMemcpyDeviceToHost, st));
-        RLF_CUDA(cudaStreamSynchronize(st));
-        int first = bn;
-        for (int k = 0; k < bk; ++k) {
-          const char good = h[k].error == 0;
-          if (first == bn && (good || good_prev[j0 + k])) first = j0 + k;
-          good_prev[j0 + k] = good;
-        }
-        if (first == bn) {
-          ob->stats[RLF_STAT_SKIPPED_GAL] += (long long)bn * (nr - 1 - rd);
-          break;
-        }
-        j0 = first;
-        ob->stats[RLF_STAT_SKIPPED_GAL] += j0;
+        k_round_end<<<1, 256, 0, st>>>(bn, rd, nr, dout.p + b0, dgoodp.p, dctl.p, dstats.p);
+        count_launch();
+        RLF_CUDA(cudaGetLastError());
       }
+      RLF_OK(pt.mark(kPhaseFit, st));
     }
     if (facets_out) {
       // extraction only: hand the packed facets of this unit back as doubles
@@ -690,12 +746,26 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         RLF_OK(launch_remove_mixed(o, ob->data32.p, ob->sky32.p, dg.p + i, e12, err, opt.gaussian, st));
     }
     RLF_OK(pt.mark(kPhaseRemove, st));
+    if (graph) {
+      cudaGraph_t gr = nullptr;
+      RLF_CUDA(cudaStreamEndCapture(st, &gr));
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&ex, gr, 0);
+      cudaGraphDestroy(gr);
+      if (ie != cudaSuccess) { fprintf(stderr, "rlf: cudaGraphInstantiate: %s\n", cudaGetErrorString(ie)); return (int)ie; }
+      execs.push_back(ex);
+      RLF_CUDA(cudaGraphLaunch(ex, st));
+      ob->stats[RLF_STAT_GRAPHS] += 1;
+    }
   }
   if (!facets_out) RLF_OK(dout.download(out.data(), n, st));
   unsigned long long changed = 0;
   if (dchanged.p) RLF_CUDA(copy_async(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
+  long long hstats[RLF_NSTATS];
+  RLF_CUDA(copy_async(hstats, dstats.p, sizeof(hstats), cudaMemcpyDeviceToHost, st));
   RLF_CUDA(cudaStreamSynchronize(st));
   ob->stats[RLF_STAT_CHANGED] += (long long)changed;
+  for (int k = 0; k < RLF_NSTATS; ++k) ob->stats[k] += hstats[k];
   if (ms3) {
     double seq_ms = 0;
     pt.sum(ms3, &seq_ms);

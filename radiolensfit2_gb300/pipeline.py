@@ -119,7 +119,7 @@ class DeviceObservation:
     def process(self, cat: Catalogue, *, batch: int = 1, refit: bool = True, gaussian: int = 0,
                 start=None, verbose: int = 0, fit_precision: int = _lib.RLF_F64, rounds: int = 0,
                 board_wait_us: int = 0, proposal: int = 0, seq_facet_kb: int = 0,
-                fit_ctas_per_sm: int = 0) -> ProcessResult:
+                fit_ctas_per_sm: int = 0, graphs: int = 0) -> ProcessResult:
         ro, pro = _d(K.ro_grid())
         arrs = [_d(x) for x in (cat.flux, cat.scale, cat.l, cat.m)]
         opt = _lib.Options()
@@ -134,6 +134,7 @@ class DeviceObservation:
         opt.proposal = int(proposal)
         opt.seq_facet_kb = int(seq_facet_kb)
         opt.fit_ctas_per_sm = int(fit_ctas_per_sm)
+        opt.graphs = int(graphs)
         st = None
         if start is not None:
             st = np.ascontiguousarray(start, dtype=np.float64).reshape(-1)
@@ -147,7 +148,7 @@ class DeviceObservation:
         self.lib.rlf_obs_last_timing(self.h, ms)
         names = ("extract_passes", "extract_single", "remove_batches", "remove_single", "fitted",
                  "extract_gal", "changed", "extract_gal_first", "skipped_gal",
-                 "extract_seq_us")  # RLF_NSTATS entries
+                 "extract_seq_us", "graphs")  # RLF_NSTATS entries
         sv = (C.c_longlong * len(names))()
         self.lib.rlf_obs_last_stats(self.h, sv)
         stats = dict(zip(names, (int(x) for x in sv)))

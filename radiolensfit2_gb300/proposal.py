@@ -7,7 +7,7 @@ this module drives them:
 * ``training_set`` simulates galaxies with the project's own visibility simulator on an array
   (rlf_obs_simulate + rlf_obs_sky_model) and extracts their facets with the batched extraction
   (rlf_obs_extract), which the library resamples to 64 x 64 x 4 images in the network's device
-  store; targets are the true (sheared) ellipticity and ln scalelength;
+  store; targets are where the plain fit's simplex ends (its maximum) and ln scalelength;
 * ``train`` runs Adam over the store (rlf_cnn_train_step) and keeps the parameters of the best
   validation loss;
 * ``load`` hands a trained network to the pipeline (rlf_proposal_set_params), after which

@@ -88,6 +88,10 @@ WORKLOADS = {
     # data and sky model, larger than the 129 MB L2), 64 galaxies
     "mid_128ant_16ch": dict(n_ant=128, ha_hours=1.0, dt_s=60.0, n_ch=16, n_gal=64,
                             fmin=10.0, fmax=200.0, g=(0.03, -0.02)),
+    # profiling case with the full-scale channel layout (64 channels): 62M visibilities (1 GB of
+    # FP32 data and sky model, larger than the 129 MB L2), 64 galaxies of the full-scale flux range
+    "mid_128ant_64ch": dict(n_ant=128, ha_hours=0.5, dt_s=30.0, n_ch=64, n_gal=64,
+                            fmin=5.0, fmax=200.0, g=(0.02, 0.01)),
 }
 
 ARRAY_SEED, CATALOGUE_SEED, NOISE_SEED = 1, 2, 3
