@@ -214,8 +214,9 @@ int rlf_obs_remove(rlf_observation *obs, int n_gal, const double *flux, const do
  * galaxy_fitting.c:59-65).  A convolutional network (4 convolutions 3x3 stride 2 of 32 channels on
  * bf16 tensor cores, FP32 accumulation, a dense head) reads a 64 x 64 x 4 resampling of a galaxy's
  * facet (visibility / flux re and im, cell mask, cell SNR) and proposes (e1, e2, ln r, ln sigma);
- * a galaxy with sigma <= 0.05 starts its fit at (e1, e2) with step 2 sigma (at least 0.02), the
- * others at the reference's (0, 0) with step 0.1; the fit stays the judge.  Parameters:
+ * a galaxy with sigma <= max_sigma (rlf_proposal_set_max_sigma, default 0.05) starts its fit at
+ * (e1, e2) with step 2 sigma (at least 0.02), the others at the reference's (0, 0) with step 0.1;
+ * the fit stays the judge.  Parameters:
  * rlf_cnn_param_count() floats, per convolution W[32][9 cin] (k = (3 ky + kx) cin + ci) and b[32],
  * then the head's W[4][512] (feature (4 y + x) 32 + c) and b[4]. */
 typedef struct rlf_cnn rlf_cnn;
@@ -244,6 +245,9 @@ int rlf_cnn_train_step(rlf_cnn *cnn, const int *idx, int n, float lr, float *los
 int rlf_cnn_predict(rlf_cnn *cnn, int first, int n, float *out);
 /* the network rlf_obs_process / data_processing use with rlf_options.proposal (NULL unloads) */
 int rlf_proposal_set_params(const float *params);
+/* the gate of the loaded network: galaxies whose predicted sigma exceeds max_sigma (default 0.05)
+ * keep the reference's start */
+int rlf_proposal_set_max_sigma(float max_sigma);
 
 /* -------- gridding without device allocation --------
  * No counterpart in the reference.  The gridding of gridding_visibilities (evaluate_uv_grid.c),

@@ -102,6 +102,7 @@ def load():
         "rlf_cnn_train_step": (C.c_int, [C.c_void_p, PI, C.c_int, C.c_float, PF]),
         "rlf_cnn_predict": (C.c_int, [C.c_void_p, C.c_int, C.c_int, PF]),
         "rlf_proposal_set_params": (C.c_int, [PF]),
+        "rlf_proposal_set_max_sigma": (C.c_int, [C.c_float]),
         # reference-named drop-in entry points
         "facet_size": (C.c_uint, [D, D]),
         "evaluate_uv_grid_size": (C.c_uint, [C.c_int, C.c_int, D, PD, C.c_uint, C.c_uint, PD, PD, C.c_uint, PU8]),
@@ -157,4 +158,5 @@ EXPORTED = [
     "rlf_cnn_param_count", "rlf_cnn_create", "rlf_cnn_destroy",
     "rlf_cnn_set_params", "rlf_cnn_get_params", "rlf_cnn_store_facets", "rlf_cnn_set_targets",
     "rlf_cnn_read_images", "rlf_cnn_set_images", "rlf_cnn_grads", "rlf_cnn_train_step", "rlf_cnn_predict", "rlf_proposal_set_params",
+    "rlf_proposal_set_max_sigma",
 ]

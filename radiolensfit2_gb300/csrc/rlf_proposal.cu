@@ -577,11 +577,11 @@ __global__ void k_unpack_dw(const float* __restrict__ dwt, int k, float* __restr
 
 // proposal (e1, e2, step) for the fit from the head's outputs: e clamped to |e| <= 0.7 (the fit's
 // objective is finite for |e|^2 < 0.65, likelihood.c:87-100), step 2 sigma in [0.02, 0.1].  A galaxy
-// whose predicted sigma exceeds kPropMaxSigma keeps the reference's start (0, 0) with step 0.1: for
+// whose predicted sigma exceeds max_sigma keeps the reference's start (0, 0) with step 0.1: for
 // the unresolved, noise-dominated galaxies the proposal carries no information beyond the prior,
 // and a different start only moves the end of the simplex on a flat likelihood.
-constexpr float kPropMaxSigma = 0.05f;
-__global__ void k_to_start(int n, const float* __restrict__ out, double* __restrict__ start) {
+constexpr float kPropMaxSigma = 0.05f;  // default gate (rlf_proposal_set_max_sigma)
+__global__ void k_to_start(int n, const float* __restrict__ out, float max_sigma, double* __restrict__ start) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const float* o = out + (size_t)g * kHeadOut;
@@ -593,7 +593,7 @@ __global__ void k_to_start(int n, const float* __restrict__ out, double* __restr
     e2 *= s;
   }
   const float sig = __expf(fminf(fmaxf(o[3], -5.f), 0.5f));
-  const bool use = sig <= kPropMaxSigma && isfinite(e1) && isfinite(e2);
+  const bool use = sig <= max_sigma && isfinite(e1) && isfinite(e2);
   start[3 * g + 0] = use ? (double)e1 : 0.0;
   start[3 * g + 1] = use ? (double)e2 : 0.0;
   start[3 * g + 2] = use ? (double)fminf(fmaxf(2.f * sig, 0.02f), 0.1f) : 0.1;
@@ -657,6 +657,7 @@ struct DBuf {
 struct Cnn {
   int max_batch = 0;
   int capacity = 0;
+  float max_sigma = kPropMaxSigma;  // proposals with a larger predicted sigma keep the reference start
   cudaStream_t st = nullptr;
   int step = 0;
   DBuf<float> params, grads, m, v, loss, out, dout, targets, dwt;
@@ -822,7 +823,7 @@ static int propose_t(Cnn& c, int n, const int* offset, const int* count, const i
                                         flux_stride, len, c.act[0].p);
     RLF_P_OK(check_p("k_resample"));
     RLF_P_OK(c.forward(k));
-    k_to_start<<<(k + 127) / 128, 128, 0, c.st>>>(k, c.out.p, start + 3 * (size_t)i0);
+    k_to_start<<<(k + 127) / 128, 128, 0, c.st>>>(k, c.out.p, c.max_sigma, start + 3 * (size_t)i0);
     RLF_P_OK(check_p("k_to_start"));
   }
   RLF_P_CUDA(cudaEventRecord(ev, c.st));
@@ -1000,6 +1001,13 @@ int rlf_cnn_predict(rlf_cnn* h, int first, int n, float* out) {
     RLF_P_CUDA(cudaStreamSynchronize(c.st));
   }
   return c.status();
+}
+
+int rlf_proposal_set_max_sigma(float max_sigma) {
+  std::lock_guard<std::mutex> lock(rlf::g_prop_mu);
+  if (!rlf::g_prop || !(max_sigma > 0.f)) return 1;
+  rlf::g_prop->max_sigma = max_sigma;
+  return 0;
 }
 
 int rlf_proposal_set_params(const float* params) {

@@ -212,15 +212,22 @@ def save(params, path=WEIGHTS, **meta):
     np.savez(path, params=np.asarray(params, np.float32), **{k: np.asarray(v) for k, v in meta.items()})
 
 
-def load(path=WEIGHTS) -> np.ndarray:
-    """Load trained parameters and hand them to the pipeline (rlf_proposal_set_params)."""
+def load(path=WEIGHTS, max_sigma: float | None = None) -> np.ndarray:
+    """Load trained parameters and hand them to the pipeline (rlf_proposal_set_params); max_sigma:
+    the gate above which a galaxy keeps the reference's start (default: the stored one, else 0.05)."""
     if not os.path.exists(path):
         raise FileNotFoundError(f"{path}: no trained proposal network")
     p = np.ascontiguousarray(np.load(path)["params"], np.float32)
     if p.size != param_count():
         raise ValueError("proposal parameters of another layout")
-    if _lib.load().rlf_proposal_set_params(p.ctypes.data_as(_lib.PF)):
+    lib = _lib.load()
+    if lib.rlf_proposal_set_params(p.ctypes.data_as(_lib.PF)):
         raise RuntimeError("rlf_proposal_set_params failed")
+    if max_sigma is None:
+        z = np.load(path)
+        max_sigma = float(z["max_sigma"]) if "max_sigma" in z else 0.05
+    if lib.rlf_proposal_set_max_sigma(float(max_sigma)):
+        raise RuntimeError("rlf_proposal_set_max_sigma failed")
     return p
 
 

@@ -24,19 +24,33 @@ from . import proposal as PR, synth
 from .pipeline import DeviceObservation
 
 
-def evaluate(obs, n_gal, seed=11, batch=1000, fmin=10.0, fmax=200.0, g=(0.03, -0.02)):
+def evaluate(obs, n_gal, seed=11, batch=1000, fmin=10.0, fmax=200.0, g=(0.03, -0.02), gates=(0.02, 0.03, 0.05)):
+    """Held-out galaxies through the batched pipeline with the reference's start and with the
+    proposal at each gate (galaxies whose predicted sigma exceeds the gate keep the reference's
+    start)."""
+    from . import _lib
     cat = synth.make_catalogue(n_gal, fmin, fmax, g=g, seed=seed)
     dev = DeviceObservation(obs)
     dev.simulate(cat, obs.sigma, seed=seed)
     dev.sky_model(cat)
     dev.snapshot()
-    runs = {}
-    for name, prop in (("plain_start", 0), ("learned_start", 1)):
+    dev.restore()
+    t0 = time.time()
+    base = dev.process(cat, batch=batch, refit=True, proposal=0)
+    base_wall = time.time() - t0
+    out = {}
+    for gate in gates:
+        _lib.load().rlf_proposal_set_max_sigma(float(gate))
         dev.restore()
         t0 = time.time()
-        r = dev.process(cat, batch=batch, refit=True, proposal=prop)
-        runs[name] = (r, time.time() - t0)
+        r = dev.process(cat, batch=batch, refit=True, proposal=1)
+        out[f"gate_{gate}"] = compare(n_gal, (base, base_wall), (r, time.time() - t0))
     dev.close()
+    return out
+
+
+def compare(n_gal, base, learned):
+    runs = {"plain_start": base, "learned_start": learned}
     a, b = runs["plain_start"][0].results, runs["learned_start"][0].results
     ok = (a["error"] == 0) & (b["error"] == 0)
     de = np.maximum(np.abs(a["e1"] - b["e1"]), np.abs(a["e2"] - b["e2"]))[ok]
@@ -69,7 +83,13 @@ def main():
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--workload", default="c2_ska_mid_32ch")
     ap.add_argument("--out", default=PR.WEIGHTS)
+    ap.add_argument("--eval-only", action="store_true", help="evaluate the parameters in --out on held-out galaxies")
     a = ap.parse_args()
+    if a.eval_only:
+        PR.load(a.out)
+        obs = synth.make_observation(**synth.WORKLOADS[a.workload])
+        print(json.dumps({"heldout": evaluate(obs, a.heldout)}), flush=True)
+        return
     n_val = max(256, a.train // 10)
     n_all = a.train + n_val
     t0 = time.time()

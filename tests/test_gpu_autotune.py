@@ -1,7 +1,9 @@
-"""The autotuner's candidate launch shapes: every candidate gives the FP64 path's results unchanged
-(the fit of a galaxy does not depend on how many thread blocks share an SM, and the FP64 path takes
-galaxies one at a time), the batched FP32 path stays within its accuracy against the FP64 path for
-every candidate, and the tuner returns one of the candidates with a timing for each."""
+"""The autotuner's candidate launch shapes: every candidate gives the FP64 path's results to 1e-12
+relative, with equal error flags and evaluation counts (the FP64 path takes galaxies one at a time;
+the number of fit thread blocks changes which block evaluates each sampling-grid point, and the
+results are not bit-identical across candidates), the batched FP32 path stays within its accuracy
+against the FP64 path for every candidate, and the tuner returns one of the candidates with a
+timing for each."""
 import numpy as np
 import pytest
 
@@ -28,8 +30,12 @@ def test_candidates_keep_f64_results_identical():
         if base is None:
             base = r
         else:
-            for k in ("e1", "e2", "var_e1", "var_e2", "maxL", "error", "nevals"):
+            for k in ("error", "nevals"):
                 assert np.array_equal(r[k], base[k]), (cand, k)
+            for k in ("e1", "e2", "var_e1", "var_e2", "maxL"):
+                d = np.max(np.abs(r[k] - base[k]) / np.maximum(np.abs(base[k]), 1e-3))
+                print(cand, k, f"{d:.1e}")
+                assert d < 1e-12, (cand, k, d)
     f64.close()
     mixed = DeviceObservation(case.obs, precision=_lib.RLF_MIXED, sigma2=case.sigma2, flag=case.flag)
     mixed.set_vis(case.data, sky)
