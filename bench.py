@@ -55,8 +55,9 @@ def parse():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--galaxies", type=int, default=0, help="catalogue size (0 = the workload's)")
     ap.add_argument("--window", type=int, default=500, help="galaxies per step (at most the catalogue)")
-    ap.add_argument("--proposal", default="auto", choices=["auto", "none"],
-                    help="learned simplex-start proposal: auto = the package's trained network when present")
+    ap.add_argument("--proposal", default="report", choices=["report", "on", "none"],
+                    help="learned simplex-start proposal: report = measured path with the reference's start, the "
+                         "proposal's effect measured on the prefix beside it; on = measured path with the proposal")
     ap.add_argument("--tune", default="auto", choices=["auto", "none"],
                     help="autotune the batched launch shapes on the first window before the warm-up")
     ap.add_argument("--batch", type=int, default=1000)
@@ -495,9 +496,11 @@ def main():
     # the learned proposal of the simplex starts (trained network shipped with the package)
     from radiolensfit2_gb300 import proposal as PR, autotune as AT
     use_prop = 0
-    prop_desc = "none (simplex start (0, 0), step 0.1)"
-    if args.proposal == "auto" and os.path.exists(PR.WEIGHTS):
+    prop_desc = "none (the reference's simplex start (0, 0), step 0.1)"
+    have_prop = args.proposal != "none" and os.path.exists(PR.WEIGHTS)
+    if have_prop:
         PR.load()
+    if args.proposal == "on" and have_prop:
         use_prop = 1
         prop_desc = "learned (radiolensfit2_gb300/proposal_weights.npz, rlf_options.proposal = 1)"
     # launch shapes tuned on the first window, from the snapshot (restored after every candidate)
@@ -583,15 +586,18 @@ def main():
     if rank == 0 and args.plain_prefix > 0:
         P = min(args.plain_prefix, cat.n)
         pre = cat.subset(range(P))
-        # the same prefix from the same data: learned+batched (the measured path), batched with the
+        # the same prefix from the same data: batched with the learned start, batched with the
         # reference's simplex start, and the plain one-galaxy-at-a-time fit
-        dev.restore()
-        rb = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds, proposal=use_prop,
-                         **shapes)
+        rl = None
+        if have_prop:
+            dev.restore()
+            rl = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds, proposal=1,
+                             **shapes)
         dev.restore()
         rn = dev.process(pre, batch=B, refit=True, fit_precision=fit_prec, rounds=args.rounds, **shapes)
         dev.restore()
         rp = dev.process(pre, batch=1, refit=True, fit_precision=fit_prec)
+        rb = rl if use_prop else rn  # the measured path
         bt, bn, pl = rb.results, rn.results, rp.results
         gpu_first = bt
 
@@ -609,13 +615,19 @@ def main():
                             "evals_per_galaxy": float(np.mean(pl["nevals"])),
                             "measured_path_on_prefix": {"value": P / (rb.ms[0] * 1e-3), "ms": rb.ms[0],
                                                         "evals_per_galaxy": float(np.mean(bt["nevals"]))},
-                            "batched_reference_start_on_prefix": {"value": P / (rn.ms[0] * 1e-3), "ms": rn.ms[0],
-                                                                  "evals_per_galaxy": float(np.mean(bn["nevals"]))},
                             "speedup_measured_path_vs_plain_same_prefix": rp.ms[0] / rb.ms[0],
                             "speedup_value_vs_plain": value / plain_rate,
-                            "abs_de_measured_vs_plain": dev_of(bt, pl),
-                            "abs_de_batched_reference_start_vs_plain": dev_of(bn, pl),
-                            "abs_de_learned_vs_reference_start": dev_of(bt, bn)}
+                            "abs_de_measured_vs_plain": dev_of(bt, pl)}
+        if rl is not None:
+            lr = rl.results
+            out["learned_proposal"] = {
+                "prefix_galaxies": P, "gate_max_sigma": 0.05,
+                "evals_per_galaxy": {"reference_start": float(np.mean(bn["nevals"])),
+                                     "learned_start": float(np.mean(lr["nevals"]))},
+                "ms": {"reference_start": rn.ms[0], "learned_start": rl.ms[0]},
+                "fit_ms": {"reference_start": rn.ms[2], "learned_start": rl.ms[2]},
+                "abs_de_learned_vs_reference_start": dev_of(lr, bn), "abs_de_learned_vs_plain": dev_of(lr, pl),
+                "in_measured_path": bool(use_prop)}
         if snr is not None:
             out["shear"].append(shear_block(pre, bt, snr[:P], "measured path, prefix"))
             out["shear"].append(shear_block(pre, pl, snr[:P], "plain, prefix"))

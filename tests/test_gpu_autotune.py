@@ -1,4 +1,4 @@
-"""The autotuner's candidate launch shapes: every candidate gives the FP64 path's results to 1e-12
+"""The autotuner's candidate launch shapes: every candidate gives the FP64 path's results to 1e-11
 relative, with equal error flags and evaluation counts (the FP64 path takes galaxies one at a time;
 the number of fit thread blocks changes which block evaluates each sampling-grid point, and the
 results are not bit-identical across candidates), the batched FP32 path stays within its accuracy
@@ -35,7 +35,7 @@ def test_candidates_keep_f64_results_identical():
             for k in ("e1", "e2", "var_e1", "var_e2", "maxL"):
                 d = np.max(np.abs(r[k] - base[k]) / np.maximum(np.abs(base[k]), 1e-3))
                 print(cand, k, f"{d:.1e}")
-                assert d < 1e-12, (cand, k, d)
+                assert d < 1e-11, (cand, k, d)
     f64.close()
     mixed = DeviceObservation(case.obs, precision=_lib.RLF_MIXED, sigma2=case.sigma2, flag=case.flag)
     mixed.set_vis(case.data, sky)
