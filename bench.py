@@ -60,6 +60,8 @@ def parse():
                          "proposal's effect measured on the prefix beside it; on = measured path with the proposal")
     ap.add_argument("--tune", default="auto", choices=["auto", "none"],
                     help="autotune the batched launch shapes on the first window before the warm-up")
+    ap.add_argument("--graphs", type=int, default=0, choices=[0, 1],
+                    help="capture each sub-batch's rounds and removal as one CUDA graph")
     ap.add_argument("--batch", type=int, default=1000)
     ap.add_argument("--rounds", type=int, default=0,
                     help="extraction + fit rounds per batch (0 = library default)")
@@ -509,6 +511,8 @@ def main():
         a0, b0, _ = plan[0]
         shapes, tune_ms = AT.tune(dev, cat.subset(range(a0, b0)), batch=B, fit_precision=fit_prec,
                                   rounds=args.rounds, proposal=use_prop)
+    if args.graphs:
+        shapes = dict(shapes, graphs=1)
     # the first walk over the catalogue: its results (shear) and device time (whole-job throughput)
     full = np.zeros(cat.n, RESULT_DTYPE)
     seen = np.zeros(cat.n, bool)
