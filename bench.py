@@ -172,7 +172,8 @@ def shear_block(cat, res, snr, label):
     g1, g2 = cat.g
     return {"fit": label, "g_true": [g1, g2], "g": [est.g1, est.g2], "g_err": [est.g1_err, est.g2_err],
             "bias": [est.g1 - g1, est.g2 - g2], "galaxies_used": est.n_used,
-            "within_1sigma": bool(abs(est.g1 - g1) <= est.g1_err and abs(est.g2 - g2) <= est.g2_err)}
+            "within_1sigma": bool(abs(est.g1 - g1) <= est.g1_err and abs(est.g2 - g2) <= est.g2_err)
+            if est.n_used else None}
 
 
 def cpu_sample_size(args, obs):

@@ -168,6 +168,21 @@ struct FwdPolicy {
     const int per = s.out_side * s.out_side;
     const int n = live ? m / per : 0, r = live ? m - n * per : 0;
     const int oy = r / s.out_side, ox = r - oy * s.out_side;
+    if (s.cin % 8 == 0) {
+      // 8 consecutive K of one tap are 8 consecutive channels: one 16-byte load (or zero padding)
+      for (int kg = 0; kg < kChunkK / 8; ++kg) {
+        const int k = k0 + kg * 8;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (live && k < 9 * s.cin) {
+          const int tap = k / s.cin, ci = k - tap * s.cin;
+          const int iy = 2 * oy - 1 + tap / 3, ix = 2 * ox - 1 + tap % 3;
+          if (iy >= 0 && iy < s.in_side && ix >= 0 && ix < s.in_side)
+            v = *reinterpret_cast<const uint4*>(x + (((size_t)n * s.in_side + iy) * s.in_side + ix) * s.cin + ci);
+        }
+        put8_raw(tile, row, kg, kTileM, v);
+      }
+      return;
+    }
     for (int kg = 0; kg < kChunkK / 8; ++kg) {
       float v[8];
 #pragma unroll

@@ -107,6 +107,10 @@ def estimate_shear(me1, me2, err1, err2, onedvar, snr=None, *, snr_min=10.0, boo
     var = np.asarray(onedvar, float)
     snr = np.full(len(me1), np.inf) if snr is None else np.asarray(snr, float)
     kept, bad = reference_selection(err1, err2, var, snr, snr_min)
+    if len(kept) < 2:  # no pair left: no estimate (the reference's script fails on an empty sample)
+        nan = float("nan")
+        return ShearEstimate(g1=nan, g2=nan, g1_err=nan, g2_err=nan, n_used=int(len(kept)), n_rejected=int(bad),
+                             shape_noise=nan)
     e1, e2, v = me1[kept], me2[kept], var[kept]
     pe = prior_ellipticity(e1, e2) if prior_weighted_moments else None
     m1, m2 = np.average(e1, weights=pe), np.average(e2, weights=pe)

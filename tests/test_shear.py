@@ -55,3 +55,9 @@ def test_reference_selection_rules():
     v[9] = 0.0   # the last row, odd: the reference deletes row 7 instead of row 8
     kept, bad = shear.reference_selection(np.full(n, 0.1), np.full(n, 0.1), v, np.full(n, 50.0))
     assert kept.tolist() == [0, 1, 2, 3, 4, 5, 6, 8] and bad == 1
+
+
+def test_no_pair_left_gives_no_estimate():
+    n = 6
+    est = shear.estimate_shear(np.zeros(n), np.zeros(n), np.full(n, 0.1), np.full(n, 0.1), np.zeros(n))
+    assert est.n_used == 0 and np.isnan(est.g1) and np.isnan(est.g2)
