@@ -361,6 +361,7 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample, gpu_first):
     de = np.maximum(np.abs(res[ok, 0] - g["e1"][ok]), np.abs(res[ok, 1] - g["e2"][ok]))
     parity = {"galaxies": int(n_sample), "good_in_both": int(ok.sum()),
               "error_flags_equal": bool(np.array_equal(res[:, 2].astype(int), g["error"])),
+              "error_flags_differ": int(np.sum(res[:, 2].astype(int) != g["error"])),
               "max_abs_de": float(de.max()) if de.size else None,
               "frac_le_1e-4": float(np.mean(de <= 1e-4)) if de.size else None,
               "gpu_path": "batched mixed-precision, both passes, same data"}

@@ -537,18 +537,22 @@ __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(
 // one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order.
 // MODE 0: exact per-channel profiles; 1: the profiles from the chunk polynomial, one profile
 // evaluation per galaxy and chunk; 2: as 1 for an observation of exactly one 16-channel chunk, so
-// that the channel constants are compile-time operands.  Single-run items (SIMPLE) are called by
-// all lanes of a warp (run_deposit), a lane without an item with live = false and any valid t.
-template <int GAUSS, bool SIMPLE, int MODE, bool FIT>
+// that the channel constants are compile-time operands; 3: as 1 for 2-4 full 16-channel chunks,
+// the item's chunk CI a compile-time constant when the caller knows it (CI >= 0: the channel
+// constants are then operands of the arithmetic instructions, not loads of a dynamic index), CI =
+// -1 for any chunk.  Single-run items (SIMPLE) are called by all lanes of a warp (run_deposit), a
+// lane without an item with live = false and any valid t.
+template <int GAUSS, bool SIMPLE, int MODE, bool FIT, int CI = -1>
 __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, int ng, const RowF* __restrict__ rows,
                                          const float2* __restrict__ data, const float2* __restrict__ sky,
                                          const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, float2* acc) {
   constexpr bool POLY = MODE > 0;
   constexpr bool ONE = MODE == 2;
+  constexpr bool FIXED = CI >= 0;
   const int tid = threadIdx.x;
-  const int r = ONE ? t : t % n_rows;
-  const int c0 = ONE ? 0 : (t / n_rows) * kChunk;
-  const int nk = ONE ? kChunk : min(kChunk, nch - c0);
+  const int r = ONE ? t : (FIXED ? t - CI * n_rows : t % n_rows);
+  const int c0 = ONE ? 0 : (FIXED ? CI * kChunk : (t / n_rows) * kChunk);
+  const int nk = (ONE || FIXED) ? kChunk : min(kChunk, nch - c0);
   const RowF rw = rows[r];
   float pr[kChunk], pi[kChunk];
 #pragma unroll
@@ -710,15 +714,16 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
 // rounds the phase recurrence with the rotated residual summed per run; the round model of each
 // run from the moments of its channels.  Needs the chunk polynomials (MODE 1 or 2).  Called by all
 // lanes of a warp, as seq_item's single-run items.
-template <int GAUSS, int MODE, bool FIT>
+template <int GAUSS, int MODE, bool FIT, int CI = -1>
 __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, int ng, const RowF* __restrict__ rows,
                                           const float2* __restrict__ data, const float2* __restrict__ sky,
                                           const SeqBatch& b, const SeqGal* sg, uint32_t* dcache, uint16_t* d1cache,
                                           float2* acc) {
   constexpr bool ONE = MODE == 2;
+  constexpr bool FIXED = CI >= 0;
   const int tid = threadIdx.x;
-  const int r = ONE ? t : t % n_rows;
-  const int c0 = ONE ? 0 : (t / n_rows) * kChunk;
+  const int r = ONE ? t : (FIXED ? t - CI * n_rows : t % n_rows);
+  const int c0 = ONE ? 0 : (FIXED ? CI * kChunk : (t / n_rows) * kChunk);
   const int ci = c0 / kChunk;
   const RowF rw = rows[r];
   float pr[kChunk], pi[kChunk];
@@ -812,6 +817,13 @@ __device__ __forceinline__ void seq_item2(int t, bool live, int n_rows, int ng, 
   }
 }
 
+// the chunk of item t if every lane of the warp has an item of that chunk, else -1 (all lanes call)
+__device__ __forceinline__ int uniform_chunk(int t, int n_rows) {
+  const int ci = t / n_rows;
+  const int c0 = __shfl_sync(0xffffffffu, ci, 0);
+  return __all_sync(0xffffffffu, ci == c0) ? c0 : -1;
+}
+
 template <int GAUSS, int MODE, bool FIT>
 __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int n_rows, const RowF* __restrict__ rows,
                                                                 const float2* __restrict__ data,
@@ -859,6 +871,9 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     if (k < ngen) seq_item<GAUSS, false, MODE, FIT>(b.items[total - ngen + k], true, n_rows, nch, ng, rows, data, sky, b, sg, dcache, acc);
   }
   // the two-run and single-run items: 32 consecutive items of the list (neighbours in uv) at a time
+  // MODE 3: the items of a block of the list come from one chunk (the list is in chunk-major
+  // order), so a warp's 32 items almost always share it; such a warp runs the item code compiled
+  // for that chunk, the rare mixed warp the code for any chunk
   if (MODE > 0) {
     const int nt = *b.n_two;
     while (true) {
@@ -867,7 +882,17 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
       base = __shfl_sync(0xffffffffu, base, 0);
       if (base >= nt) break;
       const int q = base + lane;
-      seq_item2<GAUSS, MODE, FIT>(b.items2[min(q, nt - 1)], q < nt, n_rows, ng, rows, data, sky, b, sg, dcache, d1cache, acc);
+      const int t = b.items2[min(q, nt - 1)];
+      const int ci = MODE == 3 ? uniform_chunk(t, n_rows) : -1;
+#define RLF_ITEM2(C) seq_item2<GAUSS, MODE, FIT, C>(t, q < nt, n_rows, ng, rows, data, sky, b, sg, dcache, d1cache, acc)
+      switch (ci) {
+        case 0: RLF_ITEM2(0); break;
+        case 1: RLF_ITEM2(1); break;
+        case 2: RLF_ITEM2(2); break;
+        case 3: RLF_ITEM2(3); break;
+        default: RLF_ITEM2(-1);
+      }
+#undef RLF_ITEM2
     }
   }
   while (true) {
@@ -876,7 +901,17 @@ __global__ void __launch_bounds__(kSeqThreads, kSeqCtasPerSm) k_extract_seq(int 
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= ns) break;
     const int q = base + lane;
-    seq_item<GAUSS, true, MODE, FIT>(b.items[min(q, ns - 1)], q < ns, n_rows, nch, ng, rows, data, sky, b, sg, dcache, acc);
+    const int t = b.items[min(q, ns - 1)];
+    const int ci = MODE == 3 ? uniform_chunk(t, n_rows) : -1;
+#define RLF_ITEM(C) seq_item<GAUSS, true, MODE, FIT, C>(t, q < ns, n_rows, nch, ng, rows, data, sky, b, sg, dcache, acc)
+    switch (ci) {
+      case 0: RLF_ITEM(0); break;
+      case 1: RLF_ITEM(1); break;
+      case 2: RLF_ITEM(2); break;
+      case 3: RLF_ITEM(3); break;
+      default: RLF_ITEM(-1);
+    }
+#undef RLF_ITEM
   }
   __syncthreads();
   double2* out = partial + (size_t)blockIdx.x * b.total_cells;
@@ -900,18 +935,19 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
   int dev = 0;
   cudaGetDevice(&dev);
   const bool known = dev >= 0 && dev < 64;
-  const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+  int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+  if (mode == 1 && g_nch[dev] % kChunk == 0 && g_nch[dev] <= 4 * kChunk) mode = 3;
   // FIT: a correction round (fitted - round model differences to remove); the first round's kernel
   // leaves that path out
-  const void* kernels[2][2][3] = {
+  const void* kernels[2][2][4] = {
       {{(const void*)k_extract_seq<0, 0, false>, (const void*)k_extract_seq<0, 1, false>,
-        (const void*)k_extract_seq<0, 2, false>},
+        (const void*)k_extract_seq<0, 2, false>, (const void*)k_extract_seq<0, 3, false>},
        {(const void*)k_extract_seq<1, 0, false>, (const void*)k_extract_seq<1, 1, false>,
-        (const void*)k_extract_seq<1, 2, false>}},
+        (const void*)k_extract_seq<1, 2, false>, (const void*)k_extract_seq<1, 3, false>}},
       {{(const void*)k_extract_seq<0, 0, true>, (const void*)k_extract_seq<0, 1, true>,
-        (const void*)k_extract_seq<0, 2, true>},
+        (const void*)k_extract_seq<0, 2, true>, (const void*)k_extract_seq<0, 3, true>},
        {(const void*)k_extract_seq<1, 0, true>, (const void*)k_extract_seq<1, 1, true>,
-        (const void*)k_extract_seq<1, 2, true>}}};
+        (const void*)k_extract_seq<1, 2, true>, (const void*)k_extract_seq<1, 3, true>}}};
   const void* kern = kernels[b.fit ? 1 : 0][gaussian ? 1 : 0][mode];
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&data, (void*)&sky, (void*)&b, (void*)&partial};
@@ -998,18 +1034,74 @@ int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, con
 }
 
 // ---------------------------------------------------------------- removal
+// The models of the galaxies sg[0..gn) at one (row, chunk): ar, ai += the round models, br, bi +=
+// the fitted models (flux times profile times the phase exp(+2 pi i T), before the spectral
+// factor).  CI >= 0: the chunk CI (compile-time channel constants, MODE 3); -1: the chunk of ch0.
+template <int GAUSS, int MODE, int CI>
+__device__ __forceinline__ void remove_models(const RowF& rw, int ch0, int nch, const GalF* sg, int gn,
+                                              float (&ar)[kRemCh], float (&ai)[kRemCh], float (&br)[kRemCh],
+                                              float (&bi)[kRemCh]) {
+  constexpr bool POLY = MODE > 0;
+  if (CI >= 0) ch0 = CI * kChunk;
+  for (int i = 0; i < gn; ++i) {
+    const GalF g = sg[i];
+    if (!g.active) continue;
+    const f2 p = delay_df(rw, g);
+    const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
+    const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
+    float zs, zc, ws, wc;
+    sincos_turn_sfu(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
+    sincos_turn(dT.hi + dT.lo, &ws, &wc);
+    float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
+    const float k1q = g.A * (rw.u_hi * rw.u_hi) + g.B * rw.uv + g.Cc * (rw.v_hi * rw.v_hi);
+    float c0p[4], c1p[4];
+    if (POLY) {
+      const float wc2 = c_chunk[ch0 / kChunk].wn2c;
+      profile_poly<GAUSS>(g.sf0 * wc2 * rw.q, c0p);
+      profile_poly<GAUSS>(g.sf1 * wc2 * k1q, c1p);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) { c0p[j] *= g.flux; c1p[j] *= g.flux; }
+    }
+#pragma unroll
+    for (int k = 0; k < kRemCh; ++k) {
+      const int ch = ch0 + k;
+      if (CI >= 0 || ch < nch) {
+        const BatchChan bc = c_bch[ch];
+        float a0, a1;
+        if (POLY) {
+          a0 = poly3(c0p, bc.dl);
+          a1 = poly3(c1p, bc.dl);
+        } else {
+          const float x0 = g.sf0 * bc.wn2 * rw.q;
+          const float x1 = g.sf1 * bc.wn2 * k1q;
+          a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * g.flux;
+          a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * g.flux;
+        }
+        ar[k] = fmaf(a0, zr, ar[k]);
+        ai[k] = fmaf(a0, zi, ai[k]);
+        br[k] = fmaf(a1, zr, br[k]);
+        bi[k] = fmaf(a1, zi, bi[k]);
+        const float nzr = fmaf(zr, wc, -zi * ws);
+        const float nzi = fmaf(zr, ws, zi * wc);
+        zr = nzr;
+        zi = nzi;
+      }
+    }
+  }
+}
+
 // grid-stride over (row, chunk of kRemCh channels); galaxies staged through shared memory in
 // tiles of kRemTile.  Inactive galaxies (bad fits) are skipped.  The channel's spectral factor
 // multiplies the sums over galaxies once, after the galaxy loop.  MODE as k_extract_seq: 0 exact
 // per-channel profiles; 1 the profiles of a chunk from its cubic in dl (profile_poly), one profile
 // evaluation per model, galaxy and chunk; 2 as 1 with exactly one 16-channel chunk (compile-time
-// channel constants).
+// channel constants); 3 as 1 with 2-4 full chunks, a warp whose items share a chunk running the
+// code compiled for that chunk.
 static_assert(kRemCh == kChunk, "removal chunks must be the chunks of the channel polynomials");
 template <int GAUSS, int MODE>
 __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __restrict__ rows, float2* data,
                                                       float2* sky, const GalaxyParams* __restrict__ gals,
                                                       const FitOut* __restrict__ fit, int n_gal) {
-  constexpr bool POLY = MODE > 0;
   constexpr bool ONE = MODE == 2;
   __shared__ GalF sg[kRemTile];
   const int nch = ONE ? kChunk : c_bnch;
@@ -1023,6 +1115,13 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
     const bool live = t < total;
     const int r = live ? (ONE ? (int)t : (int)(t % n_rows)) : 0;
     const int ch0 = ONE ? 0 : (live ? (int)(t / n_rows) * kRemCh : 0);
+    // a warp of one chunk (its lanes without an item count as any chunk)
+    int ci = ONE ? 0 : -1;
+    if (MODE == 3) {
+      const int mine = live ? ch0 / kChunk : -1;
+      const int lead = __reduce_max_sync(0xffffffffu, mine);
+      ci = __all_sync(0xffffffffu, mine == lead || mine < 0) ? lead : -1;
+    }
     RowF rw = rows[r];
     float ar[kRemCh], ai[kRemCh], br[kRemCh], bi[kRemCh];
 #pragma unroll
@@ -1034,50 +1133,12 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
         sg[i] = load_gal(gals[g0 + i], &fit[g0 + i].e1, &fit[g0 + i].error);
       __syncthreads();
       if (!live) continue;
-      for (int i = 0; i < gn; ++i) {
-        const GalF g = sg[i];
-        if (!g.active) continue;
-        const f2 p = delay_df(rw, g);
-        const f2 T0 = turns_mod1(p, c_il0_hi, c_il0_lo);
-        const f2 dT = turns_mod1(p, c_dil_hi, c_dil_lo);
-        float zs, zc, ws, wc;
-        sincos_turn_sfu(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
-        sincos_turn(dT.hi + dT.lo, &ws, &wc);
-        float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
-        const float k1q = g.A * (rw.u_hi * rw.u_hi) + g.B * rw.uv + g.Cc * (rw.v_hi * rw.v_hi);
-        float c0p[4], c1p[4];
-        if (POLY) {
-          const float wc2 = c_chunk[ch0 / kChunk].wn2c;
-          profile_poly<GAUSS>(g.sf0 * wc2 * rw.q, c0p);
-          profile_poly<GAUSS>(g.sf1 * wc2 * k1q, c1p);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) { c0p[j] *= g.flux; c1p[j] *= g.flux; }
-        }
-#pragma unroll
-        for (int k = 0; k < kRemCh; ++k) {
-          const int ch = ch0 + k;
-          if (ch < nch) {
-            const BatchChan bc = c_bch[ch];
-            float a0, a1;
-            if (POLY) {
-              a0 = poly3(c0p, bc.dl);
-              a1 = poly3(c1p, bc.dl);
-            } else {
-              const float x0 = g.sf0 * bc.wn2 * rw.q;
-              const float x1 = g.sf1 * bc.wn2 * k1q;
-              a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * g.flux;
-              a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * g.flux;
-            }
-            ar[k] = fmaf(a0, zr, ar[k]);
-            ai[k] = fmaf(a0, zi, ai[k]);
-            br[k] = fmaf(a1, zr, br[k]);
-            bi[k] = fmaf(a1, zi, bi[k]);
-            const float nzr = fmaf(zr, wc, -zi * ws);
-            const float nzi = fmaf(zr, ws, zi * wc);
-            zr = nzr;
-            zi = nzi;
-          }
-        }
+      switch (MODE == 3 ? ci : -1) {
+        case 0: remove_models<GAUSS, MODE, 0>(rw, ch0, nch, sg, gn, ar, ai, br, bi); break;
+        case 1: remove_models<GAUSS, MODE, 1>(rw, ch0, nch, sg, gn, ar, ai, br, bi); break;
+        case 2: remove_models<GAUSS, MODE, 2>(rw, ch0, nch, sg, gn, ar, ai, br, bi); break;
+        case 3: remove_models<GAUSS, MODE, 3>(rw, ch0, nch, sg, gn, ar, ai, br, bi); break;
+        default: remove_models<GAUSS, MODE, ONE ? 0 : -1>(rw, ch0, nch, sg, gn, ar, ai, br, bi);
       }
     }
     if (!live) continue;
@@ -1108,11 +1169,12 @@ int launch_remove_batch(int n_rows, const RowF* rows, float2* data, float2* sky,
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = sms * 4;
   const bool known = dev >= 0 && dev < 64;
-  const int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
-  const void* kernels[2][3] = {{(const void*)k_remove_batch<0, 0>, (const void*)k_remove_batch<0, 1>,
-                                (const void*)k_remove_batch<0, 2>},
+  int mode = known && g_chunk_poly[dev] ? (g_nch[dev] == kChunk ? 2 : 1) : 0;
+  if (mode == 1 && g_nch[dev] % kChunk == 0 && g_nch[dev] <= 4 * kChunk) mode = 3;
+  const void* kernels[2][4] = {{(const void*)k_remove_batch<0, 0>, (const void*)k_remove_batch<0, 1>,
+                                (const void*)k_remove_batch<0, 2>, (const void*)k_remove_batch<0, 3>},
                                {(const void*)k_remove_batch<1, 0>, (const void*)k_remove_batch<1, 1>,
-                                (const void*)k_remove_batch<1, 2>}};
+                                (const void*)k_remove_batch<1, 2>, (const void*)k_remove_batch<1, 3>}};
   void* args[] = {(void*)&n_rows, (void*)&rows, (void*)&data, (void*)&sky, (void*)&gals, (void*)&fit, (void*)&n_gal};
   const cudaError_t le = cudaLaunchKernel(kernels[gaussian ? 1 : 0][mode], dim3(blocks), dim3(256), args, 0, st);
   if (le != cudaSuccess) { fprintf(stderr, "rlf: k_remove_batch: %s\n", cudaGetErrorString(le)); return (int)le; }

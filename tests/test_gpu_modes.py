@@ -69,8 +69,10 @@ def test_batch_with_large_facet(orc):
     _compare(pr.results, ref, 1e-4, "large facet")
 
 
-def test_batched_two_passes(orc):
-    case = Case(n_ant=48, ha_hours=2.0, dt_s=600.0, n_ch=8, n_gal=16, fmin=10.0, fmax=200.0, noise=1500.0,
+@pytest.mark.parametrize("n_ch", [8, 64])
+def test_batched_two_passes(orc, n_ch):
+    # 64 channels: four full chunks, the extraction and removal code compiled per chunk
+    case = Case(n_ant=48, ha_hours=2.0, dt_s=600.0, n_ch=n_ch, n_gal=16, fmin=10.0, fmax=200.0, noise=1500.0,
                 flag_frac=0.02)
     sky = oracle_sky_model(orc, case)
     d1, s1, nbad, bl, res1 = oracle_data_processing(orc, case, case.data, sky)
@@ -125,12 +127,12 @@ def test_sky_model_and_simulator(orc, gaussian, n_ch):
         assert es < tol and ed < tol
 
 
-@pytest.mark.parametrize("n_ch,gaussian", [(16, 0), (32, 0), (16, 1)])
+@pytest.mark.parametrize("n_ch,gaussian", [(16, 0), (32, 0), (16, 1), (48, 1), (64, 0)])
 def test_batched_full_chunks(orc, n_ch, gaussian):
-    """The batched path on 16 and 32 channels, where most work items are single-run 16-channel
+    """The batched path on 16 to 64 channels, where most work items are single-run 16-channel
     chunks (the kernels' fast path; 16 channels: the single-chunk variant with compile-time channel
-    constants) and the galaxy profiles come from the chunk polynomials, against the oracle's
-    one-galaxy-at-a-time data_processing."""
+    constants; 32-64 channels: the item code compiled for each chunk) and the galaxy profiles come
+    from the chunk polynomials, against the oracle's one-galaxy-at-a-time data_processing."""
     case = Case(n_ant=40, ha_hours=2.0, dt_s=600.0, n_ch=n_ch, n_gal=12, fmin=30.0, fmax=200.0, noise=1500.0,
                 flag_frac=0.01, gaussian=bool(gaussian))
     sky = oracle_sky_model(orc, case)
