@@ -41,6 +41,9 @@ __constant__ BatchChunk c_chunk[kChunks];
 // moments of the channels before and from channel s of a chunk: [chunk][s][0..3] = sum_{k<s},
 // [4..7] = sum_{k>=s} of spec_k dl_k^j (the two runs of a chunk crossing a cell boundary at s)
 __constant__ float c_chunk_split[kChunks][17][8];
+// the channels 2q and 2q + 1 side by side for the packed (two-lane FP32) channel loops:
+// dl of both, then minus the spectral factor of both
+__constant__ float4 c_pair[kMaxCh / 2];
 __constant__ int c_chunk_poly;
 static int g_chunk_poly[64];  // host copy of c_chunk_poly per device (selects the kernel variant)
 static int g_nch[64];         // host copy of c_bnch per device
@@ -72,6 +75,7 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   }
   if (worst * max_delay_m > 1e-9) return -1;
   static BatchChan h[kMaxCh];
+  static float4 hp[kMaxCh / 2];
   static BatchChunk hc[kChunks];
   static float hs[kChunks][17][8];
   double dmax = 0.0;
@@ -113,6 +117,10 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
     }
     k.pad[0] = k.pad[1] = k.pad[2] = 0.f;
   }
+  for (int q = 0; 2 * q < n_ch; ++q) {
+    const int c1 = std::min(2 * q + 1, n_ch - 1);
+    hp[q] = make_float4(h[2 * q].dl, h[c1].dl, -h[2 * q].spec, 2 * q + 1 < n_ch ? -h[c1].spec : 0.f);
+  }
   // truncation of the cubic: below 2.5 dl^4 of the peak (exponential profile; less for the
   // Gaussian one over the range where it is not negligible)
   const int poly = 2.5 * dmax * dmax * dmax * dmax <= 1e-8 ? 1 : 0;
@@ -127,6 +135,8 @@ int batch_set_channels(int n_ch, const double* wavenumbers, const double* spec, 
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk, hc, sizeof(BatchChunk) * ((n_ch + 15) / 16), 0,
                                                      cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_poly, &poly, 4, 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_pair, hp, sizeof(float4) * ((n_ch + 1) / 2), 0,
+                                                     cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_chunk_split, hs, sizeof(float) * 17 * 8 * ((n_ch + 15) / 16), 0,
                                                      cudaMemcpyHostToDevice, st);
   int dev = 0;
@@ -534,6 +544,13 @@ __device__ __forceinline__ void profile_poly(float xc, float cf[4]) {
 }
 __device__ __forceinline__ float poly3(const float c[4], float d) { return fmaf(fmaf(fmaf(c[3], d, c[2]), d, c[1]), d, c[0]); }
 
+// Packed FP32 pairs (the two-lane FMA of this GPU: one instruction for both lanes, each lane
+// rounded as fmaf).  The channel loops below run channels 2q and 2q + 1 side by side, the phase
+// stepping by w^2 from exp(-2 pi i T) at the first two channels.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
 // one work item (row r, channels c0 .. c0 + 15) against every galaxy of the batch, in order.
 // MODE 0: exact per-channel profiles; 1: the profiles from the chunk polynomial, one profile
 // evaluation per galaxy and chunk; 2: as 1 for an observation of exactly one 16-channel chunk, so
@@ -554,15 +571,18 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
   const int c0 = ONE ? 0 : (FIXED ? CI * kChunk : (t / n_rows) * kChunk);
   const int nk = (ONE || FIXED) ? kChunk : min(kChunk, nch - c0);
   const RowF rw = rows[r];
-  float pr[kChunk], pi[kChunk];
+  // the residual of channel c0 + k: real part in rp[k / 2], imaginary part in ip[k / 2] (lane k % 2)
+  float2 rp[kChunk / 2], ip[kChunk / 2];
+#define PR(k) (((k) & 1) ? rp[(k) >> 1].y : rp[(k) >> 1].x)
+#define PI(k) (((k) & 1) ? ip[(k) >> 1].y : ip[(k) >> 1].x)
 #pragma unroll
   for (int k = 0; k < kChunk; ++k) {
-    pr[k] = pi[k] = 0.f;
+    PR(k) = PI(k) = 0.f;
     if (SIMPLE || k < nk) {
       const size_t idx = (size_t)(c0 + k) * n_rows + r;
       const float2 d = data[idx], s = sky[idx];
-      pr[k] = d.x - s.x;
-      pi[k] = d.y - s.y;
+      PR(k) = d.x - s.x;
+      PI(k) = d.y - s.y;
     }
   }
   for (int f = 0; f < b.n_sizes; ++f) dcache[f * kSeqThreads + tid] = b.desc[f][t];
@@ -602,46 +622,72 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
     if (SIMPLE) {
       // one run: all 16 channels valid and in the cell d & 0xffff
       float cr, ci;
-      if (!apply) {
+      if (!apply && POLY) {
+        // sum_k residual_k w^k as two Horner sums in w^2, channels 2q (lane x) and 2q + 1 (lane y),
+        // then the odd one times w
+        const float w2r = fmaf(wr, wr, -wi * wi), w2i = 2.f * wr * wi;
+        const float2 W2R = dup2(w2r), W2I = dup2(w2i), NW2I = dup2(-w2i);
+        float2 SR = make_float2(0.f, 0.f), SI = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = kChunk / 2 - 1; q >= 0; --q) {
+          const float2 nr_ = ffma2(SR, W2R, ffma2(SI, NW2I, rp[q]));
+          const float2 ni_ = ffma2(SR, W2I, ffma2(SI, W2R, ip[q]));
+          SR = nr_;
+          SI = ni_;
+        }
+        const float sr = fmaf(SR.y, wr, fmaf(-SI.y, wi, SR.x));
+        const float si = fmaf(SR.y, wi, fmaf(SI.y, wr, SI.x));
+        const BatchChunk& ck = c_chunk[c0 / kChunk];
+        const float rs = fmaf(c0p[3], ck.mom[3], fmaf(c0p[2], ck.mom[2], fmaf(c0p[1], ck.mom[1], c0p[0] * ck.mom[0])));
+        cr = fmaf(sr, zr0, fmaf(-si, zi0, rs * g.flux));
+        ci = fmaf(sr, zi0, si * zr0);
+      } else if (!apply) {
         float sr = 0.f, si = 0.f, rs = 0.f;
 #pragma unroll
         for (int k = kChunk - 1; k >= 0; --k) {
-          const float nr_ = fmaf(sr, wr, fmaf(-si, wi, pr[k]));
-          const float ni_ = fmaf(sr, wi, fmaf(si, wr, pi[k]));
+          const float nr_ = fmaf(sr, wr, fmaf(-si, wi, PR(k)));
+          const float ni_ = fmaf(sr, wi, fmaf(si, wr, PI(k)));
           sr = nr_;
           si = ni_;
-          if (!POLY) rs = fmaf(profile(g.sf0 * XB(k), GAUSS), c_bch[c0 + k].spec, rs);
-        }
-        if (POLY) {
-          const BatchChunk& ck = c_chunk[c0 / kChunk];
-          rs = fmaf(c0p[3], ck.mom[3], fmaf(c0p[2], ck.mom[2], fmaf(c0p[1], ck.mom[1], c0p[0] * ck.mom[0])));
+          rs = fmaf(profile(g.sf0 * XB(k), GAUSS), c_bch[c0 + k].spec, rs);
         }
         cr = fmaf(sr, zr0, fmaf(-si, zi0, rs * g.flux));
         ci = fmaf(sr, zi0, si * zr0);
       } else if (POLY) {
-        float ar = 0.f, ai = 0.f, zr = zr0, zi = zi0;
+        // channels 2q and 2q + 1 side by side: z = exp(-2 pi i T) as (ZR, NZI = -Im z), stepped by w^2;
+        // the residual rotated and summed (ar, ai), then the galaxy's model difference
+        // a = spec * poly3(dfp, dl) removed from it: residual -= a exp(+2 pi i T)
+        const float w2r = fmaf(wr, wr, -wi * wi), w2i = 2.f * wr * wi;
+        const float2 W2R = dup2(w2r), W2I = dup2(w2i), NW2I = dup2(-w2i);
+        const float z1r = fmaf(zr0, wr, -zi0 * wi), z1i = fmaf(zr0, wi, zi0 * wr);
+        float2 ZR = make_float2(zr0, z1r), NZI = make_float2(-zi0, -z1i);
+        const float2 D0 = dup2(dfp[0]), D1 = dup2(dfp[1]), D2 = dup2(dfp[2]), D3 = dup2(dfp[3]);
+        float2 AR = make_float2(0.f, 0.f), AI = make_float2(0.f, 0.f), BI = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-          ar = fmaf(pr[k], zr, fmaf(-pi[k], zi, ar));
-          ai = fmaf(pr[k], zi, fmaf(pi[k], zr, ai));
-          const float a = c_bch[c0 + k].spec * poly3(dfp, c_bch[c0 + k].dl);
-          pr[k] = fmaf(-a, zr, pr[k]);
-          pi[k] = fmaf(a, zi, pi[k]);
-          const float nzr = fmaf(zr, wr, -zi * wi);
-          const float nzi = fmaf(zr, wi, zi * wr);
-          zr = nzr;
-          zi = nzi;
+        for (int q = 0; q < kChunk / 2; ++q) {
+          AR = ffma2(ip[q], NZI, ffma2(rp[q], ZR, AR));  // + re z re - im z im
+          AI = ffma2(ip[q], ZR, AI);                     // + res im * re z
+          BI = ffma2(rp[q], NZI, BI);                    // - res re * im z
+          const float4 cp = c_pair[c0 / 2 + q];
+          const float2 DL = make_float2(cp.x, cp.y);
+          const float2 AN = fmul2(make_float2(cp.z, cp.w), ffma2(ffma2(ffma2(D3, DL, D2), DL, D1), DL, D0));
+          rp[q] = ffma2(AN, ZR, rp[q]);
+          ip[q] = ffma2(AN, NZI, ip[q]);
+          const float2 nzr = ffma2(NZI, W2I, fmul2(ZR, W2R));
+          const float2 nzi = ffma2(ZR, NW2I, fmul2(NZI, W2R));
+          ZR = nzr;
+          NZI = nzi;
         }
         const BatchChunk& ck = c_chunk[c0 / kChunk];
         const float rs = fmaf(c0p[3], ck.mom[3], fmaf(c0p[2], ck.mom[2], fmaf(c0p[1], ck.mom[1], c0p[0] * ck.mom[0])));
-        cr = fmaf(rs, g.flux, ar);
-        ci = ai;
+        cr = fmaf(rs, g.flux, AR.x + AR.y);
+        ci = (AI.x + AI.y) - (BI.x + BI.y);
       } else {
         float ar = 0.f, ai = 0.f, rs = 0.f, zr = zr0, zi = zi0;
 #pragma unroll
         for (int k = 0; k < kChunk; ++k) {
-          ar = fmaf(pr[k], zr, fmaf(-pi[k], zi, ar));
-          ai = fmaf(pr[k], zi, fmaf(pi[k], zr, ai));
+          ar = fmaf(PR(k), zr, fmaf(-PI(k), zi, ar));
+          ai = fmaf(PR(k), zi, fmaf(PI(k), zr, ai));
           const float spec = c_bch[c0 + k].spec;
           const float xbk = XB(k);
           const float s0 = profile(g.sf0 * xbk, GAUSS);
@@ -649,8 +695,8 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
           rs = fmaf(s0, spec, rs);
           const float a = g.flux * spec * (s1 - s0);
           // residual -= a * exp(+2 pi i T)
-          pr[k] = fmaf(-a, zr, pr[k]);
-          pi[k] = fmaf(a, zi, pi[k]);
+          PR(k) = fmaf(-a, zr, PR(k));
+          PI(k) = fmaf(a, zi, PI(k));
           const float nzr = fmaf(zr, wr, -zi * wi);
           const float nzi = fmaf(zr, wi, zi * wr);
           zr = nzr;
@@ -677,8 +723,8 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
           const float s0 = POLY ? poly3(c0p, c_bch[c0 + k].dl) : profile(g.sf0 * xbk, GAUSS);
           const int c = (mask & (1u << k)) ? (int)cl[(size_t)(c0 + k) * n_rows + r] : (int)cell0;
           if (c != kNoCell) {
-            const float cr = fmaf(pr[k], zr, fmaf(-pi[k], zi, s0 * spec * g.flux));
-            const float ci = fmaf(pr[k], zi, pi[k] * zr);
+            const float cr = fmaf(PR(k), zr, fmaf(-PI(k), zi, s0 * spec * g.flux));
+            const float ci = fmaf(PR(k), zi, PI(k) * zr);
             if (c != cur) {
               if (cur != kNoCell) comp_add2(fac, cur, b.total_cells, ur, ui);
               cur = c;
@@ -692,8 +738,8 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
           if (apply) {
             const float a = POLY ? spec * poly3(dfp, c_bch[c0 + k].dl)
                                  : g.flux * spec * (profile(f1 * xbk, GAUSS) - s0);
-            pr[k] = fmaf(-a, zr, pr[k]);
-            pi[k] = fmaf(a, zi, pi[k]);
+            PR(k) = fmaf(-a, zr, PR(k));
+            PI(k) = fmaf(a, zi, PI(k));
           }
           const float nzr = fmaf(zr, wr, -zi * wi);
           const float nzi = fmaf(zr, wi, zi * wr);
@@ -705,6 +751,8 @@ __device__ __forceinline__ void seq_item(int t, bool live, int n_rows, int nch, 
     }
   }
 #undef XB
+#undef PR
+#undef PI
 }
 
 // one work item whose chunk is, for every facet size of the batch, one run or two runs: channels
@@ -1036,11 +1084,13 @@ int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, con
 // ---------------------------------------------------------------- removal
 // The models of the galaxies sg[0..gn) at one (row, chunk): ar, ai += the round models, br, bi +=
 // the fitted models (flux times profile times the phase exp(+2 pi i T), before the spectral
-// factor).  CI >= 0: the chunk CI (compile-time channel constants, MODE 3); -1: the chunk of ch0.
+// factor), channel c0 + k in lane k % 2 of element k / 2.  CI >= 0: the chunk CI (compile-time
+// channel constants, MODE 3); -1: the chunk of ch0.  With the chunk polynomials the channels 2q and
+// 2q + 1 run side by side in packed FP32 pairs, the phase stepping by w^2.
 template <int GAUSS, int MODE, int CI>
 __device__ __forceinline__ void remove_models(const RowF& rw, int ch0, int nch, const GalF* sg, int gn,
-                                              float (&ar)[kRemCh], float (&ai)[kRemCh], float (&br)[kRemCh],
-                                              float (&bi)[kRemCh]) {
+                                              float2 (&ar)[kRemCh / 2], float2 (&ai)[kRemCh / 2],
+                                              float2 (&br)[kRemCh / 2], float2 (&bi)[kRemCh / 2]) {
   constexpr bool POLY = MODE > 0;
   if (CI >= 0) ch0 = CI * kChunk;
   for (int i = 0; i < gn; ++i) {
@@ -1052,39 +1102,62 @@ __device__ __forceinline__ void remove_models(const RowF& rw, int ch0, int nch, 
     float zs, zc, ws, wc;
     sincos_turn_sfu(ch0 == 0 ? T0.hi + T0.lo : turns_at(T0, dT, ch0), &zs, &zc);
     sincos_turn(dT.hi + dT.lo, &ws, &wc);
-    float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
     const float k1q = g.A * (rw.u_hi * rw.u_hi) + g.B * rw.uv + g.Cc * (rw.v_hi * rw.v_hi);
-    float c0p[4], c1p[4];
     if (POLY) {
+      float c0p[4], c1p[4];
       const float wc2 = c_chunk[ch0 / kChunk].wn2c;
       profile_poly<GAUSS>(g.sf0 * wc2 * rw.q, c0p);
       profile_poly<GAUSS>(g.sf1 * wc2 * k1q, c1p);
+      const float2 E0 = dup2(c0p[0] * g.flux), E1 = dup2(c0p[1] * g.flux), E2 = dup2(c0p[2] * g.flux),
+                   E3 = dup2(c0p[3] * g.flux);
+      const float2 F0 = dup2(c1p[0] * g.flux), F1 = dup2(c1p[1] * g.flux), F2 = dup2(c1p[2] * g.flux),
+                   F3 = dup2(c1p[3] * g.flux);
+      // z = exp(+2 pi i T) at channels ch0 + 2q (lane x) and ch0 + 2q + 1 (lane y), stepped by w^2
+      const float w2r = fmaf(wc, wc, -ws * ws), w2i = 2.f * wc * ws;
+      const float2 W2R = dup2(w2r), W2I = dup2(w2i), NW2I = dup2(-w2i);
+      float2 ZR = make_float2(zc, fmaf(zc, wc, -zs * ws)), ZI = make_float2(zs, fmaf(zc, ws, zs * wc));
 #pragma unroll
-      for (int j = 0; j < 4; ++j) { c0p[j] *= g.flux; c1p[j] *= g.flux; }
-    }
+      for (int q = 0; q < kRemCh / 2; ++q) {
+        if (CI >= 0 || ch0 + 2 * q < nch) {
+          const float4 cp = c_pair[ch0 / 2 + q];
+          const float2 DL = make_float2(cp.x, cp.y);
+          const float2 a0 = ffma2(ffma2(ffma2(E3, DL, E2), DL, E1), DL, E0);
+          const float2 a1 = ffma2(ffma2(ffma2(F3, DL, F2), DL, F1), DL, F0);
+          ar[q] = ffma2(a0, ZR, ar[q]);
+          ai[q] = ffma2(a0, ZI, ai[q]);
+          br[q] = ffma2(a1, ZR, br[q]);
+          bi[q] = ffma2(a1, ZI, bi[q]);
+          const float2 nzr = ffma2(ZI, NW2I, fmul2(ZR, W2R));
+          const float2 nzi = ffma2(ZR, W2I, fmul2(ZI, W2R));
+          ZR = nzr;
+          ZI = nzi;
+        }
+      }
+    } else {
+      float zr = zc, zi = zs;  // exp(+2 pi i T): the model phase
 #pragma unroll
-    for (int k = 0; k < kRemCh; ++k) {
-      const int ch = ch0 + k;
-      if (CI >= 0 || ch < nch) {
-        const BatchChan bc = c_bch[ch];
-        float a0, a1;
-        if (POLY) {
-          a0 = poly3(c0p, bc.dl);
-          a1 = poly3(c1p, bc.dl);
-        } else {
+      for (int k = 0; k < kRemCh; ++k) {
+        const int ch = ch0 + k;
+        if (ch < nch) {
+          const BatchChan bc = c_bch[ch];
           const float x0 = g.sf0 * bc.wn2 * rw.q;
           const float x1 = g.sf1 * bc.wn2 * k1q;
-          a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * g.flux;
-          a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * g.flux;
+          const float a0 = (GAUSS ? __expf(-0.5f * x0) : round_shape(x0)) * g.flux;
+          const float a1 = (GAUSS ? __expf(-0.5f * x1) : round_shape(x1)) * g.flux;
+          float2& A = ar[k >> 1];
+          float2& B = ai[k >> 1];
+          float2& C = br[k >> 1];
+          float2& D = bi[k >> 1];
+          if (k & 1) {
+            A.y = fmaf(a0, zr, A.y); B.y = fmaf(a0, zi, B.y); C.y = fmaf(a1, zr, C.y); D.y = fmaf(a1, zi, D.y);
+          } else {
+            A.x = fmaf(a0, zr, A.x); B.x = fmaf(a0, zi, B.x); C.x = fmaf(a1, zr, C.x); D.x = fmaf(a1, zi, D.x);
+          }
+          const float nzr = fmaf(zr, wc, -zi * ws);
+          const float nzi = fmaf(zr, ws, zi * wc);
+          zr = nzr;
+          zi = nzi;
         }
-        ar[k] = fmaf(a0, zr, ar[k]);
-        ai[k] = fmaf(a0, zi, ai[k]);
-        br[k] = fmaf(a1, zr, br[k]);
-        bi[k] = fmaf(a1, zi, bi[k]);
-        const float nzr = fmaf(zr, wc, -zi * ws);
-        const float nzi = fmaf(zr, ws, zi * wc);
-        zr = nzr;
-        zi = nzi;
       }
     }
   }
@@ -1123,9 +1196,9 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
       ci = __all_sync(0xffffffffu, mine == lead || mine < 0) ? lead : -1;
     }
     RowF rw = rows[r];
-    float ar[kRemCh], ai[kRemCh], br[kRemCh], bi[kRemCh];
+    float2 ar[kRemCh / 2], ai[kRemCh / 2], br[kRemCh / 2], bi[kRemCh / 2];
 #pragma unroll
-    for (int k = 0; k < kRemCh; ++k) { ar[k] = ai[k] = br[k] = bi[k] = 0.f; }
+    for (int q = 0; q < kRemCh / 2; ++q) ar[q] = ai[q] = br[q] = bi[q] = make_float2(0.f, 0.f);
     for (int g0 = 0; g0 < n_gal; g0 += kRemTile) {
       const int gn = min(kRemTile, n_gal - g0);
       __syncthreads();
@@ -1148,13 +1221,16 @@ __global__ void __launch_bounds__(256) k_remove_batch(int n_rows, const RowF* __
       if (ch < nch) {
         const size_t idx = (size_t)ch * n_rows + r;
         const float spec = c_bch[ch].spec;
+        const int q = k >> 1;
+        const float mr = (k & 1) ? ar[q].y : ar[q].x, mi = (k & 1) ? ai[q].y : ai[q].x;
+        const float fr = (k & 1) ? br[q].y : br[q].x, fi = (k & 1) ? bi[q].y : bi[q].x;
         float2 s = sky[idx];
-        s.x = fmaf(-spec, ar[k], s.x);
-        s.y = fmaf(-spec, ai[k], s.y);
+        s.x = fmaf(-spec, mr, s.x);
+        s.y = fmaf(-spec, mi, s.y);
         sky[idx] = s;
         float2 d = data[idx];
-        d.x = fmaf(-spec, br[k], d.x);
-        d.y = fmaf(-spec, bi[k], d.y);
+        d.x = fmaf(-spec, fr, d.x);
+        d.y = fmaf(-spec, fi, d.y);
         data[idx] = d;
       }
     }
