@@ -462,6 +462,22 @@ __device__ __forceinline__ void comp_add2(float2* fac, int k, int lo_off, float 
 // lo accumulators).  All 32 lanes must call it.
 __device__ __forceinline__ void warp_deposit(float2* fac, int lo_off, int key, float vr, float vi, int lane) {
   const unsigned mag = max(__float_as_uint(fabsf(vr)), __float_as_uint(fabsf(vi)));  // NaN above inf
+  // the common case, every lane in one cell: the first group of the loop below without its
+  // bookkeeping (the same sums and the same deposit)
+  const int k0 = __shfl_sync(0xffffffffu, key, 0);
+  if (__all_sync(0xffffffffu, key == k0) && k0 >= 0) {
+    const int e = (int)(__reduce_max_sync(0xffffffffu, mag) >> 23);
+    if (e >= 24 && e < 255) {
+      const float sc = __uint_as_float((unsigned)(278 - e) << 23);
+      const float inv = __uint_as_float((unsigned)(e - 24) << 23);
+      const int sr = __reduce_add_sync(0xffffffffu, __float2int_rn(vr * sc));
+      const int si = __reduce_add_sync(0xffffffffu, __float2int_rn(vi * sc));
+      if (lane == 0) comp_add2(fac, k0, lo_off, (float)sr * inv, (float)si * inv);
+    } else {
+      comp_add2(fac, key, lo_off, vr, vi);
+    }
+    return;
+  }
   unsigned todo = __ballot_sync(0xffffffffu, key >= 0), rest = 0;
 #pragma unroll 1
   for (int it = 0; it < 4 && todo; ++it) {
