@@ -370,11 +370,11 @@ def cpu_baseline(obs, cat, data_h, sky_h, n_sample, gpu_first):
 
 # DRAM bytes of one k_extract_seq launch per algorithmic byte, from the ncu capture of
 # profiles/k_extract_seq_mid_128ant_64ch.md (the full-scale channel layout; the mean of its first
-# round and two correction rounds): dram__bytes_read.sum + dram__bytes_write.sum = 1215.2 MB + 16.4 MB
+# round and two correction rounds): dram__bytes_read.sum + dram__bytes_write.sum = 1214.0 MB + 16.3 MB
 # against 16 B per visibility (975,360 rows x 64 channels) + 32 B per row.  A launch reads data and
 # sky model once per visibility and the row table, work items and run descriptors once per (row,
 # 16-channel chunk), so its traffic grows with those units.
-EXTRACT_DRAM_PER_ALG_BYTE = (1215.157e6 + 16.409515e6) / (975360 * 64 * 16 + 975360 * 32)
+EXTRACT_DRAM_PER_ALG_BYTE = (1214.021e6 + 16.319915e6) / (975360 * 64 * 16 + 975360 * 32)
 EXTRACT_TRAFFIC_SOURCE = ("ncu DRAM bytes of one k_extract_seq launch on mid_128ant_64ch "
                           "(profiles/k_extract_seq_mid_128ant_64ch.md) per algorithmic byte, times this "
                           "launch's algorithmic bytes")
