@@ -216,7 +216,7 @@ int rlf_obs_remove(rlf_observation *obs, int n_gal, const double *flux, const do
  * facet (visibility / flux re and im, cell mask, cell SNR) and proposes (e1, e2, ln r, ln sigma);
  * a galaxy with sigma <= max_sigma (rlf_proposal_set_max_sigma, default 0.05) starts its fit at
  * (e1, e2) with step 2 sigma (at least 0.02), the others at the reference's (0, 0) with step 0.1;
- * the fit stays the judge.  Parameters:
+ * the fit keeps the last word.  Parameters:
  * rlf_cnn_param_count() floats, per convolution W[32][9 cin] (k = (3 ky + kx) cin + ci) and b[32],
  * then the head's W[4][512] (feature (4 y + x) 32 + c) and b[4]. */
 typedef struct rlf_cnn rlf_cnn;

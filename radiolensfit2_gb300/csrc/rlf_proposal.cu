@@ -1,7 +1,7 @@
 // Learned proposal of the simplex start: a small convolutional network reads a 64 x 64 resampling of
 // each galaxy's facet and proposes (e1, e2, ln r) and a step scale for the fit's nmsimplex2, whose
-// start the reference fixes at (0, 0) with step 0.1 (galaxy_fitting.c:59-65).  The fit stays the
-// judge: it starts from the proposal and converges to the likelihood maximum as before.  No
+// start the reference fixes at (0, 0) with step 0.1 (galaxy_fitting.c:59-65).  The fit keeps the
+// last word: it starts from the proposal and converges to the likelihood maximum as before.  No
 // counterpart in the reference.
 //
 // Network (NHWC bf16 activations, FP32 accumulation):

@@ -14,7 +14,7 @@ this module drives them:
   ``DeviceObservation.process(..., proposal=1)`` starts every fit at the proposal.
 
 The reference's fit starts every galaxy at (0, 0) with step 0.1 (galaxy_fitting.c:59-65); the
-fit itself is unchanged and judges every proposal.
+fit itself is unchanged and has the last word on every proposal.
 """
 from __future__ import annotations
 
