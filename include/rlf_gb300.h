@@ -195,8 +195,9 @@ int rlf_obs_last_stats(rlf_observation *obs, long long *stats);
  * (data_processing-mpi.c:65-216), one process per GPU holding its own channels:
  * rlf_obs_facet_partials: every galaxy's facet sums over this observation's channels, un-averaged,
  *   out[g][4][stride] = sum of vis re, sum of vis im, sum of sigma^2, sum of weights per cell of the
- *   galaxy's F x F facet (row-major, F^2 <= stride; the rest zero), extracted against the current
- *   data and sky model as source_extraction does (evaluate_uv_grid.c:143-195 before averaging);
+ *   galaxy's F x F facet (row-major, F^2 <= stride; the rest zero), every galaxy extracted against
+ *   the current data and sky model as source_extraction does (evaluate_uv_grid.c:143-195 before
+ *   averaging); FP32 observations in batches (the sequential extraction's first round);
  * rlf_fit_partials: the facets of the summed partials of all shards (average_facets,
  *   evaluate_facet_coords), fitted together by the persistent fit kernel: source_fitting's results;
  * rlf_obs_remove: removal of the given fits from this observation's data and sky model, in order,

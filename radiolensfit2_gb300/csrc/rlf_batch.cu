@@ -1091,6 +1091,44 @@ __global__ void k_finalize_seq(SeqBatch b, int ctas, const double2* __restrict__
   if (threadIdx.x == 0) out.ncoords[slot] = base;
 }
 
+// one block per galaxy of the batch: the un-averaged facet sums of a channel shard, out[slot][4][stride]
+// = (sum of vis re, sum of vis im, sum of sigma^2, sum of weights) per cell of the galaxy's F x F
+// facet in row-major order (evaluate_uv_grid.c:143-195 before the averaging of :196-209), FP64 sums
+// of the CTA partials in CTA order; cells F^2 .. stride - 1 zero
+__global__ void k_partials_seq(SeqBatch b, int ctas, const double2* __restrict__ partial,
+                               const double* const* __restrict__ ss_of, const double* const* __restrict__ sw_of,
+                               double* __restrict__ out, int stride) {
+  const int slot = blockIdx.x;
+  if (slot >= b.n_gal) return;
+  const int F = b.facet[slot], off = b.foff[slot];
+  const int nc = F * F;
+  const double* ss = ss_of[slot];
+  const double* sw = sw_of[slot];
+  double* row = out + (size_t)slot * 4 * stride;
+  for (int c = threadIdx.x; c < stride; c += blockDim.x) {
+    double sre = 0.0, sim = 0.0, s2 = 0.0, w = 0.0;
+    if (c < nc) {
+      for (int p = 0; p < ctas; ++p) {
+        const double2 v = partial[(size_t)p * b.total_cells + off + c];
+        sre += v.x;
+        sim += v.y;
+      }
+      s2 = ss[c];
+      w = sw[c];
+    }
+    row[c] = sre;
+    row[stride + c] = sim;
+    row[2 * stride + c] = s2;
+    row[3 * stride + c] = w;
+  }
+}
+
+int launch_partials_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
+                        const double* const* sw, double* out, int stride, cudaStream_t st) {
+  k_partials_seq<<<b.n_gal, 256, 0, st>>>(b, ctas, partial, ss, sw, out, stride);
+  return check("k_partials_seq");
+}
+
 int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
                         const double* const* sw, double len, FacetOut out, cudaStream_t st) {
   k_finalize_seq<<<b.n_gal, 256, 0, st>>>(b, ctas, partial, ss, sw, len, out);

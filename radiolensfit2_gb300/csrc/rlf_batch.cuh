@@ -97,6 +97,10 @@ int launch_extract_seq(int n_rows, const RowF* rows, const float2* data, const f
 // finalisation and compaction into out (slot = galaxy index in the batch)
 int launch_finalize_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
                         const double* const* sw, double len, FacetOut out, cudaStream_t st);
+// the un-averaged facet sums of every galaxy of the batch (channel shards): out[slot][4][stride] =
+// sum of vis re, sum of vis im, sum of sigma^2, sum of weights per cell, zero beyond F^2
+int launch_partials_seq(const SeqBatch& b, int ctas, const double2* partial, const double* const* ss,
+                        const double* const* sw, double* out, int stride, cudaStream_t st);
 // vis += the round models (sheared = 0: the sky model) or the sheared models (sheared = 1: the
 // simulator) of n_gal galaxies, FP32 visibilities, evenly spaced channels (batch_set_channels)
 int launch_model_sum_batch(int n_rows, const RowF* rows, float2* vis, const GalaxyParams* gals, int n_gal,

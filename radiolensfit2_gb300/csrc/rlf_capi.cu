@@ -381,7 +381,7 @@ __global__ void k_count_changed(int n, const FitOut* a, const FitOut* b, double 
 static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, const std::vector<int>& order,
                     int numr, const double* ro, const rlf_options& opt, std::vector<FitOut>& out,
                     cudaStream_t st, double* ms3, double* facets_out = nullptr, int* ncoords_out = nullptr,
-                    int facets_stride = 0) {
+                    int facets_stride = 0, double* partials_out = nullptr, int partials_stride = 0) {
   const int n = (int)order.size();
   out.assign(n, FitOut{});
   if (n == 0) return 0;
@@ -389,7 +389,10 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   const Precision prec = (ob->precision == RLF_F64) ? kF64 : kMixed;   // visibility passes
   const Precision fprec = (opt.fit_precision == RLF_MIXED) ? kMixed : kF64;  // the fit
   const int B = opt.batch > 0 ? opt.batch : 1;
-  const int rounds = facets_out ? 1 : (opt.rounds > 0 ? opt.rounds : 3);
+  // extraction only (one round, no fit or removal): the packed facets (facets_out) or the
+  // un-averaged facet sums of a channel shard (partials_out)
+  const bool extract_only = facets_out || partials_out;
+  const int rounds = extract_only ? 1 : (opt.rounds > 0 ? opt.rounds : 3);
   const Observation o = ob->view();
   unsigned fmax = 0;
   for (int i = 0; i < n; ++i) fmax = std::max<unsigned>(fmax, (unsigned)gals[order[i]].facet);
@@ -481,7 +484,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   RLF_OK(dfoff.upload(foff.data(), n, st));
   RLF_OK(dfac.upload(facets.data(), n, st));
   // learned proposal of the simplex starts: computed on the device from each round's facets
-  const bool learned = !opt.start && opt.proposal && proposal_ready() && !facets_out;
+  const bool learned = !opt.start && opt.proposal && proposal_ready() && !extract_only;
   if (learned) RLF_OK(dstart.ensure((size_t)3 * n));
   if (opt.start) {
     std::vector<double> sv((size_t)3 * n);
@@ -497,7 +500,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   DevBuf<SampleSlot> bslot;
   DevBuf<double> bL;
   DevBuf<int> berr, bflag, bnewton, bdone;
-  if (!facets_out) {
+  if (!extract_only) {
     RLF_OK(bslot.ensure(max_unit));
     RLF_OK(bL.ensure((size_t)max_unit * 2 * kBoardCap));
     RLF_OK(berr.ensure((size_t)max_unit * 2 * kBoardCap));
@@ -522,6 +525,8 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
   DevBuf<unsigned char> cells;
   const size_t plane = (size_t)max_unit * max_cells * esz;
   RLF_OK(cells.ensure(5 * plane));
+  DevBuf<double> dpart;  // [max_unit][4][partials_stride] un-averaged facet sums of a unit
+  if (partials_out) RLF_OK(dpart.ensure((size_t)max_unit * 4 * partials_stride));
   void* gu = cells.p;
   void* gv = cells.p + plane;
   void* dre = cells.p + 2 * plane;
@@ -621,7 +626,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
     // CUDA graph of the sub-batch: every round (round control, extraction, finalisation, proposal,
     // fit) and the removal are captured from the stream and launched as one graph, the host never
     // waiting within the sub-batch (rlf_options.graphs)
-    const bool graph = u.seq && opt.graphs && !facets_out;
+    const bool graph = u.seq && opt.graphs && !extract_only;
     if (graph) RLF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     // Galaxies [j0, bn) of the unit take part in a round.  Round r+1 extracts galaxy k with the
     // fitted - round model differences of round r's good fits among the galaxies before k, round r
@@ -660,7 +665,11 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         RLF_OK(launch_extract_seq(ob->n_rows, ob->rows.p, ob->data32.p, ob->sky32.p, sr, opt.gaussian, seq_ctas,
                                   ob->bpartial.p, st));
         RLF_OK(pt.mark(kPhaseExtractSeq, st));
-        RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, ob->len, fq, st));
+        if (partials_out)
+          RLF_OK(launch_partials_seq(sr, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, dpart.p, partials_stride,
+                                     st));
+        else
+          RLF_OK(launch_finalize_seq(sr, seq_ctas, ob->bpartial.p, dss.p + b0, dsw.p + b0, ob->len, fq, st));
       } else {
         const int i = b0;
         const unsigned F = (unsigned)facets[i];
@@ -674,10 +683,21 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
                                       ob->partial.p, ob->n_part, st));
         double* sums = ob->partial.p + (size_t)ob->n_part * 2 * F * F;
         RLF_OK(launch_reduce_partials(ob->partial.p, ob->n_part, 2 * F * F, sums, st));
-        RLF_OK(launch_facet_finalize(1, dfac.p + i, sums, 1, 0, dss.p + i, dsw.p + i, ob->len, fo, st));
+        if (partials_out) {
+          const size_t nc = (size_t)F * F;
+          RLF_CUDA(cudaMemsetAsync(dpart.p, 0, (size_t)4 * partials_stride * sizeof(double), st));
+          RLF_CUDA(copy_async(dpart.p, sums, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+          RLF_CUDA(copy_async(dpart.p + partials_stride, sums + nc, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+          RLF_CUDA(copy_async(dpart.p + 2 * partials_stride, cache[i]->ss.p, nc * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st));
+          RLF_CUDA(copy_async(dpart.p + 3 * partials_stride, cache[i]->sw.p, nc * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st));
+        } else {
+          RLF_OK(launch_facet_finalize(1, dfac.p + i, sums, 1, 0, dss.p + i, dsw.p + i, ob->len, fo, st));
+        }
       }
       RLF_OK(pt.mark(kPhaseExtract, st));
-      if (facets_out) break;
+      if (extract_only) break;
       // ---- fit
       if (learned) {
         static_assert(sizeof(GalaxyParams) % sizeof(double) == 0, "GalaxyParams holds whole doubles");
@@ -710,6 +730,15 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
         RLF_CUDA(cudaGetLastError());
       }
       RLF_OK(pt.mark(kPhaseFit, st));
+    }
+    if (partials_out) {
+      // a channel shard's un-averaged facet sums of this unit, in the caller's galaxy order
+      for (int k = 0; k < bn; ++k)
+        RLF_CUDA(copy_async(partials_out + (size_t)order[b0 + k] * 4 * partials_stride,
+                            dpart.p + (size_t)k * 4 * partials_stride, (size_t)4 * partials_stride * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+      RLF_CUDA(cudaStreamSynchronize(st));  // dpart is reused by the next unit
+      continue;
     }
     if (facets_out) {
       // extraction only: hand the packed facets of this unit back as doubles
@@ -758,7 +787,7 @@ static int run_pass(rlf_observation* ob, const std::vector<GalaxyParams>& gals, 
       ob->stats[RLF_STAT_GRAPHS] += 1;
     }
   }
-  if (!facets_out) RLF_OK(dout.download(out.data(), n, st));
+  if (!extract_only) RLF_OK(dout.download(out.data(), n, st));
   unsigned long long changed = 0;
   if (dchanged.p) RLF_CUDA(copy_async(&changed, dchanged.p, sizeof(changed), cudaMemcpyDeviceToHost, st));
   long long hstats[RLF_NSTATS];
@@ -1378,39 +1407,23 @@ int rlf_obs_extract(rlf_observation* obs, int n_gal, const double* flux, const d
 int rlf_obs_facet_partials(rlf_observation* obs, int n_gal, const double* flux, const double* scale,
                            const double* l, const double* m, double* out, int stride) {
   if (!obs || n_gal < 0 || (n_gal && !out)) return 1;
+  if (n_gal == 0) return 0;
   cudaStream_t st;
   RLF_OK(lib_stream(&st));
   RLF_OK(set_channels(obs->n_ch, obs->wavenumbers.data(), obs->spec.data(), st));
   const unsigned fmax = rlf::facet_size(kRMax, obs->len);
   if ((unsigned)stride < fmax * fmax) { fprintf(stderr, "rlf: partials stride %d below %u\n", stride, fmax * fmax); return 1; }
   std::vector<GalaxyParams> gals = make_gals(n_gal, flux, scale, nullptr, nullptr, l, m, obs->len, fmax);
-  DevBuf<GalaxyParams> dg;
-  RLF_OK(dg.upload(gals.data(), n_gal, st));
-  RLF_OK(obs->partial.ensure((size_t)obs->n_part * 4 * fmax * fmax + 4 * fmax * fmax));
-  const Observation o = obs->view();
-  for (int g = 0; g < n_gal; ++g) {
-    const unsigned F = (unsigned)gals[g].facet;
-    const int nc = (int)(F * F);
-    FacetCache* fc = nullptr;
-    RLF_OK(obs_facet(obs, F, &fc, st));
-    if (obs->precision == RLF_F64)
-      RLF_OK(launch_extract_f64(o, obs->data64.p, obs->sky64.p, fc->cell.p, dg.p + g, F, g_lib.opt.gaussian,
-                                obs->partial.p, obs->n_part, st));
-    else
-      RLF_OK(launch_extract_mixed(o, obs->data32.p, obs->sky32.p, fc->cell.p, dg.p + g, F, g_lib.opt.gaussian,
-                                  obs->partial.p, obs->n_part, st));
-    double* sums = obs->partial.p + (size_t)obs->n_part * 2 * nc;
-    RLF_OK(launch_reduce_partials(obs->partial.p, obs->n_part, 2 * nc, sums, st));
-    double* row = out + (size_t)g * 4 * stride;
-    RLF_CUDA(copy_async(row, sums, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RLF_CUDA(copy_async(row + stride, sums + nc, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RLF_CUDA(copy_async(row + 2 * stride, fc->ss.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RLF_CUDA(copy_async(row + 3 * stride, fc->sw.p, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RLF_CUDA(cudaStreamSynchronize(st));  // `sums` is reused by the next galaxy
-    for (int a = 0; a < 4; ++a)
-      for (int c = nc; c < stride; ++c) row[(size_t)a * stride + c] = 0.0;
-  }
-  return 0;
+  std::vector<int> order(n_gal);
+  for (int i = 0; i < n_gal; ++i) order[i] = i;
+  // every galaxy extracted against the same data (no removal in between): FP32 observations take the
+  // sequential batch extraction's first round for sub-batches of galaxies, FP64 ones (and galaxies
+  // with facets beyond the batched kernels) one pass per galaxy
+  rlf_options o = g_lib.opt;
+  o.batch = kSeqMaxGal;
+  std::vector<FitOut> res;
+  std::vector<double> ro(kMaxNodes, 1.0);
+  return run_pass(obs, gals, order, 24, ro.data(), o, res, st, nullptr, nullptr, nullptr, 0, out, stride);
 }
 
 int rlf_fit_partials(int n_gal, const double* partials, int stride, const double* flux, const double* scale,

@@ -58,3 +58,42 @@ def test_channel_shards_match_unsharded_and_oracle():
         assert np.max(np.abs(data - d_ref2[sl])) < 1e-11 * np.max(np.abs(d_ref2))
         assert np.max(np.abs(skym - s_ref2[sl])) < 1e-11 * np.max(np.abs(sky))
         d.close()
+
+
+def test_mixed_partials_batched():
+    """FP32 observations extract the partials with the sequential batch extraction's first round
+    (every galaxy against the same data): against the FP64 observation's partials of the same
+    FP32-representable data (weights and variance sums equal, the sums within 2e-6 of their
+    largest magnitude), and the sum of three 16-channel shards against the unsharded 48-channel
+    observation (another chunking of the FP32 channel passes: the same bound)."""
+    orc = O.load_oracle()
+    case = Case(n_ant=40, ha_hours=2.0, dt_s=600.0, n_ch=48, n_gal=12, fmin=30.0, fmax=200.0, noise=1500.0,
+                flag_frac=0.01)
+    o = case.obs
+    data = case.data.astype(np.complex64).astype(np.complex128)
+    sky = oracle_sky_model(orc, case).astype(np.complex64).astype(np.complex128)
+    stride = K.facet_size(K.RMAX, case.len) ** 2
+    parts = {}
+    for name, prec in (("f64", _lib.RLF_F64), ("mixed", _lib.RLF_MIXED)):
+        d = DeviceObservation(o, precision=prec, sigma2=case.sigma2, flag=case.flag)
+        d.set_vis(data, sky)
+        parts[name] = d.facet_partials(case.cat, stride)
+        d.close()
+    shards = []
+    for r in range(3):
+        so, (lo, hi) = shard.shard_observation(o, 3, r)
+        sl = slice(lo * o.n_rows, hi * o.n_rows)
+        d = DeviceObservation(so, precision=_lib.RLF_MIXED, sigma2=case.sigma2[sl], flag=case.flag[sl])
+        d.set_vis(data[sl], sky[sl])
+        shards.append(d.facet_partials(case.cat, stride))
+        d.close()
+    parts["shards"] = shard.LocalExchange().allreduce(shards)
+    ref = parts["f64"]
+    for name in ("mixed", "shards"):
+        P = parts[name]
+        assert np.array_equal(P[:, 3], ref[:, 3]), name
+        assert np.allclose(P[:, 2], ref[:, 2], rtol=1e-14, atol=0.0), name
+        for a in range(2):
+            err = np.max(np.abs(P[:, a] - ref[:, a]))
+            print(f"{name} component {a}: max |d| {err:.3e} of {np.max(np.abs(ref[:, a])):.3e}")
+            assert err <= 2e-6 * np.max(np.abs(ref[:, a])), name
