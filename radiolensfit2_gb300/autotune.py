@@ -25,7 +25,7 @@ import numpy as np
 
 from . import constants as K
 
-CANDIDATES = tuple(dict(seq_facet_kb=kb, fit_ctas_per_sm=c) for kb in (64, 96, 128, 160) for c in (2, 3))
+CANDIDATES = tuple(dict(seq_facet_kb=kb, fit_ctas_per_sm=c) for kb in (96, 128, 160, 192) for c in (2, 3))
 _cache: dict = {}
 
 
